@@ -1,0 +1,174 @@
+/* pisurf.h - C ABI of the GB300-native particle-isosurface library.
+ *
+ * This is the drop-in boundary for the field-evaluation + octree-meshing
+ * path of LCM1999/ParticleIsosurface.  The reference exposes that path as
+ * in-process C++ classes (no plugin or FFI layer); each entry point below
+ * names the reference interface it replaces.  Plain pointers and sizes only.
+ *
+ * Conventions
+ *  - Every call returns PI_OK (0) or a negative PI_ERR_* code; the message of
+ *    the last error on the calling thread is returned by pi_last_error().
+ *  - Host pointers are caller-owned and only read/written during the call.
+ *  - A frame is used by one thread at a time; frames of one context share its
+ *    CUDA stream, so their work is ordered.
+ *  - All computation runs on the GPU.  There is no CPU fallback: without a
+ *    usable CUDA device every call that computes returns PI_ERR_CUDA.
+ *  - Constant particle radius, anisotropic cubic B-spline kernel
+ *    (the reference's USE_ANI=1, USE_POLY6=0, CALC_P_NORMAL=1,
+ *    src/main.cpp:29-52).
+ */
+#ifndef PISURF_H
+#define PISURF_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PI_OK 0
+#define PI_ERR_INVALID (-1) /* bad argument: null pointer, n <= 0, non-finite position, ... */
+#define PI_ERR_CUDA (-2)    /* CUDA runtime error (message in pi_last_error) */
+#define PI_ERR_NOMEM (-3)   /* device memory budget of the context exceeded */
+#define PI_ERR_STATE (-4)   /* stage called before the stages it depends on */
+#define PI_ERR_LIMIT (-5)   /* size limit: >= 2^31 hash cells, octree depth > 20, ... */
+
+typedef struct pi_ctx pi_ctx;
+typedef struct pi_frame pi_frame;
+
+/* Reconstruction parameters: the reference's SurfReconstructor arguments and
+ * Run(iso_factor, smooth_factor) (include/surface_reconstructor.h:71-79). */
+typedef struct pi_params {
+  float radius;        /* particle radius r (RADIUS) */
+  float smooth_factor; /* SMOOTH_FACTOR, default 2 */
+  float iso_factor;    /* ISO_FACTOR, default 1.9 (poly6 variant only; kept for the API) */
+  int32_t qef;         /* 0: leaf value at the cell centre (reference default);
+                          1: per-leaf QEF vertex (TNode::NodeCalcNode switched on) */
+  int32_t max_depth;   /* 0: no cap; otherwise PI_ERR_LIMIT if D_max exceeds it */
+  int32_t reserved[7];
+} pi_params;
+
+/* Per-frame results of the non-mesh stages (pi_frame_info). */
+typedef struct pi_frame_info {
+  int64_t num_particles;
+  int64_t num_invalid_keys;  /* particles outside the hash grid (key -1) */
+  float bounding[6];         /* HashGrid::Bounding */
+  float cell_size;           /* HashGrid::CellSize = 4r */
+  int32_t xyz_cell_num[3];   /* HashGrid::XYZCellNum */
+  int64_t cell_num;          /* HashGrid::CellNum */
+  int32_t depth_max, depth_min;
+  float root_center[3], root_half;
+  float iso_value, max_scalar, influence2, sigma;
+  int64_t num_nodes, num_leaves, num_empty;
+  int64_t num_dual_cells, num_vertices, num_triangles;
+  int64_t field_evals;      /* SingleEval-equivalents: node samples, leaf values, bisection */
+  int64_t candidate_pairs;  /* particle candidates visited by those evaluations */
+  int64_t bisection_evals;
+  int64_t fp64_eigen;       /* particles whose eigen-decomposition ran in FP64 */
+  float stage_ms[8];        /* device time of upload, hash, aniso, normals, octree, qef,
+                               extract, download */
+} pi_frame_info;
+
+/* Parity dumps (pi_stage_dump).  Arrays are in original particle order unless
+ * noted.  Sizes from pi_stage_dump_size. */
+#define PI_DUMP_KEYS 1        /* int64[N]  cell key or -1 (HashGrid::CalcCellHash) */
+#define PI_DUMP_INDEX_LIST 2  /* int32[N]  HashGrid::IndexList (sorted order) */
+#define PI_DUMP_CELL_OFFSETS 3 /* int32[C+1] cell c -> IndexList[off[c], off[c+1]) */
+#define PI_DUMP_XMEANS 4      /* float[N*3] Evaluator::GlobalxMeans */
+#define PI_DUMP_G 5           /* float[N*9] Evaluator::GlobalGs (row major) */
+#define PI_DUMP_DET 6         /* float[N]   Evaluator::GlobalDeterminant */
+#define PI_DUMP_NORMALS 7     /* float[N*3] Evaluator::PariclesNormals */
+#define PI_DUMP_NODES 8       /* pi_node[num_nodes], creation (level) order */
+#define PI_DUMP_FP64_FLAGS 9  /* int8[N] 1 where the eigen step ran in FP64 */
+
+typedef struct pi_node {
+  uint64_t id;      /* TNode::id */
+  float center[3];  /* TNode::center */
+  float half;       /* TNode::half_length */
+  float node[4];    /* TNode::node (position, value) */
+  float curv;       /* checkEmptyAndCalcCurv curvature */
+  int32_t parent;   /* index of the parent, -1 for the root */
+  int32_t first_child; /* index of child 0 (children are consecutive), -1 if none */
+  int8_t depth, type, signchange, pad; /* type: 0 EMPTY, 1 INTERNAL, 2 LEAF */
+} pi_node;
+
+const char* pi_last_error(void);
+const char* pi_version(void);
+void pi_params_default(pi_params* p);
+
+/* Context: one CUDA device, one stream, a stream-ordered memory pool capped at
+ * budget_bytes (0 = no cap). */
+int pi_ctx_create(int device, size_t budget_bytes, pi_ctx** out);
+int pi_ctx_destroy(pi_ctx* ctx);
+/* launches: kernels launched by the library since load; bytes: device bytes
+ * held by the context's frames. */
+int pi_ctx_stats(const pi_ctx* ctx, uint64_t* launches, uint64_t* bytes);
+/* Device time accounting of the dominant kernel class (field evaluation at
+ * octree samples), for roofline reporting: when enabled, each launch is
+ * bracketed with CUDA events on the context stream.  Read and reset with
+ * pi_ctx_kernel_time. */
+int pi_ctx_profile(pi_ctx* ctx, int enable);
+int pi_ctx_kernel_time(pi_ctx* ctx, double* total_ms, int64_t* launches, int64_t* pairs,
+                       int64_t* evals);
+/* The context stream as a cudaStream_t cast to void*. */
+void* pi_ctx_stream(pi_ctx* ctx);
+
+/* SurfReconstructor(particles, radiuses, mesh, radius)
+ * (src/surface_reconstructor.cpp:13-28): a frame owns copies of the
+ * particles and all device state of one reconstruction. */
+int pi_frame_create(pi_ctx* ctx, const pi_params* params, pi_frame** out);
+int pi_frame_destroy(pi_frame* f);
+int pi_frame_upload(pi_frame* f, const float* xyz, int64_t n);        /* host xyz[n*3] */
+int pi_frame_upload_device(pi_frame* f, const float* d_xyz, int64_t n); /* device xyz[n*3] */
+
+/* The stages of SurfReconstructor::Run (src/surface_reconstructor.cpp:409-479),
+ * each enqueued on the context stream and synchronised before return. */
+int pi_hashgrid_build(pi_frame* f);  /* loadRootBox + HashGrid ctor (:418-424) */
+int pi_aniso_compute(pi_frame* f);   /* Evaluator::compute_Gs_xMeans (:432-435) */
+int pi_normals_compute(pi_frame* f); /* resizeRootBoxConstR, CalculateMaxScalarConstR,
+                                        RecommendIsoValueConstR, CalcParticlesNormal (:453-470) */
+int pi_octree_build(pi_frame* f);    /* genIsoOurs state 0 (:326-407), incl. QEF when enabled */
+int pi_extract_mesh(pi_frame* f);    /* genIsoOurs state 1 (:290-323) */
+int pi_run(pi_frame* f);             /* all remaining stages (Run) */
+
+int pi_frame_info_get(const pi_frame* f, pi_frame_info* out);
+
+/* Mesh (Mesh::vertices / Mesh::tris, include/global.h:86-115): vertices as
+ * float xyz, triangles as 0-based int32 index triples, vkeys (optional) the
+ * sorted leaf-id pair naming each vertex (Mesh::insert_vert key). */
+int pi_mesh_counts(const pi_frame* f, int64_t* nverts, int64_t* ntris);
+int pi_mesh_get(pi_frame* f, float* verts, int32_t* tris, uint64_t* vkeys);
+/* writeObjFile (src/main.cpp:54-67): "v %f %f %f" and 1-based "f" lines */
+int pi_mesh_write_obj(pi_frame* f, const char* path);
+
+/* Evaluator::SingleEval / SingleEvalWithGrad (src/evaluator.cpp:60-125) at m
+ * host points; grad may be null.  Needs pi_normals_compute. */
+int pi_eval_field(pi_frame* f, const float* pts, int64_t m, float* scalar, float* grad);
+
+/* HashGrid::GetPIdxList (src/hash_grid.cpp:196-214) for m host points:
+ * offsets[m+1] and the concatenated particle indices; *total receives the
+ * number of indices; PI_ERR_LIMIT (with *total set) if cap is too small. */
+int pi_hashgrid_neighbors(pi_frame* f, const float* pts, int64_t m, int64_t* offsets, int32_t* idx,
+                          int64_t cap, int64_t* total);
+/* HashGrid::GetInBoxParticles (src/hash_grid.cpp:164-194). */
+int pi_hashgrid_in_box(pi_frame* f, const float* box1, const float* box2, int32_t* idx, int64_t cap,
+                       int64_t* total);
+
+int pi_stage_dump_size(const pi_frame* f, int what, size_t* bytes);
+int pi_stage_dump(pi_frame* f, int what, void* host_buf, size_t bytes);
+
+/* One call, host in / host out: upload, Run, download (the e2e path of a
+ * frame).  verts/tris must hold max_verts / max_tris entries; the actual
+ * counts are returned (PI_ERR_LIMIT if the buffers are too small). */
+int pi_reconstruct(pi_ctx* ctx, const pi_params* params, const float* xyz, int64_t n, float* verts,
+                   int64_t max_verts, int32_t* tris, int64_t max_tris, int64_t* nverts,
+                   int64_t* ntris);
+
+/* The dual-marching-cubes canonicalisation table the library uses
+ * (include/visitorextract.h:35-293 in the reference). */
+int pi_dmc_table(int32_t* trans8x256, int8_t* flip256, int32_t* code256);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

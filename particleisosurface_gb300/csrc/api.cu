@@ -1,0 +1,705 @@
+// C ABI (include/pisurf.h): context and frame lifecycle, stage
+// orchestration, dumps and queries.  SurfReconstructor::Run
+// (src/surface_reconstructor.cpp:409-479) is pi_run.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace pisurf {
+
+struct NoMem : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+struct StateError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+thread_local std::string g_last_error;
+
+void ctx_account(pi_ctx* c, long long delta) {
+  if (!c) return;
+  long long now = c->used.fetch_add(delta) + delta;
+  if (delta > 0 && c->budget && now > (long long)c->budget) {
+    c->used.fetch_sub(delta);
+    throw NoMem("device memory budget exceeded: need " + std::to_string(now) + " bytes, budget " +
+                std::to_string(c->budget));
+  }
+}
+
+template <class T>
+void DBuf<T>::alloc(pi_ctx* c, cudaStream_t st, size_t count) {
+  release();
+  if (count == 0) count = 1;
+  ctx_account(c, (long long)(count * sizeof(T)));
+  void* q = nullptr;
+  cudaError_t e = cudaMallocAsync(&q, count * sizeof(T), st);
+  if (e != cudaSuccess) {
+    ctx_account(c, -(long long)(count * sizeof(T)));
+    (void)cudaGetLastError();
+    if (e == cudaErrorMemoryAllocation) throw NoMem("cudaMallocAsync: out of device memory");
+    throw CudaError(std::string("cudaMallocAsync: ") + cudaGetErrorString(e), (int)e);
+  }
+  p = static_cast<T*>(q);
+  n = count;
+  ctx = c;
+  s = st;
+}
+
+template <class T>
+void DBuf<T>::grow(pi_ctx* c, cudaStream_t st, size_t count, size_t keep) {
+  if (count <= n) return;
+  T* old = p;
+  size_t oldn = n;
+  pi_ctx* oc = ctx;
+  cudaStream_t os = s;
+  p = nullptr;
+  n = 0;
+  alloc(c, st, count);
+  if (old) {
+    if (keep) PI_CUDA(cudaMemcpyAsync(p, old, keep * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    cudaFreeAsync(old, os);
+    ctx_account(oc, -(long long)(oldn * sizeof(T)));
+  }
+}
+
+template <class T>
+void DBuf<T>::release() {
+  if (p) {
+    cudaFreeAsync(p, s);
+    ctx_account(ctx, -(long long)(n * sizeof(T)));
+  }
+  p = nullptr;
+  n = 0;
+}
+
+template struct DBuf<float>;
+template struct DBuf<float4>;
+template struct DBuf<int>;
+template struct DBuf<int4>;
+template struct DBuf<unsigned>;
+template struct DBuf<int8_t>;
+template struct DBuf<uint64_t>;
+template struct DBuf<unsigned long long>;
+template struct DBuf<long long>;
+
+// Bspline_kernel (src/evaluator.cpp:383-396) with the reference's types:
+// float in, polynomial in double, float out.
+float bspline_host(float ratio, float sigma) {
+  if (ratio < 2) {
+    if (ratio <= 1) return (float)(sigma * (1 - 1.5 * std::pow(ratio, 2) + 0.75 * std::pow(ratio, 3)));
+    float tmq = 2 - ratio;
+    return (float)(sigma * (0.25 * std::pow(tmq, 3)));
+  }
+  return 0.0f;
+}
+
+void prof_begin(pi_ctx* c, cudaStream_t s) {
+  if (!c->profile) return;
+  cudaEvent_t e;
+  PI_CUDA(cudaEventCreate(&e));
+  PI_CUDA(cudaEventRecord(e, s));
+  c->prof_events.push_back(e);
+}
+void prof_end(pi_ctx* c, cudaStream_t s, long long, long long) {
+  if (!c->profile) return;
+  cudaEvent_t e;
+  PI_CUDA(cudaEventCreate(&e));
+  PI_CUDA(cudaEventRecord(e, s));
+  c->prof_events.push_back(e);
+  c->kernel_launches++;
+}
+
+// resizeRootBoxConstR (src/surface_reconstructor.cpp:97-122),
+// CalculateMaxScalarConstR / RecommendIsoValueConstR (src/evaluator.cpp:272-335)
+static void host_root_and_scalars(pi_frame* f) {
+  const float r = f->P.radius;
+  const float* bb = f->bbox6;
+  float maxLen = std::max({(bb[1] - bb[0]), (bb[3] - bb[2]), (bb[5] - bb[4])});
+  int dmax = int(std::ceil(std::log2(std::ceil(maxLen / r))));
+  float resizeLen = (float)(std::pow(2, dmax) * r);
+  while (resizeLen - maxLen < (4.0f * r * 2)) {
+    dmax++;
+    resizeLen = (float)(std::pow(2, dmax) * r);
+  }
+  f->rootH = resizeLen / 2;
+  for (int i = 0; i < 3; ++i) f->rootC[i] = (bb[i * 2] + bb[i * 2 + 1]) / 2;
+  f->dmax = dmax;
+  f->dmin = dmax - (f->singleLayer ? 1 : 3);
+  const float sqrt2 = 1.4142135623730950488016887242097f;
+  const float sqrt3 = 1.7320508075688772935274463415059f;
+  float k = 0;
+  k += bspline_host(0.0f, f->sigma);
+  k += bspline_host(1.0f, f->sigma) * 6;
+  k += bspline_host(sqrt2, f->sigma) * 12;
+  k += bspline_host(sqrt3, f->sigma) * 8;
+  f->maxScalar = k;
+  f->iso = bspline_host((float)0.01, f->sigma);
+}
+
+static void ev_record(pi_frame* f, int i) {
+  if (!f->ev[i]) PI_CUDA(cudaEventCreate(&f->ev[i]));
+  PI_CUDA(cudaEventRecord(f->ev[i], f->ctx->stream));
+}
+static void ev_close(pi_frame* f, int stage_slot, int a, int b) {
+  PI_CUDA(cudaEventSynchronize(f->ev[b]));
+  float ms = 0;
+  PI_CUDA(cudaEventElapsedTime(&ms, f->ev[a], f->ev[b]));
+  f->stage_ms[stage_slot] += ms;
+}
+
+static void need(const pi_frame* f, int stage) {
+  if (f->stage < stage) throw StateError("stage called before the stages it depends on");
+}
+
+static void run_stage(pi_frame* f, int target) {
+  // target: 2 hash, 3 aniso, 4 normals, 5 octree, 6 mesh
+  if (f->stage >= target) return;
+  need(f, target - 1);
+  ev_record(f, 0);
+  switch (target) {
+    case 2:
+      stage_hashgrid(f);
+      break;
+    case 3:
+      stage_aniso(f);
+      break;
+    case 4:
+      host_root_and_scalars(f);
+      if (f->P.max_depth > 0 && f->dmax > f->P.max_depth)
+        throw std::length_error("octree depth " + std::to_string(f->dmax) + " exceeds max_depth " +
+                                std::to_string(f->P.max_depth));
+      stage_normals(f);
+      break;
+    case 5:
+      stage_octree(f);
+      if (f->ctx->profile) {
+        f->ctx->kernel_pairs += f->pairs;
+        f->ctx->kernel_evals += f->fieldEvals;
+      }
+      break;
+    case 6:
+      stage_extract(f);
+      break;
+  }
+  ev_record(f, 1);
+  const int slot = target == 2 ? 1 : target == 3 ? 2 : target == 4 ? 3 : target == 5 ? 4 : 6;
+  ev_close(f, slot, 0, 1);
+  f->stage = target;
+}
+
+}  // namespace pisurf
+
+using namespace pisurf;
+
+#define PI_API_BEGIN try {
+#define PI_API_END                                 \
+  }                                                \
+  catch (const NoMem& e) {                         \
+    g_last_error = e.what();                       \
+    return PI_ERR_NOMEM;                           \
+  }                                                \
+  catch (const StateError& e) {                    \
+    g_last_error = e.what();                       \
+    return PI_ERR_STATE;                           \
+  }                                                \
+  catch (const CudaError& e) {                     \
+    g_last_error = e.what();                       \
+    return PI_ERR_CUDA;                            \
+  }                                                \
+  catch (const std::invalid_argument& e) {         \
+    g_last_error = e.what();                       \
+    return PI_ERR_INVALID;                         \
+  }                                                \
+  catch (const std::length_error& e) {             \
+    g_last_error = e.what();                       \
+    return PI_ERR_LIMIT;                           \
+  }                                                \
+  catch (const std::bad_alloc& e) {                \
+    g_last_error = "host allocation failed";       \
+    return PI_ERR_NOMEM;                           \
+  }                                                \
+  catch (const std::exception& e) {                \
+    g_last_error = e.what();                       \
+    return PI_ERR_CUDA;                            \
+  }                                                \
+  return PI_OK;
+
+#define PI_CHECK(cond, msg)                 \
+  do {                                      \
+    if (!(cond)) throw std::invalid_argument(msg); \
+  } while (0)
+
+static void set_device(pi_ctx* c) { PI_CUDA(cudaSetDevice(c->device)); }
+
+template <class T>
+static std::vector<T> d2h(const T* d, size_t n, cudaStream_t s) {
+  std::vector<T> h(n);
+  if (n) PI_CUDA(cudaMemcpyAsync(h.data(), d, sizeof(T) * n, cudaMemcpyDeviceToHost, s));
+  PI_CUDA(cudaStreamSynchronize(s));
+  return h;
+}
+
+
+extern "C" {
+
+const char* pi_last_error(void) { return g_last_error.c_str(); }
+const char* pi_version(void) { return "particleisosurface_gb300 0.1 (sm_103a)"; }
+
+void pi_params_default(pi_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->radius = 0.01f;
+  p->smooth_factor = 2.0f;
+  p->iso_factor = 1.9f;
+  p->qef = 0;
+  p->max_depth = 0;
+}
+
+int pi_ctx_create(int device, size_t budget_bytes, pi_ctx** out) {
+  PI_API_BEGIN
+  PI_CHECK(out, "out is null");
+  *out = nullptr;
+  int ndev = 0;
+  PI_CUDA(cudaGetDeviceCount(&ndev));
+  PI_CHECK(device >= 0 && device < ndev, "no such CUDA device");
+  std::unique_ptr<pi_ctx> c(new pi_ctx());
+  c->device = device;
+  c->budget = budget_bytes;
+  PI_CUDA(cudaSetDevice(device));
+  PI_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  PI_CUDA(cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, device));
+  cudaMemPool_t pool;
+  PI_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+  uint64_t thr = UINT64_MAX;
+  PI_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  *out = c.release();
+  PI_API_END
+}
+
+int pi_ctx_destroy(pi_ctx* c) {
+  PI_API_BEGIN
+  if (!c) return PI_OK;
+  set_device(c);
+  cudaStreamSynchronize(c->stream);
+  for (auto e : c->prof_events) cudaEventDestroy(e);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  PI_API_END
+}
+
+int pi_ctx_stats(const pi_ctx* c, uint64_t* launches, uint64_t* bytes) {
+  PI_API_BEGIN
+  PI_CHECK(c, "ctx is null");
+  if (launches) *launches = g_launches;
+  if (bytes) *bytes = (uint64_t)c->used.load();
+  PI_API_END
+}
+
+int pi_ctx_profile(pi_ctx* c, int enable) {
+  PI_API_BEGIN
+  PI_CHECK(c, "ctx is null");
+  c->profile = enable != 0;
+  PI_API_END
+}
+
+int pi_ctx_kernel_time(pi_ctx* c, double* total_ms, int64_t* launches, int64_t* pairs, int64_t* evals) {
+  PI_API_BEGIN
+  PI_CHECK(c, "ctx is null");
+  set_device(c);
+  PI_CUDA(cudaStreamSynchronize(c->stream));
+  double ms = 0;
+  for (size_t i = 0; i + 1 < c->prof_events.size(); i += 2) {
+    float t = 0;
+    PI_CUDA(cudaEventElapsedTime(&t, c->prof_events[i], c->prof_events[i + 1]));
+    ms += t;
+  }
+  for (auto e : c->prof_events) cudaEventDestroy(e);
+  c->prof_events.clear();
+  c->kernel_ms += ms;
+  if (total_ms) *total_ms = c->kernel_ms;
+  if (launches) *launches = c->kernel_launches;
+  if (pairs) *pairs = c->kernel_pairs;
+  if (evals) *evals = c->kernel_evals;
+  c->kernel_ms = 0;
+  c->kernel_launches = c->kernel_pairs = c->kernel_evals = 0;
+  PI_API_END
+}
+
+void* pi_ctx_stream(pi_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int pi_frame_create(pi_ctx* c, const pi_params* p, pi_frame** out) {
+  PI_API_BEGIN
+  PI_CHECK(c && p && out, "null argument");
+  PI_CHECK(std::isfinite(p->radius) && p->radius > 0, "radius must be positive");
+  PI_CHECK(std::isfinite(p->smooth_factor) && p->smooth_factor > 0, "smooth_factor must be positive");
+  *out = nullptr;
+  pi_frame* f = new pi_frame();
+  f->ctx = c;
+  f->P = *p;
+  *out = f;
+  PI_API_END
+}
+
+int pi_frame_destroy(pi_frame* f) {
+  PI_API_BEGIN
+  if (!f) return PI_OK;
+  set_device(f->ctx);
+  for (auto& e : f->ev)
+    if (e) cudaEventDestroy(e);
+  delete f;
+  PI_API_END
+}
+
+int pi_frame_upload(pi_frame* f, const float* xyz, int64_t n) {
+  PI_API_BEGIN
+  PI_CHECK(f && xyz && n > 0, "bad upload arguments");
+  PI_CHECK(n < (1LL << 31), "more than 2^31 particles");
+  set_device(f->ctx);
+  ev_record(f, 0);
+  stage_upload_host(f, xyz, n);
+  ev_record(f, 1);
+  ev_close(f, 0, 0, 1);
+  f->stage = 1;
+  PI_API_END
+}
+
+int pi_frame_upload_device(pi_frame* f, const float* d_xyz, int64_t n) {
+  PI_API_BEGIN
+  PI_CHECK(f && d_xyz && n > 0, "bad upload arguments");
+  PI_CHECK(n < (1LL << 31), "more than 2^31 particles");
+  set_device(f->ctx);
+  stage_upload_device(f, d_xyz, n);
+  f->stage = 1;
+  PI_API_END
+}
+
+int pi_hashgrid_build(pi_frame* f) {
+  PI_API_BEGIN
+  PI_CHECK(f, "frame is null");
+  set_device(f->ctx);
+  run_stage(f, 2);
+  PI_API_END
+}
+int pi_aniso_compute(pi_frame* f) {
+  PI_API_BEGIN
+  PI_CHECK(f, "frame is null");
+  set_device(f->ctx);
+  run_stage(f, 3);
+  PI_API_END
+}
+int pi_normals_compute(pi_frame* f) {
+  PI_API_BEGIN
+  PI_CHECK(f, "frame is null");
+  set_device(f->ctx);
+  run_stage(f, 4);
+  PI_API_END
+}
+int pi_octree_build(pi_frame* f) {
+  PI_API_BEGIN
+  PI_CHECK(f, "frame is null");
+  set_device(f->ctx);
+  run_stage(f, 5);
+  PI_API_END
+}
+int pi_extract_mesh(pi_frame* f) {
+  PI_API_BEGIN
+  PI_CHECK(f, "frame is null");
+  set_device(f->ctx);
+  run_stage(f, 6);
+  PI_API_END
+}
+int pi_run(pi_frame* f) {
+  PI_API_BEGIN
+  PI_CHECK(f, "frame is null");
+  set_device(f->ctx);
+  need(f, 1);
+  for (int t = 2; t <= 6; ++t) run_stage(f, t);
+  PI_API_END
+}
+
+int pi_frame_info_get(const pi_frame* f, pi_frame_info* o) {
+  PI_API_BEGIN
+  PI_CHECK(f && o, "null argument");
+  std::memset(o, 0, sizeof(*o));
+  o->num_particles = f->N;
+  o->num_invalid_keys = f->g.nInvalid;
+  for (int k = 0; k < 6; ++k) o->bounding[k] = f->g.bounding[k];
+  o->cell_size = f->g.cell;
+  o->xyz_cell_num[0] = f->g.nx;
+  o->xyz_cell_num[1] = f->g.ny;
+  o->xyz_cell_num[2] = f->g.nz;
+  o->cell_num = f->g.cellNum;
+  o->depth_max = f->dmax;
+  o->depth_min = f->dmin;
+  for (int k = 0; k < 3; ++k) o->root_center[k] = f->rootC[k];
+  o->root_half = f->rootH;
+  o->iso_value = f->iso;
+  o->max_scalar = f->maxScalar;
+  o->influence2 = f->influ2;
+  o->sigma = f->sigma;
+  o->num_nodes = f->nNodes;
+  o->num_leaves = f->nLeaves;
+  o->num_empty = f->nEmpty;
+  o->num_dual_cells = f->nDual;
+  o->num_vertices = f->nV;
+  o->num_triangles = f->nT;
+  o->field_evals = f->fieldEvals;
+  o->candidate_pairs = f->pairs;
+  o->bisection_evals = f->bisectEvals;
+  o->fp64_eigen = f->fp64Count;
+  for (int k = 0; k < 8; ++k) o->stage_ms[k] = f->stage_ms[k];
+  PI_API_END
+}
+
+int pi_mesh_counts(const pi_frame* f, int64_t* nv, int64_t* nt) {
+  PI_API_BEGIN
+  PI_CHECK(f && nv && nt, "null argument");
+  need(f, 6);
+  *nv = f->nV;
+  *nt = f->nT;
+  PI_API_END
+}
+
+int pi_mesh_get(pi_frame* f, float* verts, int32_t* tris, uint64_t* vkeys) {
+  PI_API_BEGIN
+  PI_CHECK(f, "frame is null");
+  need(f, 6);
+  set_device(f->ctx);
+  cudaStream_t s = f->ctx->stream;
+  if (verts && f->nV) PI_CUDA(cudaMemcpyAsync(verts, f->mv.p, sizeof(float) * 3 * f->nV, cudaMemcpyDeviceToHost, s));
+  if (tris && f->nT) PI_CUDA(cudaMemcpyAsync(tris, f->mt.p, sizeof(int) * 3 * f->nT, cudaMemcpyDeviceToHost, s));
+  if (vkeys && f->nV)
+    PI_CUDA(cudaMemcpyAsync(vkeys, f->mk.p, sizeof(uint64_t) * 2 * f->nV, cudaMemcpyDeviceToHost, s));
+  PI_CUDA(cudaStreamSynchronize(s));
+  PI_API_END
+}
+
+int pi_mesh_write_obj(pi_frame* f, const char* path) {
+  PI_API_BEGIN
+  PI_CHECK(f && path, "null argument");
+  need(f, 6);
+  std::vector<float> v(3 * f->nV);
+  std::vector<int> t(3 * f->nT);
+  int rc = pi_mesh_get(f, v.data(), t.data(), nullptr);
+  if (rc) return rc;
+  FILE* fp = std::fopen(path, "w");
+  PI_CHECK(fp, "cannot open output file");
+  for (long long i = 0; i < f->nV; ++i) std::fprintf(fp, "v %f %f %f\n", v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+  for (long long i = 0; i < f->nT; ++i) std::fprintf(fp, "f %d %d %d\n", t[3 * i] + 1, t[3 * i + 1] + 1, t[3 * i + 2] + 1);
+  std::fclose(fp);
+  PI_API_END
+}
+
+int pi_eval_field(pi_frame* f, const float* pts, int64_t m, float* scalar, float* grad) {
+  PI_API_BEGIN
+  PI_CHECK(f && pts && scalar && m > 0, "bad arguments");
+  need(f, 4);
+  set_device(f->ctx);
+  cudaStream_t s = f->ctx->stream;
+  DBuf<float> dp, dv, dg;
+  dp.alloc(f->ctx, s, m * 3);
+  dv.alloc(f->ctx, s, m);
+  if (grad) dg.alloc(f->ctx, s, m * 3);
+  PI_CUDA(cudaMemcpyAsync(dp.p, pts, sizeof(float) * 3 * m, cudaMemcpyHostToDevice, s));
+  eval_points(f, dp.p, m, dv.p, grad ? dg.p : nullptr);
+  PI_CUDA(cudaMemcpyAsync(scalar, dv.p, sizeof(float) * m, cudaMemcpyDeviceToHost, s));
+  if (grad) PI_CUDA(cudaMemcpyAsync(grad, dg.p, sizeof(float) * 3 * m, cudaMemcpyDeviceToHost, s));
+  PI_CUDA(cudaStreamSynchronize(s));
+  PI_API_END
+}
+
+int pi_hashgrid_neighbors(pi_frame* f, const float* pts, int64_t m, int64_t* offsets, int32_t* idx, int64_t cap,
+                          int64_t* total) {
+  PI_API_BEGIN
+  PI_CHECK(f && pts && offsets && total && m > 0, "bad arguments");
+  need(f, 2);
+  set_device(f->ctx);
+  std::vector<long long> off(m + 1);
+  long long t = neighbors(f, pts, m, off.data(), idx, idx ? cap : 0);
+  for (long long i = 0; i <= m; ++i) offsets[i] = off[i];
+  *total = t;
+  if (t > cap) throw std::length_error("neighbour buffer too small");
+  PI_API_END
+}
+
+int pi_hashgrid_in_box(pi_frame* f, const float* b1, const float* b2, int32_t* idx, int64_t cap, int64_t* total) {
+  PI_API_BEGIN
+  PI_CHECK(f && b1 && b2 && total, "bad arguments");
+  need(f, 2);
+  set_device(f->ctx);
+  long long t = in_box(f, b1, b2, idx, idx ? cap : 0);
+  *total = t;
+  if (t > cap) throw std::length_error("index buffer too small");
+  PI_API_END
+}
+
+static size_t dump_size(const pi_frame* f, int what) {
+  switch (what) {
+    case PI_DUMP_KEYS: return sizeof(int64_t) * f->N;
+    case PI_DUMP_INDEX_LIST: return sizeof(int32_t) * f->N;
+    case PI_DUMP_CELL_OFFSETS: return sizeof(int32_t) * (f->g.cellNum + 1);
+    case PI_DUMP_XMEANS: return sizeof(float) * 3 * f->N;
+    case PI_DUMP_G: return sizeof(float) * 9 * f->N;
+    case PI_DUMP_DET: return sizeof(float) * f->N;
+    case PI_DUMP_NORMALS: return sizeof(float) * 3 * f->N;
+    case PI_DUMP_NODES: return sizeof(pi_node) * f->nNodes;
+    case PI_DUMP_FP64_FLAGS: return sizeof(int8_t) * f->N;
+  }
+  return 0;
+}
+
+int pi_stage_dump_size(const pi_frame* f, int what, size_t* bytes) {
+  PI_API_BEGIN
+  PI_CHECK(f && bytes, "null argument");
+  *bytes = dump_size(f, what);
+  PI_CHECK(*bytes || what == PI_DUMP_NODES, "unknown dump");
+  PI_API_END
+}
+
+int pi_stage_dump(pi_frame* f, int what, void* buf, size_t bytes) {
+  PI_API_BEGIN
+  PI_CHECK(f && buf, "null argument");
+  size_t need_b = dump_size(f, what);
+  PI_CHECK(bytes >= need_b, "dump buffer too small");
+  set_device(f->ctx);
+  cudaStream_t s = f->ctx->stream;
+  const long long N = f->N;
+  auto sorted_to_orig = [&](const std::vector<float>& src, int w, float* dst) {
+    std::vector<uint32_t> sidx = d2h(f->sidx.p, N, s);
+    for (long long t = 0; t < N; ++t)
+      for (int k = 0; k < w; ++k) dst[(size_t)sidx[t] * w + k] = src[(size_t)t * w + k];
+  };
+  switch (what) {
+    case PI_DUMP_KEYS: {
+      need(f, 2);
+      auto k = d2h(f->key.p, N, s);
+      int64_t* o = (int64_t*)buf;
+      for (long long i = 0; i < N; ++i) o[i] = k[i];
+      break;
+    }
+    case PI_DUMP_INDEX_LIST: {
+      need(f, 2);
+      auto k = d2h(f->sidx.p, N, s);
+      std::memcpy(buf, k.data(), sizeof(int32_t) * N);
+      break;
+    }
+    case PI_DUMP_CELL_OFFSETS: {
+      need(f, 2);
+      auto k = d2h(f->off.p, f->g.cellNum + 1, s);
+      std::memcpy(buf, k.data(), sizeof(int32_t) * (f->g.cellNum + 1));
+      break;
+    }
+    case PI_DUMP_XMEANS: {
+      need(f, 3);
+      auto x = d2h(f->xm.p, N, s);
+      std::vector<float> v(3 * N);
+      for (long long t = 0; t < N; ++t) v[3 * t] = x[t].x, v[3 * t + 1] = x[t].y, v[3 * t + 2] = x[t].z;
+      sorted_to_orig(v, 3, (float*)buf);
+      break;
+    }
+    case PI_DUMP_G: {
+      need(f, 3);
+      sorted_to_orig(d2h(f->gfull.p, 9 * N, s), 9, (float*)buf);
+      break;
+    }
+    case PI_DUMP_DET: {
+      need(f, 3);
+      sorted_to_orig(d2h(f->det.p, N, s), 1, (float*)buf);
+      break;
+    }
+    case PI_DUMP_NORMALS: {
+      need(f, 4);
+      auto x = d2h(f->nrm.p, N, s);
+      std::vector<float> v(3 * N);
+      for (long long t = 0; t < N; ++t) v[3 * t] = x[t].x, v[3 * t + 1] = x[t].y, v[3 * t + 2] = x[t].z;
+      sorted_to_orig(v, 3, (float*)buf);
+      break;
+    }
+    case PI_DUMP_FP64_FLAGS: {
+      need(f, 3);
+      auto x = d2h(f->f64flag.p, N, s);
+      std::vector<uint32_t> sidx = d2h(f->sidx.p, N, s);
+      int8_t* o = (int8_t*)buf;
+      for (long long t = 0; t < N; ++t) o[sidx[t]] = x[t];
+      break;
+    }
+    case PI_DUMP_NODES: {
+      need(f, 5);
+      const long long n = f->nNodes;
+      auto c = d2h(f->nd_c.p, n, s);
+      auto v = d2h(f->nd_v.p, n, s);
+      auto id = d2h(f->nd_id.p, n, s);
+      auto par = d2h(f->nd_parent.p, n, s);
+      auto ch = d2h(f->nd_child.p, n, s);
+      auto ty = d2h(f->nd_type.p, n, s);
+      auto de = d2h(f->nd_depth.p, n, s);
+      auto sc = d2h(f->nd_sc.p, n, s);
+      auto cu = d2h(f->nd_curv.p, n, s);
+      pi_node* o = (pi_node*)buf;
+      for (long long i = 0; i < n; ++i) {
+        o[i].id = id[i];
+        o[i].center[0] = c[i].x, o[i].center[1] = c[i].y, o[i].center[2] = c[i].z;
+        o[i].half = c[i].w;
+        o[i].node[0] = v[i].x, o[i].node[1] = v[i].y, o[i].node[2] = v[i].z, o[i].node[3] = v[i].w;
+        o[i].curv = cu[i];
+        o[i].parent = par[i];
+        o[i].first_child = ch[i];
+        o[i].depth = de[i];
+        o[i].type = ty[i];
+        o[i].signchange = sc[i];
+        o[i].pad = 0;
+      }
+      break;
+    }
+    default:
+      throw std::invalid_argument("unknown dump");
+  }
+  PI_API_END
+}
+
+int pi_reconstruct(pi_ctx* c, const pi_params* p, const float* xyz, int64_t n, float* verts, int64_t max_verts,
+                   int32_t* tris, int64_t max_tris, int64_t* nverts, int64_t* ntris) {
+  PI_API_BEGIN
+  PI_CHECK(c && p && xyz && nverts && ntris, "null argument");
+  pi_frame* f = nullptr;
+  int rc = pi_frame_create(c, p, &f);
+  if (rc) return rc;
+  struct Guard {
+    pi_frame* f;
+    ~Guard() { pi_frame_destroy(f); }
+  } guard{f};
+  rc = pi_frame_upload(f, xyz, n);
+  if (rc) return rc;
+  rc = pi_run(f);
+  if (rc) return rc;
+  *nverts = f->nV;
+  *ntris = f->nT;
+  if (f->nV > max_verts || f->nT > max_tris) throw std::length_error("mesh buffers too small");
+  rc = pi_mesh_get(f, verts, tris, nullptr);
+  if (rc) return rc;
+  PI_API_END
+}
+
+int pi_dmc_table(int32_t* trans, int8_t* flip, int32_t* code) {
+  PI_API_BEGIN
+  PI_CHECK(trans && flip && code, "null argument");
+  int t[256][8], c[256];
+  bool fl[256];
+  dmc_host_table(t, fl, c);
+  for (int i = 0; i < 256; ++i) {
+    for (int k = 0; k < 8; ++k) trans[8 * i + k] = t[i][k];
+    flip[i] = fl[i] ? 1 : 0;
+    code[i] = c[i];
+  }
+  PI_API_END
+}
+
+}  // extern "C"

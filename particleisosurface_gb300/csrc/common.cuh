@@ -1,0 +1,67 @@
+// Shared device/host helpers for the particle-isosurface CUDA library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+namespace pisurf {
+
+// Library-wide count of kernel launches (read by pi_ctx_stats).
+extern unsigned long long g_launches;
+
+struct CudaError : std::runtime_error {
+  int code;
+  CudaError(const std::string& s, int c) : std::runtime_error(s), code(c) {}
+};
+
+#define PI_CUDA(call)                                                                   \
+  do {                                                                                  \
+    cudaError_t _e = (call);                                                            \
+    if (_e != cudaSuccess)                                                              \
+      throw ::pisurf::CudaError(std::string(#call) + ": " + cudaGetErrorString(_e) +    \
+                                    " (" + __FILE__ + ":" + std::to_string(__LINE__) + \
+                                    ")",                                                \
+                                (int)_e);                                               \
+  } while (0)
+
+// Launch wrapper: counts the launch and checks the launch error.
+#define PI_LAUNCH(kernel, grid, block, smem, stream, ...)                 \
+  do {                                                                    \
+    if ((grid) > 0) {                                                     \
+      kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);         \
+      ::pisurf::g_launches++;                                             \
+      PI_CUDA(cudaGetLastError());                                        \
+    }                                                                     \
+  } while (0)
+
+inline unsigned int div_up(long long a, long long b) { return (unsigned int)((a + b - 1) / b); }
+
+// ---------------------------------------------------------------------------
+// Scan (exclusive, int32) and stable LSD radix sort (u32/u64 keys, u32
+// values).  Implemented in sort.cu.
+// ---------------------------------------------------------------------------
+struct Workspace;  // forward
+
+// out[i] = sum_{k<i} in[i]; returns nothing; total written to *d_total if
+// non-null.  in and out may alias.  tmp must hold scan_tmp_ints(n) ints.
+size_t scan_tmp_ints(long long n);
+void exclusive_scan_i32(const int* in, int* out, long long n, int* d_total, int* tmp,
+                        cudaStream_t s);
+
+// Sorts (keys, vals) by the bits [0, bits) of the key, stably.  Uses
+// keys_alt/vals_alt as ping-pong buffers; the sorted result is returned in
+// the pointers *keys/*vals (which may be swapped with the alt buffers).
+// tmp must hold radix_tmp_ints(n) ints.
+size_t radix_tmp_ints(long long n);
+void radix_sort_u32(uint32_t** keys, uint32_t** vals, uint32_t** keys_alt, uint32_t** vals_alt,
+                    long long n, int bits, int* tmp, cudaStream_t s);
+void radix_sort_u64(uint64_t** keys, uint32_t** vals, uint64_t** keys_alt, uint32_t** vals_alt,
+                    long long n, int bits, int* tmp, cudaStream_t s);
+
+// iota: v[i] = i
+void iota_u32(uint32_t* v, long long n, cudaStream_t s);
+
+}  // namespace pisurf

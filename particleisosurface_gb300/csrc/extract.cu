@@ -1,0 +1,504 @@
+// K6: dual-grid extraction, genIsoOurs state 1 (src/surface_reconstructor.cpp:290-323).
+//
+// The reference walks the octree recursively (include/traverse.h) and visits
+// every interior octree vertex once with the 8 leaves around it
+// (VisitorExtract::on_vert, src/visitorextract.cpp:229-256).  Those vertices
+// are exactly the corners of leaves that lie strictly inside the root box, so
+// here they are enumerated in parallel:
+//   1. every leaf emits its interior corners (integer lattice at D_max);
+//      sort + unique gives the dual vertices;
+//   2. per vertex, the leaf containing each of the 8 octants is found by
+//      descending from the root; sign code, table[256] -> canonical case;
+//   3. per non-trivial cell, the case triangles (src/visitorextract.cpp:95-199)
+//      name leaf pairs; mesh vertices are deduplicated by the sorted leaf-id
+//      pair, as Mesh::insert_vert keys them (src/global.cpp:13-32);
+//   4. one thread per mesh vertex bisects its leaf-to-leaf segment down to
+//      r/2 with a field evaluation per step and interpolates with the 0.1/0.9
+//      snap (calc_vertices, src/visitorextract.cpp:47-84);
+//   5. triangles are oriented by the table's flip and deduplicated by their
+//      sorted vertex triple (Mesh::insert_tri, src/global.cpp:34-53).
+// The output order differs from the reference's traversal order; the mesh is
+// the same set of vertices (by leaf-id pair) and triangles.
+#include <algorithm>
+#include <mutex>
+
+#include "device.cuh"
+#include "dmc.h"
+#include "internal.h"
+
+namespace pisurf {
+
+__constant__ int c_trans[256][8];
+__constant__ int c_flip[256];
+__constant__ int c_code[256];
+__constant__ int c_ntri[256];
+__constant__ int c_tri[256][15];
+
+void dmc_host_table(int trans[256][8], bool flip[256], int code[256]) {
+  DmcTables t;
+  dmc_build(&t);
+  for (int i = 0; i < 256; ++i) {
+    for (int k = 0; k < 8; ++k) trans[i][k] = t.trans[i][k];
+    flip[i] = t.flip[i] != 0;
+    code[i] = t.code[i];
+  }
+}
+
+static void upload_tables(int device) {
+  static std::mutex mu;
+  static bool done[128] = {false};
+  std::lock_guard<std::mutex> lk(mu);
+  if (device >= 0 && device < 128 && done[device]) return;
+  DmcTables t;
+  dmc_build(&t);
+  PI_CUDA(cudaMemcpyToSymbol(c_trans, t.trans, sizeof(t.trans)));
+  PI_CUDA(cudaMemcpyToSymbol(c_flip, t.flip, sizeof(t.flip)));
+  PI_CUDA(cudaMemcpyToSymbol(c_code, t.code, sizeof(t.code)));
+  PI_CUDA(cudaMemcpyToSymbol(c_ntri, t.ntri, sizeof(t.ntri)));
+  PI_CUDA(cudaMemcpyToSymbol(c_tri, t.tri, sizeof(t.tri)));
+  if (device >= 0 && device < 128) done[device] = true;
+}
+
+__device__ __forceinline__ void edge_corners(int e, int* c0, int* c1) {
+  const int axis = e >> 2, k = e & 3;
+  const int u = axis == 0 ? 1 : 0, v = axis == 2 ? 1 : 2;
+  *c0 = ((k & 1) << u) | (((k >> 1) & 1) << v);
+  *c1 = *c0 | (1 << axis);
+}
+
+__global__ void k_leaf_flag(const int* __restrict__ nd_child, long long n, int* __restrict__ flag) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flag[i] = nd_child[i] < 0 ? 1 : 0;
+  if (i == n) flag[i] = 0;
+}
+
+__global__ void k_leaf_list(const int* __restrict__ nd_child, const int* __restrict__ scan, long long n,
+                            int* __restrict__ leaves) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && nd_child[i] < 0) leaves[scan[i]] = (int)i;
+}
+
+// Interior corners of each leaf, key (x << 2B) | (y << B) | z, B = D_max + 1;
+// boundary corners get the all-ones key.
+__global__ void k_corner_keys(const int* __restrict__ leaves, long long nl, const int4* __restrict__ nd_org,
+                              int full, int B, uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nl * 8) return;
+  const int4 o = nd_org[leaves[t >> 3]];
+  const int k = (int)(t & 7);
+  const int x = o.x + ((k & 1) ? o.w : 0), y = o.y + ((k & 2) ? o.w : 0), z = o.z + ((k & 4) ? o.w : 0);
+  uint64_t key;
+  if (x > 0 && x < full && y > 0 && y < full && z > 0 && z < full)
+    key = ((uint64_t)x << (2 * B)) | ((uint64_t)y << B) | (uint64_t)z;
+  else
+    key = (1ull << (3 * B)) - 1ull;
+  keys[t] = key;
+  vals[t] = (uint32_t)t;
+}
+
+__global__ void k_unique_flag(const uint64_t* __restrict__ keys, long long n, uint64_t invalid,
+                              int* __restrict__ flag) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  if (i == n) {
+    flag[i] = 0;
+    return;
+  }
+  uint64_t k = keys[i];
+  flag[i] = (k != invalid && (i == 0 || keys[i - 1] != k)) ? 1 : 0;
+}
+
+__global__ void k_unique_write(const uint64_t* __restrict__ keys, const int* __restrict__ scan, long long n,
+                               uint64_t invalid, uint64_t* __restrict__ out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint64_t k = keys[i];
+  if (k != invalid && (i == 0 || keys[i - 1] != k)) out[scan[i]] = k;
+}
+
+// Leaf containing octant `oct` (bit set = + side) of lattice point (x, y, z).
+__device__ __forceinline__ int locate(int x, int y, int z, int oct, const int* __restrict__ nd_child,
+                                      const int4* __restrict__ nd_org) {
+  int node = 0;
+  for (int guard = 0; guard < 64; ++guard) {
+    int ch = nd_child[node];
+    if (ch < 0) return node;
+    int4 o = nd_org[node];
+    int mid = o.w >> 1;
+    int bx = (x > o.x + mid || (x == o.x + mid && (oct & 1))) ? 1 : 0;
+    int by = (y > o.y + mid || (y == o.y + mid && (oct & 2))) ? 1 : 0;
+    int bz = (z > o.z + mid || (z == o.z + mid && (oct & 4))) ? 1 : 0;
+    node = ch + (bx | (by << 1) | (bz << 2));
+  }
+  return node;
+}
+
+__global__ void k_dual(const uint64_t* __restrict__ verts, long long nu, int B, const int* __restrict__ nd_child,
+                       const int4* __restrict__ nd_org, const float4* __restrict__ nd_v, int* __restrict__ cells,
+                       int* __restrict__ procs, int* __restrict__ tcount, unsigned long long* __restrict__ ndual) {
+  long long u = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u > nu) return;
+  if (u == nu) {
+    tcount[u] = 0;
+    return;
+  }
+  const uint64_t key = verts[u];
+  const uint64_t m = (1ull << B) - 1ull;
+  const int x = (int)((key >> (2 * B)) & m), y = (int)((key >> B) & m), z = (int)(key & m);
+  int n8[8];
+  int index = 0;
+  for (int c = 0; c < 8; ++c) {
+    n8[c] = locate(x, y, z, c, nd_child, nd_org);
+    if (nd_v[n8[c]].w > 0.f) index |= 1 << c;
+  }
+  const int code = c_code[index];
+  int nt = 0;
+  if (code != 0 && code != 255) {
+    nt = c_ntri[code];
+    for (int c = 0; c < 8; ++c) cells[8 * u + c] = n8[c_trans[index][c]];
+    atomicAdd(ndual, 1ull);
+  }
+  procs[u] = index;
+  tcount[u] = nt;
+}
+
+__global__ void k_tri_slots(long long nu, const int* __restrict__ cells, const int* __restrict__ procs,
+                            const int* __restrict__ toff, const uint64_t* __restrict__ nd_id, int id_bits,
+                            int packed, int* __restrict__ slotA, int* __restrict__ slotB,
+                            uint64_t* __restrict__ khi, uint64_t* __restrict__ klo, int8_t* __restrict__ tflip) {
+  long long u = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nu) return;
+  const int index = procs[u];
+  const int code = c_code[index];
+  if (code == 0 || code == 255) return;
+  const int nt = c_ntri[code];
+  const long long t0 = toff[u];
+  for (int t = 0; t < nt; ++t) {
+    tflip[t0 + t] = (int8_t)c_flip[index];
+    for (int k = 0; k < 3; ++k) {
+      int c0, c1;
+      edge_corners(c_tri[code][3 * t + k], &c0, &c1);
+      const int A = cells[8 * u + c0], Bn = cells[8 * u + c1];
+      const long long s = 3 * (t0 + t) + k;
+      slotA[s] = A;
+      slotB[s] = Bn;
+      uint64_t ia = nd_id[A], ib = nd_id[Bn];
+      uint64_t lo = ia < ib ? ia : ib, hi = ia < ib ? ib : ia;
+      if (packed) {
+        klo[s] = (lo << id_bits) | hi;
+      } else {
+        khi[s] = lo;
+        klo[s] = hi;
+      }
+    }
+  }
+}
+
+// group starts of a sorted (hi, lo) key sequence
+__global__ void k_group_flag(const uint64_t* __restrict__ hs, const uint64_t* __restrict__ ls, long long n,
+                             int* __restrict__ flag) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  if (i == n) {
+    flag[i] = 0;
+    return;
+  }
+  bool start = i == 0 || ls[i] != ls[i - 1] || (hs && hs[i] != hs[i - 1]);
+  flag[i] = start ? 1 : 0;
+}
+
+__global__ void k_vertex_map(const uint32_t* __restrict__ perm, const int* __restrict__ scan, long long n,
+                             int* __restrict__ slot_vertex, int* __restrict__ rep) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int start = scan[i + 1] - scan[i];
+  const int vid = scan[i] + start - 1;
+  slot_vertex[perm[i]] = vid;
+  if (start) rep[vid] = (int)perm[i];
+}
+
+struct BisectArgs {
+  GridView g;
+  PartView P;
+  float iso;
+  float rr;  // r / 2
+};
+
+__global__ void k_bisect(BisectArgs a, long long nv, const int* __restrict__ rep, const int* __restrict__ slotA,
+                         const int* __restrict__ slotB, const float4* __restrict__ nd_v,
+                         const uint64_t* __restrict__ nd_id, float* __restrict__ out,
+                         uint64_t* __restrict__ vkeys, unsigned long long* __restrict__ counters) {
+  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const int s = rep[v];
+  const int A = slotA[s], B = slotB[s];
+  float4 p = nd_v[A], q = nd_v[B];
+  const float dx = __fsub_rn(p.x, q.x), dy = __fsub_rn(p.y, q.y), dz = __fsub_rn(p.z, q.z);
+  float d = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fadd_rn(__fmul_rn(dy, dy), __fmul_rn(dz, dz))));
+  long long pairs = 0;
+  int steps = 0;
+  while (d > a.rr && steps < 64) {
+    float4 m;
+    m.x = __fmul_rn(__fadd_rn(p.x, q.x), 0.5f);
+    m.y = __fmul_rn(__fadd_rn(p.y, q.y), 0.5f);
+    m.z = __fmul_rn(__fadd_rn(p.z, q.z), 0.5f);
+    m.w = a.iso - field_sum(a.g, a.P, m.x, m.y, m.z, &pairs);
+    if ((m.w > 0.f) == (p.w > 0.f))
+      p = m;
+    else
+      q = m;
+    d = __fmul_rn(d, 0.5f);
+    ++steps;
+  }
+  const float ratio = __fdiv_rn(__fsub_rn(0.0f, p.w), __fsub_rn(q.w, p.w));
+  float3 r;
+  if ((double)ratio < 0.1) {
+    r = make_float3(p.x, p.y, p.z);
+  } else if ((double)ratio > 0.9) {
+    r = make_float3(q.x, q.y, q.z);
+  } else {
+    r.x = __fadd_rn(p.x, __fmul_rn(__fsub_rn(q.x, p.x), ratio));
+    r.y = __fadd_rn(p.y, __fmul_rn(__fsub_rn(q.y, p.y), ratio));
+    r.z = __fadd_rn(p.z, __fmul_rn(__fsub_rn(q.z, p.z), ratio));
+  }
+  out[3 * v] = r.x;
+  out[3 * v + 1] = r.y;
+  out[3 * v + 2] = r.z;
+  uint64_t ia = nd_id[A], ib = nd_id[B];
+  vkeys[2 * v] = ia < ib ? ia : ib;
+  vkeys[2 * v + 1] = ia < ib ? ib : ia;
+  atomicAdd(counters + 0, (unsigned long long)steps);
+  atomicAdd(counters + 1, (unsigned long long)pairs);
+}
+
+// Oriented triangle (Mesh::insert_tri argument order) and its sorted-triple key.
+__global__ void k_tri_keys(long long nt, const int* __restrict__ slot_vertex, const int8_t* __restrict__ tflip,
+                           int vbits, int packed, int* __restrict__ otri, uint64_t* __restrict__ khi,
+                           uint64_t* __restrict__ klo) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  int a = slot_vertex[3 * t], b = slot_vertex[3 * t + 1], c = slot_vertex[3 * t + 2];
+  int o0 = a, o1 = b, o2 = c;
+  if (!tflip[t]) {
+    o0 = c;
+    o2 = a;
+  }
+  otri[3 * t] = o0;
+  otri[3 * t + 1] = o1;
+  otri[3 * t + 2] = o2;
+  int s0 = min(a, min(b, c)), s2 = max(a, max(b, c));
+  int s1 = a + b + c - s0 - s2;
+  if (packed) {
+    klo[t] = ((uint64_t)s0 << (2 * vbits)) | ((uint64_t)s1 << vbits) | (uint64_t)s2;
+  } else {
+    khi[t] = (uint64_t)s0;
+    klo[t] = ((uint64_t)s1 << 32) | (uint64_t)s2;
+  }
+}
+
+__global__ void k_tri_write(const uint32_t* __restrict__ perm, const int* __restrict__ scan, long long n,
+                            const int* __restrict__ otri, int* __restrict__ out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (scan[i + 1] - scan[i]) {
+    const int t = (int)perm[i];
+    const int o = scan[i];
+    out[3 * o] = otri[3 * t];
+    out[3 * o + 1] = otri[3 * t + 1];
+    out[3 * o + 2] = otri[3 * t + 2];
+  }
+}
+
+__global__ void k_gather_u64(const uint64_t* __restrict__ src, const uint32_t* __restrict__ perm, long long n,
+                             uint64_t* __restrict__ dst) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[perm[i]];
+}
+
+__global__ void k_pack2(const uint64_t* __restrict__ hi, const uint64_t* __restrict__ lo, long long n,
+                        int lo_bits, uint64_t* __restrict__ out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (hi[i] << lo_bits) | lo[i];
+}
+
+static int bits_of(unsigned long long v) {
+  int b = 0;
+  while (b < 64 && (b == 64 ? false : (1ull << b) <= v)) ++b;
+  return b < 1 ? 1 : b;
+}
+
+// Stable sort of n keys given as (hi, lo) words (hi may be null); on return
+// perm holds the source index of each sorted position and hs/ls the sorted
+// words (hs unused when hi is null).
+static void sort_keys(pi_frame* f, const uint64_t* hi, const uint64_t* lo, long long n, int hi_bits, int lo_bits,
+                      DBuf<uint32_t>& perm, DBuf<uint64_t>& hs, DBuf<uint64_t>& ls) {
+  pi_ctx* c = f->ctx;
+  cudaStream_t s = c->stream;
+  DBuf<uint64_t> k1, k2;
+  DBuf<uint32_t> v1, v2;
+  k1.alloc(c, s, n);
+  k2.alloc(c, s, n);
+  v1.alloc(c, s, n);
+  v2.alloc(c, s, n);
+  DBuf<int> tmp;
+  tmp.alloc(c, s, radix_tmp_ints(n));
+  iota_u32(v1.p, n, s);
+  uint64_t *kp = k1.p, *ka = k2.p;
+  uint32_t *vp = v1.p, *va = v2.p;
+  if (!hi) {
+    PI_CUDA(cudaMemcpyAsync(k1.p, lo, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, s));
+    radix_sort_u64(&kp, &vp, &ka, &va, n, lo_bits, tmp.p, s);
+  } else {
+    PI_CUDA(cudaMemcpyAsync(k1.p, lo, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, s));
+    radix_sort_u64(&kp, &vp, &ka, &va, n, lo_bits, tmp.p, s);
+    PI_LAUNCH(k_gather_u64, div_up(n, 256), 256, 0, s, hi, vp, n, ka);
+    std::swap(kp, ka);
+    radix_sort_u64(&kp, &vp, &ka, &va, n, hi_bits, tmp.p, s);
+  }
+  perm.alloc(c, s, n);
+  PI_CUDA(cudaMemcpyAsync(perm.p, vp, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
+  ls.alloc(c, s, n);
+  PI_LAUNCH(k_gather_u64, div_up(n, 256), 256, 0, s, lo, perm.p, n, ls.p);
+  if (hi) {
+    hs.alloc(c, s, n);
+    PI_LAUNCH(k_gather_u64, div_up(n, 256), 256, 0, s, hi, perm.p, n, hs.p);
+  }
+}
+
+static int read_int(pi_frame* f, const int* d) {
+  int v = 0;
+  PI_CUDA(cudaMemcpyAsync(&v, d, sizeof(int), cudaMemcpyDeviceToHost, f->ctx->stream));
+  PI_CUDA(cudaStreamSynchronize(f->ctx->stream));
+  return v;
+}
+
+void stage_extract(pi_frame* f) {
+  pi_ctx* c = f->ctx;
+  cudaStream_t s = c->stream;
+  upload_tables(c->device);
+  const long long nn = f->nNodes;
+  // 1. leaves
+  DBuf<int> flag, leaves, tmp;
+  flag.alloc(c, s, nn + 1);
+  tmp.alloc(c, s, scan_tmp_ints(nn * 8 + 1));
+  PI_LAUNCH(k_leaf_flag, div_up(nn + 1, 256), 256, 0, s, f->nd_child.p, nn, flag.p);
+  exclusive_scan_i32(flag.p, flag.p, nn + 1, nullptr, tmp.p, s);
+  const long long nl = read_int(f, flag.p + nn);
+  f->nLeaves = nl;
+  leaves.alloc(c, s, nl > 0 ? nl : 1);
+  PI_LAUNCH(k_leaf_list, div_up(nn, 256), 256, 0, s, f->nd_child.p, flag.p, nn, leaves.p);
+  // 2. dual vertices = unique interior leaf corners
+  const int B = f->dmax + 1;
+  const int full = 1 << f->dmax;
+  const uint64_t invalid = (1ull << (3 * B)) - 1ull;
+  const long long nk = nl * 8;
+  DBuf<uint64_t> keys, keys2, uverts;
+  DBuf<uint32_t> vals, vals2;
+  keys.alloc(c, s, nk);
+  keys2.alloc(c, s, nk);
+  vals.alloc(c, s, nk);
+  vals2.alloc(c, s, nk);
+  PI_LAUNCH(k_corner_keys, div_up(nk, 256), 256, 0, s, leaves.p, nl, f->nd_org.p, full, B, keys.p, vals.p);
+  {
+    DBuf<int> rtmp;
+    rtmp.alloc(c, s, radix_tmp_ints(nk));
+    uint64_t *kp = keys.p, *ka = keys2.p;
+    uint32_t *vp = vals.p, *va = vals2.p;
+    radix_sort_u64(&kp, &vp, &ka, &va, nk, 3 * B, rtmp.p, s);
+    DBuf<int> uf;
+    uf.alloc(c, s, nk + 1);
+    PI_LAUNCH(k_unique_flag, div_up(nk + 1, 256), 256, 0, s, kp, nk, invalid, uf.p);
+    exclusive_scan_i32(uf.p, uf.p, nk + 1, nullptr, tmp.p, s);
+    const long long nu = read_int(f, uf.p + nk);
+    uverts.alloc(c, s, nu > 0 ? nu : 1);
+    PI_LAUNCH(k_unique_write, div_up(nk, 256), 256, 0, s, kp, uf.p, nk, invalid, uverts.p);
+    keys.release();
+    keys2.release();
+    vals.release();
+    vals2.release();
+    // 3. dual cells
+    DBuf<int> cells, procs, toff;
+    cells.alloc(c, s, nu * 8 > 0 ? nu * 8 : 1);
+    procs.alloc(c, s, nu > 0 ? nu : 1);
+    toff.alloc(c, s, nu + 1);
+    f->dcount.alloc(c, s, 8);
+    PI_CUDA(cudaMemsetAsync(f->dcount.p, 0, sizeof(unsigned long long) * 8, s));
+    PI_LAUNCH(k_dual, div_up(nu + 1, 128), 128, 0, s, uverts.p, nu, B, f->nd_child.p, f->nd_org.p, f->nd_v.p,
+              cells.p, procs.p, toff.p, f->dcount.p);
+    exclusive_scan_i32(toff.p, toff.p, nu + 1, nullptr, tmp.p, s);
+    const long long nt0 = read_int(f, toff.p + nu);
+    // 4. triangle slots and vertex keys
+    const int id_bits = 3 * f->dmax;
+    const int packed = (2 * id_bits <= 64) ? 1 : 0;
+    const long long ns = 3 * nt0;
+    DBuf<int> slotA, slotB;
+    DBuf<uint64_t> khi, klo;
+    DBuf<int8_t> tflip;
+    slotA.alloc(c, s, ns > 0 ? ns : 1);
+    slotB.alloc(c, s, ns > 0 ? ns : 1);
+    klo.alloc(c, s, ns > 0 ? ns : 1);
+    if (!packed) khi.alloc(c, s, ns > 0 ? ns : 1);
+    tflip.alloc(c, s, nt0 > 0 ? nt0 : 1);
+    PI_LAUNCH(k_tri_slots, div_up(nu, 128), 128, 0, s, nu, cells.p, procs.p, toff.p, f->nd_id.p, id_bits, packed,
+              slotA.p, slotB.p, khi.p, klo.p, tflip.p);
+    unsigned long long nd = 0;
+    PI_CUDA(cudaMemcpyAsync(&nd, f->dcount.p, sizeof(nd), cudaMemcpyDeviceToHost, s));
+    cells.release();
+    procs.release();
+    toff.release();
+    uverts.release();
+    // 5. unique mesh vertices
+    DBuf<uint32_t> perm;
+    DBuf<uint64_t> hs, ls;
+    sort_keys(f, packed ? nullptr : khi.p, klo.p, ns, id_bits, packed ? 2 * id_bits : id_bits, perm, hs, ls);
+    DBuf<int> vf, slot_vertex, rep;
+    vf.alloc(c, s, ns + 1);
+    if (tmp.n < scan_tmp_ints(ns + 1)) tmp.alloc(c, s, scan_tmp_ints(ns + 1));
+    PI_LAUNCH(k_group_flag, div_up(ns + 1, 256), 256, 0, s, packed ? nullptr : hs.p, ls.p, ns, vf.p);
+    exclusive_scan_i32(vf.p, vf.p, ns + 1, nullptr, tmp.p, s);
+    const long long nv = read_int(f, vf.p + ns);
+    f->nDual = (long long)nd;
+    slot_vertex.alloc(c, s, ns > 0 ? ns : 1);
+    rep.alloc(c, s, nv > 0 ? nv : 1);
+    PI_LAUNCH(k_vertex_map, div_up(ns, 256), 256, 0, s, perm.p, vf.p, ns, slot_vertex.p, rep.p);
+    // 6. vertex positions by bisection
+    f->nV = nv;
+    f->mv.alloc(c, s, nv * 3 > 0 ? nv * 3 : 3);
+    f->mk.alloc(c, s, nv * 2 > 0 ? nv * 2 : 2);
+    PI_CUDA(cudaMemsetAsync(f->dcount.p, 0, sizeof(unsigned long long) * 8, s));
+    const GridHost& gh = f->g;
+    BisectArgs ba{GridView{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p},
+                  PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p}, f->iso, f->P.radius / 2};
+    PI_LAUNCH(k_bisect, div_up(nv, 128), 128, 0, s, ba, nv, rep.p, slotA.p, slotB.p, f->nd_v.p, f->nd_id.p, f->mv.p,
+              f->mk.p, f->dcount.p);
+    // 7. triangles
+    const int vbits = bits_of((unsigned long long)(nv > 0 ? nv : 1));
+    const int tpacked = (3 * vbits <= 64) ? 1 : 0;
+    DBuf<int> otri;
+    DBuf<uint64_t> thi, tlo;
+    otri.alloc(c, s, nt0 * 3 > 0 ? nt0 * 3 : 3);
+    tlo.alloc(c, s, nt0 > 0 ? nt0 : 1);
+    if (!tpacked) thi.alloc(c, s, nt0 > 0 ? nt0 : 1);
+    PI_LAUNCH(k_tri_keys, div_up(nt0, 256), 256, 0, s, nt0, slot_vertex.p, tflip.p, vbits, tpacked, otri.p, thi.p,
+              tlo.p);
+    DBuf<uint32_t> tperm;
+    DBuf<uint64_t> ths, tls;
+    sort_keys(f, tpacked ? nullptr : thi.p, tlo.p, nt0, vbits, tpacked ? 3 * vbits : 64, tperm, ths, tls);
+    DBuf<int> tf;
+    tf.alloc(c, s, nt0 + 1);
+    PI_LAUNCH(k_group_flag, div_up(nt0 + 1, 256), 256, 0, s, tpacked ? nullptr : ths.p, tls.p, nt0, tf.p);
+    exclusive_scan_i32(tf.p, tf.p, nt0 + 1, nullptr, tmp.p, s);
+    const long long nt = read_int(f, tf.p + nt0);
+    f->nT = nt;
+    f->mt.alloc(c, s, nt * 3 > 0 ? nt * 3 : 3);
+    PI_LAUNCH(k_tri_write, div_up(nt0, 256), 256, 0, s, tperm.p, tf.p, nt0, otri.p, f->mt.p);
+    unsigned long long bc[2] = {0, 0};
+    PI_CUDA(cudaMemcpyAsync(bc, f->dcount.p, sizeof(bc), cudaMemcpyDeviceToHost, s));
+    PI_CUDA(cudaStreamSynchronize(s));
+    f->bisectEvals = (long long)bc[0];
+    f->fieldEvals += (long long)bc[0];
+    f->pairs += (long long)bc[1];
+  }
+}
+
+}  // namespace pisurf

@@ -1,0 +1,132 @@
+// Host-side context and frame state shared by the stage implementations.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "../../include/pisurf.h"
+#include "common.cuh"
+
+struct pi_ctx;
+
+namespace pisurf {
+
+void ctx_account(pi_ctx* c, long long delta);
+
+// Stream-ordered device buffer (cudaMallocAsync from the device's pool on the
+// context stream), counted against the context budget.
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  pi_ctx* ctx = nullptr;
+  cudaStream_t s = nullptr;
+  DBuf() = default;
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  void alloc(pi_ctx* c, cudaStream_t st, size_t count);
+  // grows to at least count elements keeping the first `keep` elements
+  void grow(pi_ctx* c, cudaStream_t st, size_t count, size_t keep);
+  void release();
+  ~DBuf() { release(); }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+struct GridHost {
+  float bounding[6];
+  float cell;
+  int nx, ny, nz;
+  long long cellNum;
+  int nInvalid;
+  int bits;  // radix sort width for key+1
+};
+
+}  // namespace pisurf
+
+struct pi_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  size_t budget = 0;
+  std::atomic<long long> used{0};
+  bool profile = false;
+  std::vector<cudaEvent_t> prof_events;  // pairs (start, stop)
+  double kernel_ms = 0;
+  int64_t kernel_launches = 0, kernel_pairs = 0, kernel_evals = 0;
+  int smCount = 0;
+};
+
+struct pi_frame {
+  pi_ctx* ctx = nullptr;
+  pi_params P;
+  int stage = 0;  // last completed: 0 none, 1 uploaded, 2 hash, 3 aniso, 4 normals, 5 octree, 6 mesh
+  long long N = 0;
+  pisurf::GridHost g;
+
+  pisurf::DBuf<float> xyz;       // N*3, original order
+  pisurf::DBuf<unsigned> misc;   // small scalars: bbox encodings, counters
+  pisurf::DBuf<int> key;         // N, original order, -1 outside the grid
+  pisurf::DBuf<uint32_t> sidx;   // N, IndexList: sorted position -> particle
+  pisurf::DBuf<uint32_t> skey;   // N, sorted key+1
+  pisurf::DBuf<int> off;         // C+1 cell offsets
+  pisurf::DBuf<float4> pos, xm, ga, gb, nrm;  // N, sorted order
+  pisurf::DBuf<float> gfull;     // N*9, sorted order (dumps)
+  pisurf::DBuf<float> det;       // N, sorted order (dumps)
+  pisurf::DBuf<int8_t> f64flag;  // N, sorted order
+  pisurf::DBuf<int> tmp;         // scan / sort scratch
+  pisurf::DBuf<uint32_t> u32a, u32b, u32c;  // sort ping-pong scratch
+
+  // scalars (Evaluator / SurfReconstructor members)
+  float iso = 0, maxScalar = -1, influ2 = 0, sigma = 0;
+  int dmax = 0, dmin = 0;
+  float rootC[3] = {0, 0, 0}, rootH = 0;
+  float bbox6[6] = {0, 0, 0, 0, 0, 0};  // loadRootBox tight box
+  bool singleLayer = false;
+
+  // octree, all levels concatenated in creation (level) order
+  long long nNodes = 0;
+  std::vector<long long> levelBegin;
+  pisurf::DBuf<float4> nd_c;     // center xyz, half
+  pisurf::DBuf<float4> nd_v;     // node xyz, value
+  pisurf::DBuf<uint64_t> nd_id;
+  pisurf::DBuf<int> nd_parent, nd_child;
+  pisurf::DBuf<int8_t> nd_type, nd_depth, nd_sc;
+  pisurf::DBuf<float> nd_curv;
+  pisurf::DBuf<int4> nd_org;     // integer origin at depth-max resolution, size
+  pisurf::DBuf<float> nd_samp;   // 27 sample values per node (QEF mode)
+
+  // mesh
+  long long nV = 0, nT = 0, nDual = 0;
+  pisurf::DBuf<float> mv;        // nV*3
+  pisurf::DBuf<int> mt;          // nT*3
+  pisurf::DBuf<uint64_t> mk;     // nV*2
+
+  // counters
+  long long fieldEvals = 0, pairs = 0, bisectEvals = 0, fp64Count = 0, nLeaves = 0, nEmpty = 0;
+  pisurf::DBuf<unsigned long long> dcount;  // device counters
+  cudaEvent_t ev[9] = {};
+  float stage_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+namespace pisurf {
+
+void stage_upload_host(pi_frame* f, const float* xyz, long long n);
+void stage_upload_device(pi_frame* f, const float* d_xyz, long long n);
+void stage_hashgrid(pi_frame* f);
+void stage_aniso(pi_frame* f);
+void stage_normals(pi_frame* f);
+void stage_octree(pi_frame* f);
+void stage_extract(pi_frame* f);
+void eval_points(pi_frame* f, const float* d_pts, long long m, float* d_val, float* d_grad);
+long long neighbors(pi_frame* f, const float* h_pts, long long m, long long* h_off, int* h_idx,
+                    long long cap);
+long long in_box(pi_frame* f, const float* b1, const float* b2, int* h_idx, long long cap);
+void dmc_host_table(int trans[256][8], bool flip[256], int code[256]);
+void prof_begin(pi_ctx* c, cudaStream_t s);
+void prof_end(pi_ctx* c, cudaStream_t s, long long pairs, long long evals);
+
+// Host scalar constants with the reference's float/double semantics.
+float bspline_host(float ratio, float sigma);
+
+}  // namespace pisurf

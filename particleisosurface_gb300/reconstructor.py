@@ -1,0 +1,172 @@
+"""Python facade with the reference's class and method names.
+
+    mesh = Mesh()
+    rec = SurfReconstructor(particles, radiuses, mesh, radius)
+    rec.Run(iso_factor, smooth_factor)          # src/surface_reconstructor.cpp:409
+    writeObjFile(mesh, "frame.obj")              # src/main.cpp:54
+
+Everything runs in the CUDA library through the C ABI (include/pisurf.h);
+the facade only moves arrays.  Reference interfaces mirrored:
+SurfReconstructor (include/surface_reconstructor.h:71-92), Evaluator
+(include/evaluator.h:76-95), HashGrid (include/hash_grid.h:16-38),
+Mesh (include/global.h:86-115).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _native as N
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = N.Context(0)
+    return _default_ctx
+
+
+class Mesh:
+    """Mesh container: vertices (float32 n x 3) and 1-based triangles, as the
+    reference's Mesh::vertices / Mesh::tris; vertex_keys hold the leaf-id pair
+    each vertex was inserted under (Mesh::insert_vert)."""
+
+    def __init__(self, mesh_precision=10000):
+        self.MESH_PRECISION = mesh_precision
+        self.reset()
+
+    def reset(self):
+        self.vertices = np.zeros((0, 3), np.float32)
+        self.tris = np.zeros((0, 3), np.int32)
+        self.vertex_keys = np.zeros((0, 2), np.uint64)
+
+    @property
+    def verticesNum(self):
+        return int(self.vertices.shape[0])
+
+    @property
+    def trianglesNum(self):
+        return int(self.tris.shape[0])
+
+
+def writeObjFile(mesh: Mesh, fn: str):
+    """writeObjFile (src/main.cpp:54-67): "v %f %f %f" then "f %d %d %d"."""
+    with open(fn, "w") as f:
+        for p in mesh.vertices:
+            f.write("v %f %f %f\n" % (p[0], p[1], p[2]))
+        for t in mesh.tris:
+            f.write("f %d %d %d\n" % (t[0], t[1], t[2]))
+
+
+class HashGrid:
+    def __init__(self, frame: N.Frame):
+        self._f = frame
+        info = frame.info()
+        self.Bounding = np.array(info["bounding"], np.float32)
+        self.CellSize = info["cell_size"]
+        self.XYZCellNum = np.array(info["xyz_cell_num"], np.int64)
+        self.CellNum = info["cell_num"]
+        self.ParticlesNum = info["num_particles"]
+
+    @property
+    def IndexList(self):
+        return self._f.dump(N.DUMP_INDEX_LIST)
+
+    def GetPIdxList(self, pos):
+        off, idx = self._f.neighbors(np.asarray(pos, np.float32).reshape(1, 3))
+        return idx[off[0]:off[1]].tolist()
+
+    def GetInBoxParticles(self, box1, box2):
+        return self._f.in_box(box1, box2).tolist()
+
+
+class Evaluator:
+    def __init__(self, frame: N.Frame):
+        self._f = frame
+
+    def SingleEval(self, pos):
+        return float(self._f.eval(np.asarray(pos, np.float32).reshape(1, 3))[0])
+
+    def SingleEvalWithGrad(self, pos):
+        s, g = self._f.eval(np.asarray(pos, np.float32).reshape(1, 3), grad=True)
+        return float(s[0]), g[0]
+
+    def eval_many(self, pts, grad=False):
+        return self._f.eval(pts, grad=grad)
+
+    def getIsoValue(self):
+        return self._f.info()["iso_value"]
+
+    def getMaxScalar(self):
+        return self._f.info()["max_scalar"]
+
+    @property
+    def GlobalxMeans(self):
+        return self._f.dump(N.DUMP_XMEANS)
+
+    @property
+    def GlobalGs(self):
+        return self._f.dump(N.DUMP_G)
+
+    @property
+    def GlobalDeterminant(self):
+        return self._f.dump(N.DUMP_DET)
+
+    @property
+    def PariclesNormals(self):
+        return self._f.dump(N.DUMP_NORMALS)
+
+
+class SurfReconstructor:
+    def __init__(self, particles, radiuses, mesh: Mesh, radius: float, ctx: N.Context | None = None,
+                 qef: bool = False):
+        self._particles = np.ascontiguousarray(np.asarray(particles, np.float32).reshape(-1, 3))
+        self._radius = float(radius)
+        self._mesh = mesh
+        self._ctx = ctx or default_context()
+        self._qef = qef
+        self._frame = None
+
+    def Run(self, iso_factor=1.9, smooth_factor=2.0):
+        self._mesh.reset()
+        params = N.default_params(self._radius, smooth_factor=smooth_factor, iso_factor=iso_factor, qef=self._qef)
+        self._frame = N.Frame(self._ctx, params).upload(self._particles).run()
+        v, t, k = self._frame.mesh(keys=True)
+        self._mesh.vertices = v
+        self._mesh.tris = t + 1
+        self._mesh.vertex_keys = k
+
+    def _info(self):
+        return self._frame.info()
+
+    def getDepthMax(self):
+        return self._info()["depth_max"]
+
+    def getDepthMin(self):
+        return self._info()["depth_min"]
+
+    def getOverSampleQEF(self):
+        return 2
+
+    def getConstRadius(self):
+        return self._radius
+
+    def getGlobalParticlesNum(self):
+        return int(self._particles.shape[0])
+
+    def getGlobalParticles(self):
+        return self._particles
+
+    def getHashGrid(self):
+        return HashGrid(self._frame)
+
+    def getEvaluator(self):
+        return Evaluator(self._frame)
+
+    def getRoot(self):
+        """All octree nodes (pi_node records, creation order); node 0 is the root."""
+        return self._frame.dump(N.DUMP_NODES)
+
+    def frame_info(self):
+        return self._info()

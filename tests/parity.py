@@ -1,0 +1,135 @@
+"""Canonical comparisons between the CUDA library and the oracle.
+
+Tolerances (stated once, used by the parity tests and the benchmark's error
+report):
+  FIELD_TOL   field values: |f_gpu - f_oracle| <= FIELD_TOL * MaxScalar.
+              The reference sums ~30 non-zero float terms of size <= Sigma
+              naively; the library sums compensated FP32; both are within a
+              few 1e-7 of the exact sum.
+  XMEAN_TOL   smoothed centres: |dx| <= XMEAN_TOL * r.
+  G_TOL       anisotropy matrices (entries O(1)) and determinants.
+  NORMAL_TOL  particle normals relative to the largest normal of the frame.
+  VERT_TOL    mesh vertex positions: |dp| <= VERT_TOL * r.
+  ISO_EPS     a sample whose oracle value is within ISO_EPS * MaxScalar of
+              zero may take the other sign (counted, reported).
+  CURV_EPS    a node whose curvature is within CURV_EPS of 0.99 may be
+              classified the other way (counted, reported).
+"""
+import numpy as np
+
+FIELD_TOL = 1e-5
+XMEAN_TOL = 1e-4
+G_TOL = 1e-4
+NORMAL_TOL = 1e-4
+VERT_TOL = 1e-3
+ISO_EPS = 1e-5
+CURV_EPS = 1e-4
+
+
+def sample_points(center, half):
+    """TNode::GenerateSampling (src/iso_method_ours.cpp:52-75) in float32."""
+    c = np.asarray(center, np.float32)
+    h = np.float32(half)
+    mn = c - h
+    mx = c + h
+    pts = np.empty((27, 3), np.float32)
+    for z in range(3):
+        for y in range(3):
+            for x in range(3):
+                i = z * 9 + y * 3 + x
+                t = np.array([x, y, z], np.float32) / np.float32(2)
+                pts[i] = (np.float32(1) - t) * mn + t * mx
+    return pts
+
+
+def node_table(nodes, fields=("type", "node", "curv", "signchange")):
+    """dict (depth, id) -> record, from an oracle nodes() dict or a GPU pi_node array."""
+    out = {}
+    if isinstance(nodes, dict):
+        for i in range(len(nodes["id"])):
+            out[(int(nodes["depth"][i]), int(nodes["id"][i]))] = (
+                int(nodes["type"][i]), nodes["node"][i], float(nodes["curv"][i]), int(nodes["signchange"][i]),
+                nodes["center"][i], float(nodes["half"][i]))
+    else:
+        for r in nodes:
+            out[(int(r["depth"]), int(r["id"]))] = (int(r["type"]), r["node"], float(r["curv"]),
+                                                   int(r["signchange"]), r["center"], float(r["half"]))
+    return out
+
+
+def compare_octrees(o_nodes, g_nodes, oracle, max_scalar, depth_min):
+    """Node-by-node comparison keyed by (depth, id).  Returns a report dict:
+    mismatched classifications, of which how many are explained by a sample
+    within ISO_EPS of the isovalue or a curvature within CURV_EPS of 0.99
+    (their subtrees are then skipped), and the max leaf-value difference."""
+    A = node_table(o_nodes)
+    B = node_table(g_nodes)
+    rep = dict(nodes_oracle=len(A), nodes_gpu=len(B), type_mismatch=0, explained=0, unexplained=[],
+               leaf_value_maxdiff=0.0, compared=0)
+    skip_prefix = set()
+
+    def under_skipped(key):
+        d, i = key
+        while d > 0:
+            d -= 1
+            i //= 8
+            if (d, i) in skip_prefix:
+                return True
+        return False
+
+    for key in sorted(A, key=lambda k: k[0]):
+        if under_skipped(key):
+            continue
+        if key not in B:
+            rep["unexplained"].append(("missing", key))
+            continue
+        ta, na, ca, sa, cen, half = A[key]
+        tb, nb, cb, sb, _, _ = B[key]
+        rep["compared"] += 1
+        if ta != tb:
+            rep["type_mismatch"] += 1
+            near = abs(ca - 0.99) < CURV_EPS
+            if not near and key[0] >= depth_min:
+                vals = oracle.eval(sample_points(cen, half))
+                near = np.min(np.abs(vals)) < ISO_EPS * max_scalar
+            if near:
+                rep["explained"] += 1
+                skip_prefix.add(key)
+            else:
+                rep["unexplained"].append(("type", key, ta, tb, ca, cb, sa, sb))
+            continue
+        if ta == 2:
+            rep["leaf_value_maxdiff"] = max(rep["leaf_value_maxdiff"], abs(float(na[3]) - float(nb[3])))
+    for key in B:
+        if key not in A and not under_skipped(key):
+            rep["unexplained"].append(("extra", key))
+    return rep
+
+
+def canonical_mesh(verts, tris, vkeys, one_based):
+    """Vertices keyed by their sorted leaf-id pair; triangles as rotated
+    triples of vertex keys (orientation kept, rotation normalised)."""
+    t = np.asarray(tris, np.int64) - (1 if one_based else 0)
+    keys = [(int(a), int(b)) for a, b in vkeys]
+    vmap = {k: verts[i] for i, k in enumerate(keys)}
+    tri = set()
+    for a, b, c in t:
+        ka, kb, kc = keys[a], keys[b], keys[c]
+        rots = [(ka, kb, kc), (kb, kc, ka), (kc, ka, kb)]
+        tri.add(min(rots))
+    return vmap, tri
+
+
+def compare_meshes(o_mesh, g_mesh, radius):
+    ov, ot, ok = o_mesh
+    gv, gt, gk = g_mesh
+    vo, to = canonical_mesh(ov, ot, ok, True)
+    vg, tg = canonical_mesh(gv, gt, gk, False)
+    common = set(vo) & set(vg)
+    d = np.array([np.max(np.abs(vo[k] - vg[k])) for k in common]) if common else np.zeros(1)
+    rep = dict(verts_oracle=len(vo), verts_gpu=len(vg), verts_only_oracle=len(set(vo) - set(vg)),
+               verts_only_gpu=len(set(vg) - set(vo)), tris_oracle=len(to), tris_gpu=len(tg),
+               tris_only_oracle=len(to - tg), tris_only_gpu=len(tg - to),
+               vert_maxdiff_over_r=float(d.max() / radius), vert_rmsdiff_over_r=float(np.sqrt(np.mean(d ** 2)) / radius),
+               verts_off_tol=int(np.sum(d > VERT_TOL * radius)))
+    return rep
