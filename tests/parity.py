@@ -2,10 +2,12 @@
 
 Tolerances (stated once, used by the parity tests and the benchmark's error
 report):
-  FIELD_TOL   field values: |f_gpu - f_oracle| <= FIELD_TOL * MaxScalar.
-              The reference sums ~30 non-zero float terms of size <= Sigma
-              naively; the library sums compensated FP32; both are within a
-              few 1e-7 of the exact sum.
+  FIELD_TOL_FP64  field values against the FP64 oracle (same float inputs,
+              double arithmetic): |f_gpu - f_64| <= FIELD_TOL_FP64 * MaxScalar.
+  FIELD_TOL   field values against the float oracle: the reference's own
+              float arithmetic is up to ~1.1e-5 * MaxScalar off the FP64
+              answer (G from a float SVD, naive float sums), so the bound is
+              the sum of both errors.
   XMEAN_TOL   smoothed centres: |dx| <= XMEAN_TOL * r.
   G_TOL       anisotropy matrices (entries O(1)) and determinants.
   NORMAL_TOL  particle normals relative to the largest normal of the frame.
@@ -17,7 +19,8 @@ report):
 """
 import numpy as np
 
-FIELD_TOL = 1e-5
+FIELD_TOL_FP64 = 1e-5
+FIELD_TOL = 3e-5
 XMEAN_TOL = 1e-4
 G_TOL = 1e-4
 NORMAL_TOL = 1e-4

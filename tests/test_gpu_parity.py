@@ -47,6 +47,19 @@ def run_pair(ctx, name):
     return _cache[name]
 
 
+_cache64 = {}
+
+
+def fp64_oracle(name):
+    if name not in _cache64:
+        fr = CASES[name]()
+        o64 = O.OracleFrame(fr.xyz, fr.radius, flags=O.FP64)
+        for s in (1, 2, 3):
+            o64.stage(s)
+        _cache64[name] = o64
+    return _cache64[name]
+
+
 @pytest.mark.parametrize("name", list(CASES))
 def test_hashgrid_bit_exact(ctx, name):
     fr, o, g = run_pair(ctx, name)
@@ -128,7 +141,13 @@ def test_field_and_gradient_within_tolerance(ctx, name):
     pts = (fr.xyz[rng.choice(fr.n, 2000)] + rng.normal(0, 1.5 * fr.radius, (2000, 3))).astype(np.float32)
     so, go = o.eval(pts, grad=True)
     sg, gg = g.eval(pts, grad=True)
+    s64 = fp64_oracle(name).eval(pts)
     ms = o.scalars()["max_scalar"]
+    e_gpu = np.abs(sg - s64) / ms
+    e_ref = np.abs(so - s64) / ms
+    print(name, "field err vs FP64: gpu max %.3e rms %.3e | float oracle max %.3e rms %.3e"
+          % (e_gpu.max(), np.sqrt(np.mean(e_gpu ** 2)), e_ref.max(), np.sqrt(np.mean(e_ref ** 2))))
+    assert e_gpu.max() <= PR.FIELD_TOL_FP64
     assert np.abs(sg - so).max() <= PR.FIELD_TOL * ms
     assert np.abs(gg - go).max() <= PR.NORMAL_TOL * max(np.abs(go).max(), 1e-30)
 
