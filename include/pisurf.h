@@ -120,6 +120,9 @@ int pi_frame_create(pi_ctx* ctx, const pi_params* params, pi_frame** out);
 int pi_frame_destroy(pi_frame* f);
 int pi_frame_upload(pi_frame* f, const float* xyz, int64_t n);        /* host xyz[n*3] */
 int pi_frame_upload_device(pi_frame* f, const float* d_xyz, int64_t n); /* device xyz[n*3] */
+/* Keeps the uploaded particles on the device and discards every later stage,
+ * so pi_run reconstructs the same frame again (a new Run on resident input). */
+int pi_frame_reset(pi_frame* f);
 
 /* The stages of SurfReconstructor::Run (src/surface_reconstructor.cpp:409-479),
  * each enqueued on the context stream and synchronised before return. */

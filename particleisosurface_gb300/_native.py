@@ -79,6 +79,7 @@ def _declare(L):
         "pi_frame_destroy": (C.c_int, [P]),
         "pi_frame_upload": (C.c_int, [P, fp, i64]),
         "pi_frame_upload_device": (C.c_int, [P, P, i64]),
+        "pi_frame_reset": (C.c_int, [P]),
         "pi_hashgrid_build": (C.c_int, [P]),
         "pi_aniso_compute": (C.c_int, [P]),
         "pi_normals_compute": (C.c_int, [P]),
@@ -228,6 +229,10 @@ class Frame:
     def upload_device(self, dptr, n):
         self.n = n
         check(lib().pi_frame_upload_device(self.h, C.c_void_p(dptr), n))
+        return self
+
+    def reset(self):
+        check(lib().pi_frame_reset(self.h))
         return self
 
     def hashgrid(self):

@@ -381,6 +381,17 @@ int pi_frame_upload_device(pi_frame* f, const float* d_xyz, int64_t n) {
   PI_API_END
 }
 
+int pi_frame_reset(pi_frame* f) {
+  PI_API_BEGIN
+  PI_CHECK(f, "frame is null");
+  need(f, 1);
+  f->stage = 1;
+  f->nNodes = f->nV = f->nT = f->nDual = 0;
+  f->fieldEvals = f->pairs = f->bisectEvals = f->fp64Count = f->nLeaves = f->nEmpty = 0;
+  for (int k = 0; k < 8; ++k) f->stage_ms[k] = 0;
+  PI_API_END
+}
+
 int pi_hashgrid_build(pi_frame* f) {
   PI_API_BEGIN
   PI_CHECK(f, "frame is null");
