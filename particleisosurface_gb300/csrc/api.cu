@@ -284,14 +284,21 @@ int pi_ctx_create(int device, size_t budget_bytes, pi_ctx** out) {
   PI_API_END
 }
 
-int pi_ctx_destroy(pi_ctx* c) {
-  PI_API_BEGIN
-  if (!c) return PI_OK;
-  set_device(c);
+static void ctx_release(pi_ctx* c) {
+  if (c->refs.fetch_sub(1) != 1) return;
+  cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   for (auto e : c->prof_events) cudaEventDestroy(e);
   cudaStreamDestroy(c->stream);
+  (void)cudaGetLastError();
   delete c;
+}
+
+int pi_ctx_destroy(pi_ctx* c) {
+  PI_API_BEGIN
+  if (!c) return PI_OK;
+  // frames still alive keep the context (and its stream) until they are destroyed
+  ctx_release(c);
   PI_API_END
 }
 
@@ -344,6 +351,7 @@ int pi_frame_create(pi_ctx* c, const pi_params* p, pi_frame** out) {
   pi_frame* f = new pi_frame();
   f->ctx = c;
   f->P = *p;
+  c->refs.fetch_add(1);
   *out = f;
   PI_API_END
 }
@@ -351,10 +359,12 @@ int pi_frame_create(pi_ctx* c, const pi_params* p, pi_frame** out) {
 int pi_frame_destroy(pi_frame* f) {
   PI_API_BEGIN
   if (!f) return PI_OK;
-  set_device(f->ctx);
+  pi_ctx* c = f->ctx;
+  set_device(c);
   for (auto& e : f->ev)
     if (e) cudaEventDestroy(e);
-  delete f;
+  delete f;  // device buffers are freed on the context stream
+  ctx_release(c);
   PI_API_END
 }
 

@@ -17,14 +17,18 @@ struct CudaError : std::runtime_error {
   CudaError(const std::string& s, int c) : std::runtime_error(s), code(c) {}
 };
 
+// Throws on failure after clearing the runtime's last-error slot, so that a
+// failed call is reported once and does not surface again at a later launch.
 #define PI_CUDA(call)                                                                   \
   do {                                                                                  \
     cudaError_t _e = (call);                                                            \
-    if (_e != cudaSuccess)                                                              \
+    if (_e != cudaSuccess) {                                                            \
+      (void)cudaGetLastError();                                                         \
       throw ::pisurf::CudaError(std::string(#call) + ": " + cudaGetErrorString(_e) +    \
                                     " (" + __FILE__ + ":" + std::to_string(__LINE__) + \
                                     ")",                                                \
                                 (int)_e);                                               \
+    }                                                                                   \
   } while (0)
 
 // Launch wrapper: counts the launch and checks the launch error.

@@ -55,6 +55,9 @@ struct pi_ctx {
   double kernel_ms = 0;
   int64_t kernel_launches = 0, kernel_pairs = 0, kernel_evals = 0;
   int smCount = 0;
+  // one reference for the owner plus one per live frame; the context is
+  // released when the last reference goes
+  std::atomic<int> refs{1};
 };
 
 struct pi_frame {
