@@ -167,6 +167,33 @@ int pi_reconstruct(pi_ctx* ctx, const pi_params* params, const float* xyz, int64
                    int64_t max_verts, int32_t* tris, int64_t max_tris, int64_t* nverts,
                    int64_t* ntris);
 
+/* Hash-grid build that performs no device allocation.  This entry point has
+ * no counterpart in the reference.  It is for host programs that cannot let a
+ * library call cudaMalloc once they run: ones that reserve the whole GPU for
+ * their own memory pool at start-up, or whose real-time rules forbid
+ * allocation after initialisation.  The caller passes device buffers:
+ * d_xyz[n*3] particles, and outputs d_keys[n] (cell key or -1, original
+ * order), d_index_list[n] (particles in cell order, HashGrid::IndexList) and
+ * d_cell_offsets[cell_offsets_len] (cell c holds d_index_list[off[c] ..
+ * off[c+1])); the grid parameters are returned in host memory.  The results
+ * equal pi_hashgrid_build's (PI_DUMP_KEYS / _INDEX_LIST / _CELL_OFFSETS).
+ * Temporaries live in a fixed 12.5 MiB array inside the library's device
+ * image, held on every GPU that loads the library until exit; so at most
+ * PI_NOALLOC_MAX_PARTICLES particles and PI_NOALLOC_MAX_CELLS hash cells
+ * (PI_ERR_LIMIT beyond them; also PI_ERR_LIMIT, with *cell_num_out set, when
+ * cell_offsets_len < cell count + 1).  The first call on a device looks up
+ * the array's device address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  All calls on a device
+ * share the array: calls whose GPU work may overlap (unordered streams) race
+ * and must be serialised by the caller.  Work runs on `stream` (a
+ * cudaStream_t, 0 for the default stream) and is complete on return. */
+#define PI_NOALLOC_MAX_PARTICLES 1048576
+#define PI_NOALLOC_MAX_CELLS 16777216
+int pi_hashgrid_build_noalloc(const float* d_xyz, int64_t n, float radius, int32_t* d_keys,
+                              int32_t* d_index_list, int32_t* d_cell_offsets, int64_t cell_offsets_len,
+                              float* bounding_out6, int32_t* xyz_cell_num_out3, int64_t* cell_num_out,
+                              void* stream);
+
 /* The dual-marching-cubes canonicalisation table the library uses
  * (include/visitorextract.h:35-293 in the reference). */
 int pi_dmc_table(int32_t* trans8x256, int8_t* flip256, int32_t* code256);
