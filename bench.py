@@ -59,7 +59,23 @@ def parse():
     p.add_argument("--n", type=int, default=1_000_000)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-evals", type=int, default=200_000)
+    p.add_argument("--single", action="store_true",
+                   help="reconstruct one frame once and print its counters (for profiler captures)")
     return p.parse_args()
+
+
+def single(a):
+    from particleisosurface_gb300 import _native as N
+    from particleisosurface_gb300 import build as B
+    B.build()
+    fr = make_frame(a.n)
+    ctx = N.Context(0)
+    f = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz).run()
+    info = f.info()
+    print(json.dumps({k: info[k] for k in ("num_nodes", "num_vertices", "num_triangles", "field_evals",
+                                           "candidate_pairs", "stage_ms")}))
+    f.close()
+    ctx.close()
 
 
 def dist_env():
@@ -323,7 +339,9 @@ def ours(a):
 
 def main():
     a = parse()
-    if a.impl == "reference":
+    if a.single:
+        single(a)
+    elif a.impl == "reference":
         reference_arm(a)
     else:
         ours(a)
