@@ -2,19 +2,29 @@
 //
 // The reference keeps a LIFO of nodes but processes the whole frontier at
 // once (inProcessSize = 10^7), so refinement is breadth-first: one level per
-// iteration.  Here each level is three launches:
-//   k_empty_curv  beforeSampleEval / checkEmptyAndCalcCurv (:152-235): one
-//                 warp per node walks the hash-cell rows of the node box and
-//                 tests particles against the box grown by r * smooth_factor;
-//                 nodes above D_min only need existence (early exit on ballot).
-//   k_sample      afterSampleEval (:237-273) with TNode::GenerateSampling /
-//                 NodeSampling / GridEval (src/iso_method_ours.cpp:52-99,
-//                 src/evaluator.cpp:127-252): one warp per node, lanes 0..26
-//                 evaluate the 3x3x3 samples, lane 27 the centre; the sign
-//                 change is a warp ballot.
-//   k_spawn       8 children per INTERNAL node (TNode ctor,
-//                 src/iso_method_ours.cpp:25-38) after an exclusive scan of
-//                 the INTERNAL flags.
+// iteration.  Per level:
+//   k_empty      emptiness of beforeSampleEval / checkEmptyAndCalcCurv
+//                (:152-235): one warp per node, an existence test with early
+//                exit over the hash cells that the node box grown by
+//                r * smooth_factor touches.  Every particle strictly inside
+//                the grown box lies in those cells (the float cell index is
+//                monotonic in the coordinate), and they lie inside the
+//                reference's block of box +- 1 cell, so the verdict is the
+//                reference's.
+//   k_q_count /  the 27 lattice samples and the centre of every non-empty
+//   k_q_place    node (TNode::GenerateSampling, src/iso_method_ours.cpp:52-75)
+//                are bucketed by hash cell with an atomic counting sort; the
+//                order inside a bucket does not affect any result.
+//   k_q_eval     field at the bucketed points (Evaluator::SingleEval,
+//                src/evaluator.cpp:60-87): lanes of a warp whose points share
+//                a cell walk that cell's 27-cell candidate list in lockstep,
+//                so candidate loads are broadcasts and loop bounds uniform.
+//   k_classify   afterSampleEval (:237-273): sign change against sample 0
+//                (ballot), leaf by size, and the normal-coherence curvature
+//                |sum n| / sum |n| computed only where the classification reads
+//                it (nodes with a sign change that are not leaves by size).
+//   k_spawn      8 children per INTERNAL node (TNode ctor,
+//                src/iso_method_ours.cpp:25-38) after a scan of the flags.
 #include <algorithm>
 #include <cmath>
 
@@ -25,13 +35,15 @@ namespace pisurf {
 
 enum : int8_t { T_EMPTY = 0, T_INTERNAL = 1, T_LEAF = 2, T_UNCERTAIN = 3 };
 
+constexpr int kQ = 28;  // 27 samples + the centre per node
+
 struct LevelArgs {
   GridView g;
-  float B1, B3, B5;  // Bounding upper corners
   const float4* pos;
   const float4* nrm;
-  float expand;      // r * smooth_factor
+  float expand;  // r * smooth_factor
   float iso;
+  float radius;
   long long lb, le;  // node range of the level
   int big;           // depth < D_min
 };
@@ -42,133 +54,236 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
-__global__ void k_empty_curv(LevelArgs a, const float4* __restrict__ nd_c, float4* __restrict__ nd_v,
-                             int8_t* __restrict__ nd_type, float* __restrict__ nd_curv) {
+// Node box grown by `expand` and the block of hash cells it touches.
+struct GrownBox {
+  float lox, loy, loz, hix, hiy, hiz;
+  int x0, x1, y0, y1, z0, z1;
+};
+
+__device__ __forceinline__ GrownBox grown_box(const GridView& g, float4 c, float expand) {
+  GrownBox b;
+  const float h = c.w;
+  b.lox = __fsub_rn(__fsub_rn(c.x, h), expand);
+  b.loy = __fsub_rn(__fsub_rn(c.y, h), expand);
+  b.loz = __fsub_rn(__fsub_rn(c.z, h), expand);
+  b.hix = __fadd_rn(__fadd_rn(c.x, h), expand);
+  b.hiy = __fadd_rn(__fadd_rn(c.y, h), expand);
+  b.hiz = __fadd_rn(__fadd_rn(c.z, h), expand);
+  b.x0 = max(cell_coord(b.lox, g.b0, g.cell, g.nx), 0);
+  b.y0 = max(cell_coord(b.loy, g.b2, g.cell, g.ny), 0);
+  b.z0 = max(cell_coord(b.loz, g.b4, g.cell, g.nz), 0);
+  b.x1 = min(cell_coord(b.hix, g.b0, g.cell, g.nx), g.nx - 1);
+  b.y1 = min(cell_coord(b.hiy, g.b2, g.cell, g.ny), g.ny - 1);
+  b.z1 = min(cell_coord(b.hiz, g.b4, g.cell, g.nz), g.nz - 1);
+  return b;
+}
+
+__device__ __forceinline__ bool inside(const GrownBox& b, float4 p) {
+  return p.x > b.lox && p.x < b.hix && p.y > b.loy && p.y < b.hiy && p.z > b.loz && p.z < b.hiz;
+}
+
+__global__ void k_empty(LevelArgs a, const float4* __restrict__ nd_c, float4* __restrict__ nd_v,
+                        int8_t* __restrict__ nd_type, float* __restrict__ nd_curv) {
   const long long node = a.lb + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (node >= a.le) return;
-  const float4 c = nd_c[node];
-  const float h = c.w;
-  const float b1x = __fsub_rn(c.x, h), b1y = __fsub_rn(c.y, h), b1z = __fsub_rn(c.z, h);
-  const float b2x = __fadd_rn(c.x, h), b2y = __fadd_rn(c.y, h), b2z = __fadd_rn(c.z, h);
-  const float lox = __fsub_rn(b1x, a.expand), loy = __fsub_rn(b1y, a.expand), loz = __fsub_rn(b1z, a.expand);
-  const float hix = __fadd_rn(b2x, a.expand), hiy = __fadd_rn(b2y, a.expand), hiz = __fadd_rn(b2z, a.expand);
-  // GetInBoxParticles cell block (src/hash_grid.cpp:164-194)
-  int mnx, mny, mnz, mxx, mxy, mxz;
-  cell_of(a.g, fmaxf(b1x, a.g.b0), fmaxf(b1y, a.g.b2), fmaxf(b1z, a.g.b4), mnx, mny, mnz);
-  cell_of(a.g, fminf(b2x, a.B1), fminf(b2y, a.B3), fminf(b2z, a.B5), mxx, mxy, mxz);
-  const int x0 = max(mnx - 1, 0), x1 = min(mxx + 1, a.g.nx - 1);
-  const int y0 = max(mny - 1, 0), y1 = min(mxy + 1, a.g.ny - 1);
-  const int z0 = max(mnz - 1, 0), z1 = min(mxz + 1, a.g.nz - 1);
+  const GrownBox b = grown_box(a.g, nd_c[node], a.expand);
   bool found = false;
-  Kahan sx, sy, sz, ar;
-  if (x0 <= x1) {
-    for (int z = z0; z <= z1; ++z) {
-      for (int y = y0; y <= y1; ++y) {
-        long long base = ((long long)z * a.g.ny + y) * a.g.nx;
-        int s = __ldg(a.g.off + base + x0), e = __ldg(a.g.off + base + x1 + 1);
+  if (b.x0 <= b.x1) {
+    for (int z = b.z0; z <= b.z1 && !found; ++z)
+      for (int y = b.y0; y <= b.y1 && !found; ++y) {
+        const long long base = ((long long)z * a.g.ny + y) * a.g.nx;
+        const int s = __ldg(a.g.off + base + b.x0), e = __ldg(a.g.off + base + b.x1 + 1);
         for (int j0 = s; j0 < e; j0 += 32) {
-          int j = j0 + lane;
-          bool in = false;
-          if (j < e) {
-            float4 p = __ldg(a.pos + j);
-            in = p.x > lox && p.x < hix && p.y > loy && p.y < hiy && p.z > loz && p.z < hiz;
-            if (in && !a.big) {
-              float4 nv = __ldg(a.nrm + j);
-              sx.add(nv.x);
-              sy.add(nv.y);
-              sz.add(nv.z);
-              ar.add(nv.w);
-            }
+          const int j = j0 + lane;
+          const bool in = j < e && inside(b, __ldg(a.pos + j));
+          if (__any_sync(0xffffffffu, in)) {
+            found = true;
+            break;
           }
-          found |= in;
-          if (a.big && __any_sync(0xffffffffu, found)) goto done;
         }
       }
-    }
   }
-done:
-  found = __any_sync(0xffffffffu, found);
-  float nx = warp_sum(sx.s + (-sx.c)), ny = warp_sum(sy.s + (-sy.c)), nz = warp_sum(sz.s + (-sz.c));
-  float area = warp_sum(ar.s + (-ar.c));
   if (lane == 0) {
-    float curv = (area == 0.f) ? 1.0f : sqrtf(nx * nx + ny * ny + nz * nz) / area;
-    nd_curv[node] = curv;
     if (!found) {
       nd_type[node] = T_EMPTY;
+      nd_curv[node] = 1.0f;  // area == 0
       float4 v = nd_v[node];
       v.w = a.iso;
       nd_v[node] = v;
     } else {
       nd_type[node] = a.big ? T_INTERNAL : T_UNCERTAIN;
+      nd_curv[node] = -1.0f;  // not needed unless a sign change asks for it
     }
   }
 }
 
-struct SampleArgs {
+// Sample s (< 27) of the node lattice, or the node position (s == 27).
+__device__ __forceinline__ void sample_point(const float4 c, const float4 v, int s, float& qx, float& qy,
+                                             float& qz) {
+  if (s < 27) {
+    const float h = c.w;
+    const float tx = (s % 3) * 0.5f, ty = ((s / 3) % 3) * 0.5f, tz = (s / 9) * 0.5f;
+    qx = __fadd_rn(__fmul_rn(1.0f - tx, __fsub_rn(c.x, h)), __fmul_rn(tx, __fadd_rn(c.x, h)));
+    qy = __fadd_rn(__fmul_rn(1.0f - ty, __fsub_rn(c.y, h)), __fmul_rn(ty, __fadd_rn(c.y, h)));
+    qz = __fadd_rn(__fmul_rn(1.0f - tz, __fsub_rn(c.z, h)), __fmul_rn(tz, __fadd_rn(c.z, h)));
+  } else {
+    qx = v.x, qy = v.y, qz = v.z;
+  }
+}
+
+struct QArgs {
   GridView g;
   PartView P;
   float iso;
-  float radius;
   long long lb, le;
-  int qef;
+  int ekx, eky;  // extended key strides (nx + 4, ny + 4)
 };
 
-__global__ void k_sample(SampleArgs a, const float4* __restrict__ nd_c, float4* __restrict__ nd_v,
-                         int8_t* __restrict__ nd_type, int8_t* __restrict__ nd_sc,
-                         const float* __restrict__ nd_curv, float* __restrict__ nd_samp,
+// Hash cell of a point as a key over the grid grown by 2 cells on each side
+// (cell_coord clamps to [-2, n + 1]).
+__device__ __forceinline__ int ext_key(const QArgs& a, int cx, int cy, int cz) {
+  return ((cz + 2) * a.eky + (cy + 2)) * a.ekx + (cx + 2);
+}
+
+__global__ void k_q_count(QArgs a, const float4* __restrict__ nd_c, const float4* __restrict__ nd_v,
+                          const int8_t* __restrict__ nd_type, int* __restrict__ qcnt, int* __restrict__ qkey,
+                          int* __restrict__ qslot) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long node = a.lb + i / kQ;
+  if (node >= a.le) return;
+  if (nd_type[node] != T_UNCERTAIN) {
+    qkey[i] = -1;
+    return;
+  }
+  float qx, qy, qz;
+  sample_point(nd_c[node], nd_v[node], (int)(i % kQ), qx, qy, qz);
+  int cx, cy, cz;
+  cell_of(a.g, qx, qy, qz, cx, cy, cz);
+  const int k = ext_key(a, cx, cy, cz);
+  qkey[i] = k;
+  qslot[i] = atomicAdd(qcnt + k, 1);
+}
+
+__global__ void k_q_place(long long n, const int* __restrict__ qkey, const int* __restrict__ qslot,
+                          const int* __restrict__ qoff, int* __restrict__ order) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int k = qkey[i];
+  if (k >= 0) order[qoff[k] + qslot[i]] = (int)i;
+}
+
+__global__ void k_q_eval(QArgs a, const int* __restrict__ order, const int* __restrict__ total_ptr,
+                         const float4* __restrict__ nd_c, const float4* __restrict__ nd_v, float* __restrict__ qval,
                          unsigned long long* __restrict__ counters) {
+  const int lane = threadIdx.x & 31;
+  const long long wbase = ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
+  const long long total = *total_ptr;
+  if (wbase >= total) return;
+  const long long idx = wbase + lane;
+  const bool active = idx < total;
+  int q = 0, cx = 0, cy = 0, cz = 0, key = -1;
+  float qx = 0.f, qy = 0.f, qz = 0.f;
+  if (active) {
+    q = order[idx];
+    const long long node = a.lb + q / kQ;
+    sample_point(nd_c[node], nd_v[node], q % kQ, qx, qy, qz);
+    cell_of(a.g, qx, qy, qz, cx, cy, cz);
+    key = ext_key(a, cx, cy, cz);
+  }
+  Kahan acc;
+  long long pairs = 0;
+  unsigned todo = __ballot_sync(0xffffffffu, active);
+  while (todo) {
+    const int leader = __ffs(todo) - 1;
+    const int lkey = __shfl_sync(0xffffffffu, key, leader);
+    const unsigned grp = __ballot_sync(0xffffffffu, active && key == lkey);
+    const int gx = __shfl_sync(0xffffffffu, cx, leader);
+    const int gy = __shfl_sync(0xffffffffu, cy, leader);
+    const int gz = __shfl_sync(0xffffffffu, cz, leader);
+    const bool mine = (grp >> lane) & 1u;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy) {
+        int s, e;
+        if (!nb_row(a.g, gx, gy + dy, gz + dz, &s, &e)) continue;
+        if (mine) pairs += e - s;
+#pragma unroll 2
+        for (int j = s; j < e; ++j) {
+          const float4 x = __ldg(a.P.xm + j);
+          const float dx = qx - x.x, dyy = qy - x.y, dzz = qz - x.z;
+          const float e2 = fmaf(dx, dx, fmaf(dyy, dyy, dzz * dzz));
+          if (mine && e2 < x.w) {
+            const float4 ga = __ldg(a.P.ga + j);
+            const float4 gb = __ldg(a.P.gb + j);
+            float u0, u1, u2;
+            amul(ga, gb, dx, dyy, dzz, u0, u1, u2);
+            const float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
+            if (s2 < 4.0f) acc.add(gb.z * bspline_s2(s2));
+          }
+        }
+      }
+    todo &= ~grp;
+  }
+  if (active) qval[q] = a.iso - acc.s;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+  if (lane == 0) atomicAdd(counters + 1, (unsigned long long)pairs);
+}
+
+__global__ void k_classify(LevelArgs a, const float* __restrict__ qval, const float4* __restrict__ nd_c,
+                           float4* __restrict__ nd_v, int8_t* __restrict__ nd_type, int8_t* __restrict__ nd_sc,
+                           float* __restrict__ nd_curv, float* __restrict__ nd_samp, int qef,
+                           unsigned long long* __restrict__ counters) {
   const long long node = a.lb + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (node >= a.le) return;
   if (nd_type[node] != T_UNCERTAIN) return;  // warp-uniform
-  const float4 c = nd_c[node];
-  const float h = c.w;
-  float qx, qy, qz;
-  if (lane < 27) {
-    const int ix = lane % 3, iy = (lane / 3) % 3, iz = lane / 9;
-    const float mn[3] = {__fsub_rn(c.x, h), __fsub_rn(c.y, h), __fsub_rn(c.z, h)};
-    const float mx[3] = {__fadd_rn(c.x, h), __fadd_rn(c.y, h), __fadd_rn(c.z, h)};
-    const float t[3] = {ix * 0.5f, iy * 0.5f, iz * 0.5f};
-    qx = __fadd_rn(__fmul_rn(1.0f - t[0], mn[0]), __fmul_rn(t[0], mx[0]));
-    qy = __fadd_rn(__fmul_rn(1.0f - t[1], mn[1]), __fmul_rn(t[1], mx[1]));
-    qz = __fadd_rn(__fmul_rn(1.0f - t[2], mn[2]), __fmul_rn(t[2], mx[2]));
-  } else {
-    const float4 v = nd_v[node];
-    qx = v.x, qy = v.y, qz = v.z;
-  }
-  long long pairs = 0;
-  float val = 0.f;
-  if (lane < 28) val = a.iso - field_sum(a.g, a.P, qx, qy, qz, &pairs);
+  const long long qb = (node - a.lb) * kQ;
+  const float val = lane < kQ ? qval[qb + lane] : 0.f;
   // GridEval sign change against sample 0, ">= 0" (src/evaluator.cpp:169-172)
-  unsigned pos_mask = __ballot_sync(0xffffffffu, lane < 27 && val >= 0.f);
-  bool origin = pos_mask & 1u;
-  bool signchange = origin ? (pos_mask != 0x07ffffffu) : (pos_mask != 0u);
-  float vc = __shfl_sync(0xffffffffu, val, 27);
-  if (a.qef && lane < 27) nd_samp[node * 27 + lane] = val;
-  // pair count for the kernel roofline
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+  const unsigned pos_mask = __ballot_sync(0xffffffffu, lane < 27 && val >= 0.f);
+  const bool origin = pos_mask & 1u;
+  const bool signchange = origin ? (pos_mask != 0x07ffffffu) : (pos_mask != 0u);
+  const float vc = __shfl_sync(0xffffffffu, val, 27);
+  if (qef && lane < 27) nd_samp[node * 27 + lane] = val;
+  const float4 c = nd_c[node];
+  const float cellsize = 2.0f * c.w;
+  const bool leaf_by_size = (double)(cellsize - a.radius) < 1e-8;
+  int8_t type = T_LEAF;
+  float curv = -1.0f;
+  if (!leaf_by_size && signchange) {
+    // checkEmptyAndCalcCurv sums over particles inside the grown box
+    const GrownBox b = grown_box(a.g, c, a.expand);
+    Kahan sx, sy, sz, ar;
+    for (int z = b.z0; z <= b.z1; ++z)
+      for (int y = b.y0; y <= b.y1; ++y) {
+        const long long base = ((long long)z * a.g.ny + y) * a.g.nx;
+        const int s = __ldg(a.g.off + base + b.x0), e = __ldg(a.g.off + base + b.x1 + 1);
+        for (int j = s + lane; j < e; j += 32) {
+          if (inside(b, __ldg(a.pos + j))) {
+            const float4 nv = __ldg(a.nrm + j);
+            sx.add(nv.x);
+            sy.add(nv.y);
+            sz.add(nv.z);
+            ar.add(nv.w);
+          }
+        }
+      }
+    const float nx = warp_sum(sx.s - sx.c), ny = warp_sum(sy.s - sy.c), nz = warp_sum(sz.s - sz.c);
+    const float area = warp_sum(ar.s - ar.c);
+    curv = (area == 0.f) ? 1.0f : sqrtf(nx * nx + ny * ny + nz * nz) / area;
+    if ((double)curv < 0.99) type = T_INTERNAL;
+  }
   if (lane == 0) {
-    const float cellsize = 2.0f * h;
-    const float curv = nd_curv[node];
-    int8_t type;
-    if ((double)(cellsize - a.radius) < 1e-8) {
-      type = T_LEAF;
-    } else if (signchange && (double)curv < 0.99) {
-      type = T_INTERNAL;
-    } else {
-      type = T_LEAF;
-    }
     nd_type[node] = type;
     nd_sc[node] = signchange ? 1 : 0;
+    if (curv >= 0.f) nd_curv[node] = curv;
     if (type == T_LEAF) {
       float4 v = nd_v[node];
       v.w = vc;
       nd_v[node] = v;
     }
     atomicAdd(counters + 0, (unsigned long long)(27 + (type == T_LEAF ? 1 : 0)));
-    atomicAdd(counters + 1, (unsigned long long)pairs);
   }
 }
 
@@ -180,11 +295,10 @@ __global__ void k_internal_flag(const int8_t* __restrict__ nd_type, long long lb
 }
 
 __global__ void k_spawn(long long lb, long long le, long long cbase, const int* __restrict__ rank,
-                        const int8_t* __restrict__ nd_type, int child_depth, float4* __restrict__ nd_c,
+                        const int8_t* nd_type, int child_depth, float4* __restrict__ nd_c,
                         float4* __restrict__ nd_v, uint64_t* __restrict__ nd_id, int* __restrict__ nd_parent,
-                        int* __restrict__ nd_child, int8_t* __restrict__ nd_ctype,
-                        int8_t* __restrict__ nd_depth, int8_t* __restrict__ nd_sc, float* __restrict__ nd_curv,
-                        int4* __restrict__ nd_org) {
+                        int* __restrict__ nd_child, int8_t* nd_ctype, int8_t* __restrict__ nd_depth,
+                        int8_t* __restrict__ nd_sc, float* __restrict__ nd_curv, int4* __restrict__ nd_org) {
   long long i = lb + (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= le) return;
   if (nd_type[i] != T_INTERNAL) {
@@ -262,24 +376,40 @@ void stage_octree(pi_frame* f) {
   const GridHost& gh = f->g;
   GridView g{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p};
   PartView P{f->pos.p, f->xm.p, f->ga.p, f->gb.p};
+  const int ekx = gh.nx + 4, eky = gh.ny + 4;
+  const long long ek = (long long)ekx * eky * (gh.nz + 4);
   f->dcount.alloc(ctx, s, 8);
   PI_CUDA(cudaMemsetAsync(f->dcount.p, 0, sizeof(unsigned long long) * 8, s));
-  DBuf<int> flag;
+  DBuf<int> flag, qcnt, qkey, qslot, order;
+  DBuf<float> qval;
+  qcnt.alloc(ctx, s, ek + 1);
   long long lb = 0, le = 1;
   for (int depth = 0;; ++depth) {
     f->levelBegin.push_back(lb);
     const long long nl = le - lb;
-    LevelArgs la{g, gh.bounding[1], gh.bounding[3], gh.bounding[5], f->pos.p, f->nrm.p,
-                 f->P.radius * f->P.smooth_factor, f->iso, lb, le, depth < f->dmin ? 1 : 0};
+    LevelArgs la{g, f->pos.p, f->nrm.p, f->P.radius * f->P.smooth_factor, f->iso, f->P.radius, lb, le,
+                 depth < f->dmin ? 1 : 0};
     const int wpb = 8;  // warps per block
-    PI_LAUNCH(k_empty_curv, div_up(nl, wpb), 32 * wpb, 0, s, la, f->nd_c.p, f->nd_v.p, f->nd_type.p,
-              f->nd_curv.p);
+    PI_LAUNCH(k_empty, div_up(nl, wpb), 32 * wpb, 0, s, la, f->nd_c.p, f->nd_v.p, f->nd_type.p, f->nd_curv.p);
     if (depth >= f->dmin) {
-      SampleArgs sa{g, P, f->iso, f->P.radius, lb, le, f->P.qef};
+      const long long qn = nl * kQ;
+      if (f->tmp.n < scan_tmp_ints(ek + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(ek + 1));
+      qkey.alloc(ctx, s, qn);
+      qslot.alloc(ctx, s, qn);
+      qval.alloc(ctx, s, qn);
+      order.alloc(ctx, s, qn);
+      PI_CUDA(cudaMemsetAsync(qcnt.p, 0, sizeof(int) * (ek + 1), s));
+      QArgs qa{g, P, f->iso, lb, le, ekx, eky};
+      PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p,
+                qslot.p);
+      exclusive_scan_i32(qcnt.p, qcnt.p, ek + 1, nullptr, f->tmp.p, s);
+      PI_LAUNCH(k_q_place, div_up(qn, 256), 256, 0, s, qn, qkey.p, qslot.p, qcnt.p, order.p);
       prof_begin(ctx, s);
-      PI_LAUNCH(k_sample, div_up(nl, wpb), 32 * wpb, 0, s, sa, f->nd_c.p, f->nd_v.p, f->nd_type.p, f->nd_sc.p,
-                f->nd_curv.p, f->nd_samp.p, f->dcount.p);
+      PI_LAUNCH(k_q_eval, div_up(div_up(qn, 32), wpb), 32 * wpb, 0, s, qa, order.p, qcnt.p + ek, f->nd_c.p,
+                f->nd_v.p, qval.p, f->dcount.p);
       prof_end(ctx, s, -1, -1);
+      PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, f->nd_c.p, f->nd_v.p, f->nd_type.p,
+                f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, f->dcount.p);
     }
     flag.alloc(ctx, s, nl + 1);
     if (f->tmp.n < scan_tmp_ints(nl + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(nl + 1));
