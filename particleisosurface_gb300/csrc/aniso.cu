@@ -181,7 +181,7 @@ __global__ void k_cov_G(GridView g, const float4* __restrict__ pos, const float4
     for (int k = 0; k < 6; ++k) a6d[k] = (double)a6[k];
     sym_eig3<double>(a6d, wd, Vd);
     g_from_eig<double>(wd, Vd, G, &stretch);
-    atomicAdd(f64count, 1ull);
+    stripe_add(f64count, 0, 1ull);
   } else {
     g_from_eig<float>(w, V, G, &stretch);
   }
@@ -220,15 +220,13 @@ void stage_aniso(pi_frame* f) {
   f->gfull.alloc(f->ctx, s, n * 9);
   f->det.alloc(f->ctx, s, n);
   f->f64flag.alloc(f->ctx, s, n);
-  f->dcount.alloc(f->ctx, s, 8);
-  PI_CUDA(cudaMemsetAsync(f->dcount.p, 0, sizeof(unsigned long long) * 8, s));
+  counters_reset(f);
   PI_LAUNCH(k_xmean, div_up(n, 128), 128, 0, s, g, f->pos.p, n, nI, nI2, inv_h3, c_self, c_mean, f->nrm.p);
   PI_LAUNCH(k_cov_G, div_up(n, 128), 128, 0, s, g, f->pos.p, f->nrm.p, f->xm.p, n, nI, nI2, inv_h3, f->influ2,
             1.0f / h, f->sigma, f->ga.p, f->gb.p, f->gfull.p, f->det.p, f->f64flag.p, f->dcount.p);
-  unsigned long long c = 0;
-  PI_CUDA(cudaMemcpyAsync(&c, f->dcount.p, sizeof(c), cudaMemcpyDeviceToHost, s));
-  PI_CUDA(cudaStreamSynchronize(s));
-  f->fp64Count = (long long)c;
+  unsigned long long c[8];
+  counters_read(f, c);
+  f->fp64Count = (long long)c[0];
 }
 
 }  // namespace pisurf

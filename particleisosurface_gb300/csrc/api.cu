@@ -101,6 +101,24 @@ float bspline_host(float ratio, float sigma) {
   return 0.0f;
 }
 
+void counters_reset(pi_frame* f) {
+  cudaStream_t s = f->ctx->stream;
+  if (f->dcount.n < (size_t)kCounterWords) f->dcount.alloc(f->ctx, s, kCounterWords);
+  PI_CUDA(cudaMemsetAsync(f->dcount.p, 0, sizeof(unsigned long long) * kCounterWords, s));
+}
+
+void counters_read(pi_frame* f, unsigned long long out[8]) {
+  cudaStream_t s = f->ctx->stream;
+  std::vector<unsigned long long> h(kCounterWords);
+  PI_CUDA(cudaMemcpyAsync(h.data(), f->dcount.p, sizeof(unsigned long long) * kCounterWords,
+                          cudaMemcpyDeviceToHost, s));
+  PI_CUDA(cudaStreamSynchronize(s));
+  for (int w = 0; w < 8; ++w) {
+    out[w] = 0;
+    for (int k = 0; k < kStripes; ++k) out[w] += h[((size_t)w * kStripes + k) * 4];
+  }
+}
+
 void prof_begin(pi_ctx* c, cudaStream_t s) {
   if (!c->profile) return;
   cudaEvent_t e;

@@ -43,6 +43,11 @@ struct CudaError : std::runtime_error {
 
 inline unsigned int div_up(long long a, long long b) { return (unsigned int)((a + b - 1) / b); }
 
+// Striped device event counters (see stripe_add in device.cuh): 8 counters x
+// 64 stripes, 32 bytes apart.
+constexpr int kStripes = 64;
+constexpr int kCounterWords = 8 * kStripes * 4;
+
 // ---------------------------------------------------------------------------
 // Scan (exclusive, int32) and stable LSD radix sort (u32/u64 keys, u32
 // values).  Implemented in sort.cu.

@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "common.cuh"
+
 namespace pisurf {
 
 struct GridView {
@@ -32,6 +34,14 @@ struct PartView {
   const float4* ga;
   const float4* gb;
 };
+
+// Event counters (field evaluations, candidate pairs, ...) striped over 64
+// slots 32 bytes apart, so that many warps adding to one counter do not
+// serialise on a single address.  Counter w, stripe k lives at
+// c[(w * kStripes + k) * 4]; the host sums the stripes.
+__device__ __forceinline__ void stripe_add(unsigned long long* c, int w, unsigned long long v) {
+  if (v) atomicAdd(c + ((size_t)w * kStripes + (blockIdx.x & (kStripes - 1))) * 4, v);
+}
 
 struct Kahan {
   float s = 0.f, c = 0.f;

@@ -156,7 +156,7 @@ __global__ void k_dual(const uint64_t* __restrict__ verts, long long nu, int B, 
   if (code != 0 && code != 255) {
     nt = c_ntri[code];
     for (int c = 0; c < 8; ++c) cells[8 * u + c] = n8[c_trans[index][c]];
-    atomicAdd(ndual, 1ull);
+    stripe_add(ndual, 2, 1ull);
   }
   procs[u] = index;
   tcount[u] = nt;
@@ -267,8 +267,8 @@ __global__ void k_bisect(BisectArgs a, long long nv, const int* __restrict__ rep
   uint64_t ia = nd_id[A], ib = nd_id[B];
   vkeys[2 * v] = ia < ib ? ia : ib;
   vkeys[2 * v + 1] = ia < ib ? ib : ia;
-  atomicAdd(counters + 0, (unsigned long long)steps);
-  atomicAdd(counters + 1, (unsigned long long)pairs);
+  stripe_add(counters, 3, (unsigned long long)steps);
+  stripe_add(counters, 4, (unsigned long long)pairs);
 }
 
 // Oriented triangle (Mesh::insert_tri argument order) and its sorted-triple key.
@@ -421,8 +421,7 @@ void stage_extract(pi_frame* f) {
     cells.alloc(c, s, nu * 8 > 0 ? nu * 8 : 1);
     procs.alloc(c, s, nu > 0 ? nu : 1);
     toff.alloc(c, s, nu + 1);
-    f->dcount.alloc(c, s, 8);
-    PI_CUDA(cudaMemsetAsync(f->dcount.p, 0, sizeof(unsigned long long) * 8, s));
+    counters_reset(f);
     PI_LAUNCH(k_dual, div_up(nu + 1, 128), 128, 0, s, uverts.p, nu, B, f->nd_child.p, f->nd_org.p, f->nd_v.p,
               cells.p, procs.p, toff.p, f->dcount.p);
     exclusive_scan_i32(toff.p, toff.p, nu + 1, nullptr, tmp.p, s);
@@ -441,8 +440,6 @@ void stage_extract(pi_frame* f) {
     tflip.alloc(c, s, nt0 > 0 ? nt0 : 1);
     PI_LAUNCH(k_tri_slots, div_up(nu, 128), 128, 0, s, nu, cells.p, procs.p, toff.p, f->nd_id.p, id_bits, packed,
               slotA.p, slotB.p, khi.p, klo.p, tflip.p);
-    unsigned long long nd = 0;
-    PI_CUDA(cudaMemcpyAsync(&nd, f->dcount.p, sizeof(nd), cudaMemcpyDeviceToHost, s));
     cells.release();
     procs.release();
     toff.release();
@@ -457,7 +454,6 @@ void stage_extract(pi_frame* f) {
     PI_LAUNCH(k_group_flag, div_up(ns + 1, 256), 256, 0, s, packed ? nullptr : hs.p, ls.p, ns, vf.p);
     exclusive_scan_i32(vf.p, vf.p, ns + 1, nullptr, tmp.p, s);
     const long long nv = read_int(f, vf.p + ns);
-    f->nDual = (long long)nd;
     slot_vertex.alloc(c, s, ns > 0 ? ns : 1);
     rep.alloc(c, s, nv > 0 ? nv : 1);
     PI_LAUNCH(k_vertex_map, div_up(ns, 256), 256, 0, s, perm.p, vf.p, ns, slot_vertex.p, rep.p);
@@ -465,7 +461,6 @@ void stage_extract(pi_frame* f) {
     f->nV = nv;
     f->mv.alloc(c, s, nv * 3 > 0 ? nv * 3 : 3);
     f->mk.alloc(c, s, nv * 2 > 0 ? nv * 2 : 2);
-    PI_CUDA(cudaMemsetAsync(f->dcount.p, 0, sizeof(unsigned long long) * 8, s));
     const GridHost& gh = f->g;
     BisectArgs ba{GridView{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p},
                   PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p}, f->iso, f->P.radius / 2};
@@ -492,12 +487,12 @@ void stage_extract(pi_frame* f) {
     f->nT = nt;
     f->mt.alloc(c, s, nt * 3 > 0 ? nt * 3 : 3);
     PI_LAUNCH(k_tri_write, div_up(nt0, 256), 256, 0, s, tperm.p, tf.p, nt0, otri.p, f->mt.p);
-    unsigned long long bc[2] = {0, 0};
-    PI_CUDA(cudaMemcpyAsync(bc, f->dcount.p, sizeof(bc), cudaMemcpyDeviceToHost, s));
-    PI_CUDA(cudaStreamSynchronize(s));
-    f->bisectEvals = (long long)bc[0];
-    f->fieldEvals += (long long)bc[0];
-    f->pairs += (long long)bc[1];
+    unsigned long long bc[8];
+    counters_read(f, bc);
+    f->nDual = (long long)bc[2];
+    f->bisectEvals = (long long)bc[3];
+    f->fieldEvals += (long long)bc[3];
+    f->pairs += (long long)bc[4];
   }
 }
 

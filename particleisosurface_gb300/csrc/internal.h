@@ -129,6 +129,11 @@ void dmc_host_table(int trans[256][8], bool flip[256], int code[256]);
 void prof_begin(pi_ctx* c, cudaStream_t s);
 void prof_end(pi_ctx* c, cudaStream_t s, long long pairs, long long evals);
 
+// Striped device counters of a frame: zero them / read and sum the stripes
+// (synchronises the context stream).
+void counters_reset(pi_frame* f);
+void counters_read(pi_frame* f, unsigned long long out[8]);
+
 // Host scalar constants with the reference's float/double semantics.
 float bspline_host(float ratio, float sigma);
 

@@ -82,12 +82,27 @@ __device__ __forceinline__ bool inside(const GrownBox& b, float4 p) {
   return p.x > b.lox && p.x < b.hix && p.y > b.loy && p.y < b.hiy && p.z > b.loz && p.z < b.hiz;
 }
 
+// Particle range of cell c (linear index over the block) of a grown box.
+__device__ __forceinline__ void block_cell(const GridView& g, const GrownBox& b, int c, int* s, int* e) {
+  const int nxb = b.x1 - b.x0 + 1, nyb = b.y1 - b.y0 + 1;
+  const int x = b.x0 + c % nxb, y = b.y0 + (c / nxb) % nyb, z = b.z0 + c / (nxb * nyb);
+  const long long k = ((long long)z * g.ny + y) * g.nx + x;
+  *s = __ldg(g.off + k);
+  *e = __ldg(g.off + k + 1);
+}
+
+__device__ __forceinline__ int block_cells(const GrownBox& b) {
+  if (b.x0 > b.x1 || b.y0 > b.y1 || b.z0 > b.z1) return 0;
+  return (b.x1 - b.x0 + 1) * (b.y1 - b.y0 + 1) * (b.z1 - b.z0 + 1);
+}
+
 __global__ void k_empty(LevelArgs a, const float4* __restrict__ nd_c, float4* __restrict__ nd_v,
                         int8_t* __restrict__ nd_type, float* __restrict__ nd_curv) {
   const long long node = a.lb + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (node >= a.le) return;
   const GrownBox b = grown_box(a.g, nd_c[node], a.expand);
+  // rows of the cell block, 32 particles at a time; stop at the first hit
   bool found = false;
   if (b.x0 <= b.x1) {
     for (int z = b.z0; z <= b.z1 && !found; ++z)
@@ -146,23 +161,38 @@ __device__ __forceinline__ int ext_key(const QArgs& a, int cx, int cy, int cz) {
   return ((cz + 2) * a.eky + (cy + 2)) * a.ekx + (cx + 2);
 }
 
+// Bucket of a sample: its hash cell (extended key) times 8 plus the octant of
+// the cell it lies in, so that a warp's points are close together.  Slots
+// within a bucket come from one warp-aggregated atomic per bucket and warp.
 __global__ void k_q_count(QArgs a, const float4* __restrict__ nd_c, const float4* __restrict__ nd_v,
                           const int8_t* __restrict__ nd_type, int* __restrict__ qcnt, int* __restrict__ qkey,
                           int* __restrict__ qslot) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
   const long long node = a.lb + i / kQ;
-  if (node >= a.le) return;
-  if (nd_type[node] != T_UNCERTAIN) {
-    qkey[i] = -1;
-    return;
+  const bool in_level = node < a.le;
+  const bool valid = in_level && nd_type[node] == T_UNCERTAIN;
+  int k = -1;
+  if (valid) {
+    float qx, qy, qz;
+    sample_point(nd_c[node], nd_v[node], (int)(i % kQ), qx, qy, qz);
+    int cx, cy, cz;
+    cell_of(a.g, qx, qy, qz, cx, cy, cz);
+    const float fx = __fdiv_rn(__fsub_rn(qx, a.g.b0), a.g.cell) - (float)cx;
+    const float fy = __fdiv_rn(__fsub_rn(qy, a.g.b2), a.g.cell) - (float)cy;
+    const float fz = __fdiv_rn(__fsub_rn(qz, a.g.b4), a.g.cell) - (float)cz;
+    const int oct = (fx >= 0.5f ? 1 : 0) | (fy >= 0.5f ? 2 : 0) | (fz >= 0.5f ? 4 : 0);
+    k = ext_key(a, cx, cy, cz) * 8 + oct;
   }
-  float qx, qy, qz;
-  sample_point(nd_c[node], nd_v[node], (int)(i % kQ), qx, qy, qz);
-  int cx, cy, cz;
-  cell_of(a.g, qx, qy, qz, cx, cy, cz);
-  const int k = ext_key(a, cx, cy, cz);
-  qkey[i] = k;
-  qslot[i] = atomicAdd(qcnt + k, 1);
+  const unsigned peers = __match_any_sync(0xffffffffu, k);
+  const int leader = __ffs(peers) - 1;
+  int base = 0;
+  if (valid && lane == leader) base = atomicAdd(qcnt + k, __popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (in_level) {
+    qkey[i] = k;
+    if (valid) qslot[i] = base + __popc(peers & ((1u << lane) - 1u));
+  }
 }
 
 __global__ void k_q_place(long long n, const int* __restrict__ qkey, const int* __restrict__ qslot,
@@ -227,12 +257,12 @@ __global__ void k_q_eval(QArgs a, const int* __restrict__ order, const int* __re
   if (active) qval[q] = a.iso - acc.s;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
-  if (lane == 0) atomicAdd(counters + 1, (unsigned long long)pairs);
+  if (lane == 0) stripe_add(counters, 1, (unsigned long long)pairs);
 }
 
 __global__ void k_classify(LevelArgs a, const float* __restrict__ qval, const float4* __restrict__ nd_c,
                            float4* __restrict__ nd_v, int8_t* __restrict__ nd_type, int8_t* __restrict__ nd_sc,
-                           float* __restrict__ nd_curv, float* __restrict__ nd_samp, int qef,
+                           float* __restrict__ nd_curv, float* __restrict__ nd_samp, int qef, int curv_known,
                            unsigned long long* __restrict__ counters) {
   const long long node = a.lb + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
@@ -251,24 +281,28 @@ __global__ void k_classify(LevelArgs a, const float* __restrict__ qval, const fl
   const bool leaf_by_size = (double)(cellsize - a.radius) < 1e-8;
   int8_t type = T_LEAF;
   float curv = -1.0f;
-  if (!leaf_by_size && signchange) {
+  if (!leaf_by_size && signchange && curv_known) {
+    curv = nd_curv[node];  // summed by the parent's scan (k_spawn_scan)
+    if ((double)curv < 0.99) type = T_INTERNAL;
+  } else if (!leaf_by_size && signchange) {
     // checkEmptyAndCalcCurv sums over particles inside the grown box
     const GrownBox b = grown_box(a.g, c, a.expand);
     Kahan sx, sy, sz, ar;
-    for (int z = b.z0; z <= b.z1; ++z)
-      for (int y = b.y0; y <= b.y1; ++y) {
-        const long long base = ((long long)z * a.g.ny + y) * a.g.nx;
-        const int s = __ldg(a.g.off + base + b.x0), e = __ldg(a.g.off + base + b.x1 + 1);
-        for (int j = s + lane; j < e; j += 32) {
-          if (inside(b, __ldg(a.pos + j))) {
-            const float4 nv = __ldg(a.nrm + j);
-            sx.add(nv.x);
-            sy.add(nv.y);
-            sz.add(nv.z);
-            ar.add(nv.w);
-          }
+    const int ncell = block_cells(b);
+    for (int c0 = lane; c0 < ncell; c0 += 32) {
+      int s, e;
+      block_cell(a.g, b, c0, &s, &e);
+      for (int j = s; j < e; ++j) {
+        const float4 p = __ldg(a.pos + j);
+        if (inside(b, p)) {
+          const float4 nv = __ldg(a.nrm + j);
+          sx.add(nv.x);
+          sy.add(nv.y);
+          sz.add(nv.z);
+          ar.add(nv.w);
         }
       }
+    }
     const float nx = warp_sum(sx.s - sx.c), ny = warp_sum(sy.s - sy.c), nz = warp_sum(sz.s - sz.c);
     const float area = warp_sum(ar.s - ar.c);
     curv = (area == 0.f) ? 1.0f : sqrtf(nx * nx + ny * ny + nz * nz) / area;
@@ -283,7 +317,7 @@ __global__ void k_classify(LevelArgs a, const float* __restrict__ qval, const fl
       v.w = vc;
       nd_v[node] = v;
     }
-    atomicAdd(counters + 0, (unsigned long long)(27 + (type == T_LEAF ? 1 : 0)));
+    stripe_add(counters, 0, (unsigned long long)(27 + (type == T_LEAF ? 1 : 0)));
   }
 }
 
@@ -324,6 +358,111 @@ __global__ void k_spawn(long long lb, long long le, long long cbase, const int* 
     nd_depth[b + k] = (int8_t)child_depth;
     nd_sc[b + k] = 0;
     nd_curv[b + k] = 0.f;
+    nd_org[b + k] = make_int4(po.x + ((k & 1) ? hs : 0), po.y + ((k & 2) ? hs : 0), po.z + ((k & 4) ? hs : 0), hs);
+  }
+}
+
+// Spawns the 8 children of each INTERNAL node and settles their emptiness
+// and curvature sums in one scan of the parent's grown box: every child's box
+// grown by r * smooth_factor lies inside the parent's, and each particle is
+// tested against the children's float bounds exactly as the child itself
+// would compute them (checkEmptyAndCalcCurv, src/surface_reconstructor.cpp:
+// 152-222).  One warp per parent; lane k writes child k.
+__global__ void k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict__ rank, int child_depth,
+                             float4* __restrict__ nd_c, float4* __restrict__ nd_v, uint64_t* __restrict__ nd_id,
+                             int* __restrict__ nd_parent, int* __restrict__ nd_child, int8_t* nd_type,
+                             int8_t* __restrict__ nd_depth, int8_t* __restrict__ nd_sc, float* __restrict__ nd_curv,
+                             int4* __restrict__ nd_org) {
+  const long long i = a.lb + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= a.le) return;
+  if (nd_type[i] != T_INTERNAL) {
+    if (lane == 0) nd_child[i] = -1;
+    return;
+  }
+  const long long b = cbase + 8LL * rank[i - a.lb];
+  const float4 pc = nd_c[i];
+  const float hc = pc.w / 2;
+  const float e = a.expand;
+  const float pcs[3] = {pc.x, pc.y, pc.z};
+  float ctr[3][2], clo[3][2], chi[3][2];
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+    for (int bit = 0; bit < 2; ++bit) {
+      const float c = __fadd_rn(pcs[ax], bit ? hc : -hc);
+      ctr[ax][bit] = c;
+      clo[ax][bit] = __fsub_rn(__fsub_rn(c, hc), e);
+      chi[ax][bit] = __fadd_rn(__fadd_rn(c, hc), e);
+    }
+  // the parent's grown box is the union: low child's lo to high child's hi
+  GrownBox pb;
+  pb.lox = clo[0][0], pb.loy = clo[1][0], pb.loz = clo[2][0];
+  pb.hix = chi[0][1], pb.hiy = chi[1][1], pb.hiz = chi[2][1];
+  pb.x0 = max(cell_coord(pb.lox, a.g.b0, a.g.cell, a.g.nx), 0);
+  pb.y0 = max(cell_coord(pb.loy, a.g.b2, a.g.cell, a.g.ny), 0);
+  pb.z0 = max(cell_coord(pb.loz, a.g.b4, a.g.cell, a.g.nz), 0);
+  pb.x1 = min(cell_coord(pb.hix, a.g.b0, a.g.cell, a.g.nx), a.g.nx - 1);
+  pb.y1 = min(cell_coord(pb.hiy, a.g.b2, a.g.cell, a.g.ny), a.g.ny - 1);
+  pb.z1 = min(cell_coord(pb.hiz, a.g.b4, a.g.cell, a.g.nz), a.g.nz - 1);
+  unsigned found = 0;
+  float sum[8][4];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) sum[k][0] = sum[k][1] = sum[k][2] = sum[k][3] = 0.f;
+  if (pb.x0 <= pb.x1) {
+    for (int z = pb.z0; z <= pb.z1; ++z)
+      for (int y = pb.y0; y <= pb.y1; ++y) {
+        const long long base = ((long long)z * a.g.ny + y) * a.g.nx;
+        const int s = __ldg(a.g.off + base + pb.x0), en = __ldg(a.g.off + base + pb.x1 + 1);
+        for (int j = s + lane; j < en; j += 32) {
+          const float4 p = __ldg(a.pos + j);
+          const int mx = ((p.x > clo[0][0] && p.x < chi[0][0]) ? 1 : 0) | ((p.x > clo[0][1] && p.x < chi[0][1]) ? 2 : 0);
+          const int my = ((p.y > clo[1][0] && p.y < chi[1][0]) ? 1 : 0) | ((p.y > clo[1][1] && p.y < chi[1][1]) ? 2 : 0);
+          const int mz = ((p.z > clo[2][0] && p.z < chi[2][0]) ? 1 : 0) | ((p.z > clo[2][1] && p.z < chi[2][1]) ? 2 : 0);
+          if (mx && my && mz) {
+            unsigned m8 = 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+              if (((mx >> (k & 1)) & 1) && ((my >> ((k >> 1) & 1)) & 1) && ((mz >> ((k >> 2) & 1)) & 1)) m8 |= 1u << k;
+            found |= m8;
+            const float4 nv = __ldg(a.nrm + j);
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+              if ((m8 >> k) & 1u) {
+                sum[k][0] += nv.x;
+                sum[k][1] += nv.y;
+                sum[k][2] += nv.z;
+                sum[k][3] += nv.w;
+              }
+          }
+        }
+      }
+  }
+  found = __reduce_or_sync(0xffffffffu, found);
+  float mine[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float t = warp_sum(sum[k][q]);
+      if (lane == k) mine[q] = t;
+    }
+  if (lane == 0) nd_child[i] = (int)b;
+  if (lane < 8) {
+    const int k = lane;
+    const int4 po = nd_org[i];
+    const int hs = po.w >> 1;
+    const float4 cc = make_float4(ctr[0][k & 1], ctr[1][(k >> 1) & 1], ctr[2][(k >> 2) & 1], hc);
+    const bool nonempty = (found >> k) & 1u;
+    nd_c[b + k] = cc;
+    nd_v[b + k] = make_float4(cc.x, cc.y, cc.z, nonempty ? 0.f : a.iso);
+    nd_id[b + k] = nd_id[i] * 8ull + (uint64_t)k;
+    nd_parent[b + k] = (int)i;
+    nd_child[b + k] = -1;
+    nd_type[b + k] = nonempty ? T_UNCERTAIN : T_EMPTY;
+    nd_depth[b + k] = (int8_t)child_depth;
+    nd_sc[b + k] = 0;
+    nd_curv[b + k] = (mine[3] == 0.f) ? 1.0f : sqrtf(mine[0] * mine[0] + mine[1] * mine[1] + mine[2] * mine[2]) / mine[3];
     nd_org[b + k] = make_int4(po.x + ((k & 1) ? hs : 0), po.y + ((k & 2) ? hs : 0), po.z + ((k & 4) ? hs : 0), hs);
   }
 }
@@ -377,20 +516,21 @@ void stage_octree(pi_frame* f) {
   GridView g{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p};
   PartView P{f->pos.p, f->xm.p, f->ga.p, f->gb.p};
   const int ekx = gh.nx + 4, eky = gh.ny + 4;
-  const long long ek = (long long)ekx * eky * (gh.nz + 4);
-  f->dcount.alloc(ctx, s, 8);
-  PI_CUDA(cudaMemsetAsync(f->dcount.p, 0, sizeof(unsigned long long) * 8, s));
+  const long long ek = (long long)ekx * eky * (gh.nz + 4) * 8;  // buckets: cell x octant
+  counters_reset(f);
   DBuf<int> flag, qcnt, qkey, qslot, order;
   DBuf<float> qval;
   qcnt.alloc(ctx, s, ek + 1);
   long long lb = 0, le = 1;
+  bool known = false;  // emptiness and curvature of this level settled by the parents' scan
   for (int depth = 0;; ++depth) {
     f->levelBegin.push_back(lb);
     const long long nl = le - lb;
     LevelArgs la{g, f->pos.p, f->nrm.p, f->P.radius * f->P.smooth_factor, f->iso, f->P.radius, lb, le,
                  depth < f->dmin ? 1 : 0};
     const int wpb = 8;  // warps per block
-    PI_LAUNCH(k_empty, div_up(nl, wpb), 32 * wpb, 0, s, la, f->nd_c.p, f->nd_v.p, f->nd_type.p, f->nd_curv.p);
+    if (!known)
+      PI_LAUNCH(k_empty, div_up(nl, wpb), 32 * wpb, 0, s, la, f->nd_c.p, f->nd_v.p, f->nd_type.p, f->nd_curv.p);
     if (depth >= f->dmin) {
       const long long qn = nl * kQ;
       if (f->tmp.n < scan_tmp_ints(ek + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(ek + 1));
@@ -409,7 +549,7 @@ void stage_octree(pi_frame* f) {
                 f->nd_v.p, qval.p, f->dcount.p);
       prof_end(ctx, s, -1, -1);
       PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, f->nd_c.p, f->nd_v.p, f->nd_type.p,
-                f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, f->dcount.p);
+                f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p);
     }
     flag.alloc(ctx, s, nl + 1);
     if (f->tmp.n < scan_tmp_ints(nl + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(nl + 1));
@@ -421,18 +561,24 @@ void stage_octree(pi_frame* f) {
     PI_CUDA(cudaStreamSynchronize(s));
     const long long newn = 8LL * nint;
     ensure_nodes(f, le + newn);
-    PI_LAUNCH(k_spawn, div_up(nl, 256), 256, 0, s, lb, le, le, flag.p, f->nd_type.p, depth + 1, f->nd_c.p,
-              f->nd_v.p, f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p,
-              f->nd_curv.p, f->nd_org.p);
+    known = nint > 0 && depth + 1 >= f->dmin && depth < f->dmax;
+    if (known) {
+      PI_LAUNCH(k_spawn_scan, div_up(nl, wpb), 32 * wpb, 0, s, la, le, flag.p, depth + 1, f->nd_c.p, f->nd_v.p,
+                f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p, f->nd_curv.p,
+                f->nd_org.p);
+    } else {
+      PI_LAUNCH(k_spawn, div_up(nl, 256), 256, 0, s, lb, le, le, flag.p, f->nd_type.p, depth + 1, f->nd_c.p,
+                f->nd_v.p, f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p,
+                f->nd_curv.p, f->nd_org.p);
+    }
     f->nNodes = le + newn;
     // depth D_max nodes are leaves by size, so nothing spawns past it
     if (nint == 0 || depth >= f->dmax) break;
     lb = le;
     le = le + newn;
   }
-  unsigned long long cnt[2];
-  PI_CUDA(cudaMemcpyAsync(cnt, f->dcount.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
-  PI_CUDA(cudaStreamSynchronize(s));
+  unsigned long long cnt[8];
+  counters_read(f, cnt);
   f->fieldEvals = (long long)cnt[0];
   f->pairs = (long long)cnt[1];
 }
