@@ -67,6 +67,10 @@ typedef struct pi_frame_info {
   int64_t fp64_eigen;       /* particles whose eigen-decomposition ran in FP64 */
   float stage_ms[8];        /* device time of upload, hash, aniso, normals, octree, qef,
                                extract, download */
+  int64_t qef_accepted;     /* leaves whose QEF vertex lies in the cell (qef mode) */
+  int64_t qef_singular;     /* leaves whose normal matrix is singular and whose
+                               pseudo-inverse point lies in the cell; rejected, as
+                               the reference's non-finite inverse is */
 } pi_frame_info;
 
 /* Parity dumps (pi_stage_dump).  Arrays are in original particle order unless
@@ -80,6 +84,7 @@ typedef struct pi_frame_info {
 #define PI_DUMP_NORMALS 7     /* float[N*3] Evaluator::PariclesNormals */
 #define PI_DUMP_NODES 8       /* pi_node[num_nodes], creation (level) order */
 #define PI_DUMP_FP64_FLAGS 9  /* int8[N] 1 where the eigen step ran in FP64 */
+#define PI_DUMP_QEF_SAMPLES 10 /* float[num_nodes*27] GridEval sample values (qef mode) */
 
 typedef struct pi_node {
   uint64_t id;      /* TNode::id */

@@ -18,7 +18,7 @@ PI_OK = 0
 ERRORS = {-1: "PI_ERR_INVALID", -2: "PI_ERR_CUDA", -3: "PI_ERR_NOMEM", -4: "PI_ERR_STATE", -5: "PI_ERR_LIMIT"}
 
 DUMP_KEYS, DUMP_INDEX_LIST, DUMP_CELL_OFFSETS, DUMP_XMEANS, DUMP_G, DUMP_DET, DUMP_NORMALS, DUMP_NODES, \
-    DUMP_FP64_FLAGS = range(1, 10)
+    DUMP_FP64_FLAGS, DUMP_QEF_SAMPLES = range(1, 11)
 
 
 class PiError(RuntimeError):
@@ -41,7 +41,7 @@ class FrameInfo(C.Structure):
                 ("num_leaves", C.c_int64), ("num_empty", C.c_int64), ("num_dual_cells", C.c_int64),
                 ("num_vertices", C.c_int64), ("num_triangles", C.c_int64), ("field_evals", C.c_int64),
                 ("candidate_pairs", C.c_int64), ("bisection_evals", C.c_int64), ("fp64_eigen", C.c_int64),
-                ("stage_ms", C.c_float * 8)]
+                ("stage_ms", C.c_float * 8), ("qef_accepted", C.c_int64), ("qef_singular", C.c_int64)]
 
     def as_dict(self):
         out = {}
@@ -321,7 +321,7 @@ class Frame:
             DUMP_CELL_OFFSETS: (np.int32, (-1,)), DUMP_XMEANS: (np.float32, (-1, 3)),
             DUMP_G: (np.float32, (-1, 3, 3)), DUMP_DET: (np.float32, (-1,)),
             DUMP_NORMALS: (np.float32, (-1, 3)), DUMP_NODES: (NODE_DTYPE, (-1,)),
-            DUMP_FP64_FLAGS: (np.int8, (-1,)),
+            DUMP_FP64_FLAGS: (np.int8, (-1,)), DUMP_QEF_SAMPLES: (np.float32, (-1, 27)),
         }[what]
         buf = np.empty(nb.value // np.dtype(dtype).itemsize, dtype)
         check(lib().pi_stage_dump(self.h, what, buf.ctypes.data_as(C.c_void_p), nb.value))

@@ -495,6 +495,8 @@ int pi_frame_info_get(const pi_frame* f, pi_frame_info* o) {
   o->bisection_evals = f->bisectEvals;
   o->fp64_eigen = f->fp64Count;
   for (int k = 0; k < 8; ++k) o->stage_ms[k] = f->stage_ms[k];
+  o->qef_accepted = f->qefAccepted;
+  o->qef_singular = f->qefSingular;
   PI_API_END
 }
 
@@ -591,6 +593,7 @@ static size_t dump_size(const pi_frame* f, int what) {
     case PI_DUMP_NORMALS: return sizeof(float) * 3 * f->N;
     case PI_DUMP_NODES: return sizeof(pi_node) * f->nNodes;
     case PI_DUMP_FP64_FLAGS: return sizeof(int8_t) * f->N;
+    case PI_DUMP_QEF_SAMPLES: return f->P.qef ? sizeof(float) * 27 * f->nNodes : 0;
   }
   return 0;
 }
@@ -696,6 +699,13 @@ int pi_stage_dump(pi_frame* f, int what, void* buf, size_t bytes) {
         o[i].signchange = sc[i];
         o[i].pad = 0;
       }
+      break;
+    }
+    case PI_DUMP_QEF_SAMPLES: {
+      need(f, 5);
+      PI_CHECK(f->P.qef, "QEF samples exist only in qef mode");
+      auto x = d2h(f->nd_samp.p, 27 * f->nNodes, s);
+      std::memcpy(buf, x.data(), sizeof(float) * 27 * f->nNodes);
       break;
     }
     default:

@@ -107,6 +107,7 @@ struct pi_frame {
 
   // counters
   long long fieldEvals = 0, pairs = 0, bisectEvals = 0, fp64Count = 0, nLeaves = 0, nEmpty = 0;
+  long long qefAccepted = 0, qefSingular = 0;
   pisurf::DBuf<unsigned long long> dcount;  // device counters
   cudaEvent_t ev[9] = {};
   float stage_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -121,6 +122,7 @@ void stage_aniso(pi_frame* f);
 void stage_normals(pi_frame* f);
 void stage_octree(pi_frame* f);
 void stage_extract(pi_frame* f);
+void qef_level(pi_frame* f, long long lb, long long le);
 void eval_points(pi_frame* f, const float* d_pts, long long m, float* d_val, float* d_grad);
 long long neighbors(pi_frame* f, const float* h_pts, long long m, long long* h_off, int* h_idx,
                     long long cap);

@@ -1,0 +1,166 @@
+// K5: per-leaf QEF vertex, TNode::NodeCalcNode (src/iso_method_ours.cpp:101-174)
+// with QEFNormal<float,4>::combineSelf (include/qefnorm.h:18-33) and
+// calcErrorDMC (src/iso_method_ours.cpp:40-50).  In the reference both call
+// sites are commented out (src/surface_reconstructor.cpp:258,270); pi_params.qef
+// switches them on with the same semantics:
+//   leaf by size:      node = QEF vertex if it lies in the cell, value
+//                      f(node), zeroed if err / cellsize < 1e-4;
+//   leaf by criteria:  node = QEF vertex if it lies in the cell, value
+//                      f(node) (the later SingleEval undoes the zeroing).
+// Gradients are the finite differences of GridEval (src/evaluator.cpp:293-359)
+// over the 27 samples.  Accumulation and solve are FP64; the solve is a
+// pseudo-inverse through a Jacobi eigen-decomposition of the symmetric 4x4
+// normal matrix.  Where that matrix is singular the reference's
+// Matrix4f::inverse yields non-finite values and the vertex is rejected; the
+// pseudo-inverse gives a finite point, which is still rejected here, and the
+// number of such nodes is counted.
+#include "device.cuh"
+#include "internal.h"
+
+namespace pisurf {
+
+enum : int8_t { Q_EMPTY = 0, Q_INTERNAL = 1, Q_LEAF = 2 };
+
+// Symmetric 4x4 Jacobi eigen-decomposition, A = V diag(w) V^T.
+__device__ void sym_eig4(double A[4][4], double w[4], double V[4][4]) {
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) V[i][j] = (i == j) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 20; ++sweep) {
+    double off = 0.0, dia = 0.0;
+    for (int p = 0; p < 4; ++p) {
+      dia += fabs(A[p][p]);
+      for (int q = p + 1; q < 4; ++q) off += fabs(A[p][q]);
+    }
+    if (off <= 1e-18 * dia || off == 0.0) break;
+    for (int p = 0; p < 3; ++p)
+      for (int q = p + 1; q < 4; ++q) {
+        const double apq = A[p][q];
+        if (fabs(apq) <= 1e-300) continue;
+        const double theta = (A[q][q] - A[p][p]) / (2.0 * apq);
+        double t = 1.0 / (fabs(theta) + sqrt(theta * theta + 1.0));
+        if (theta < 0.0) t = -t;
+        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int r = 0; r < 4; ++r) {
+          const double arp = A[r][p], arq = A[r][q];
+          A[r][p] = c * arp - s * arq;
+          A[r][q] = s * arp + c * arq;
+        }
+        for (int r = 0; r < 4; ++r) {
+          const double apr = A[p][r], aqr = A[q][r];
+          A[p][r] = c * apr - s * aqr;
+          A[q][r] = s * apr + c * aqr;
+        }
+        for (int r = 0; r < 4; ++r) {
+          const double vrp = V[r][p], vrq = V[r][q];
+          V[r][p] = c * vrp - s * vrq;
+          V[r][q] = s * vrp + c * vrq;
+        }
+      }
+  }
+  for (int i = 0; i < 4; ++i) w[i] = A[i][i];
+}
+
+struct QefArgs {
+  GridView g;
+  PartView P;
+  float iso;
+  float radius;
+  long long lb, le;
+};
+
+// counters: 5 QEF vertices accepted, 6 singular systems, 7 field evaluations
+__global__ void k_qef(QefArgs a, float4* __restrict__ nd_v, const float4* __restrict__ nd_c,
+                      const int8_t* __restrict__ nd_type, const float* __restrict__ nd_samp,
+                      float* __restrict__ qef_err, unsigned long long* __restrict__ counters) {
+  const long long node = a.lb + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (node >= a.le || nd_type[node] != Q_LEAF) return;
+  const float4 c = nd_c[node];
+  const float h = c.w;
+  const float cellsize = 2.0f * h;
+  const float step = cellsize / 2;
+  const float mn[3] = {__fsub_rn(c.x, h), __fsub_rn(c.y, h), __fsub_rn(c.z, h)};
+  const float mx[3] = {__fadd_rn(c.x, h), __fadd_rn(c.y, h), __fadd_rn(c.z, h)};
+  const float* sv = nd_samp + node * 27;
+  double q[15];
+  for (int k = 0; k < 15; ++k) q[k] = 0.0;
+  double gx[27], gy[27], gz[27], px[27], py[27], pz[27];
+  for (int i = 0; i < 27; ++i) {
+    const int x = i % 3, y = (i / 3) % 3, z = i / 9;
+    // sample position (GenerateSampling) and GridEval finite differences
+    const float t[3] = {x * 0.5f, y * 0.5f, z * 0.5f};
+    px[i] = __fadd_rn(__fmul_rn(1.0f - t[0], mn[0]), __fmul_rn(t[0], mx[0]));
+    py[i] = __fadd_rn(__fmul_rn(1.0f - t[1], mn[1]), __fmul_rn(t[1], mx[1]));
+    pz[i] = __fadd_rn(__fmul_rn(1.0f - t[2], mn[2]), __fmul_rn(t[2], mx[2]));
+    auto fd = [&](int d, int stride) {
+      if (d == 0) return ((double)sv[i] - (double)sv[i + stride]) / step;
+      if (d == 2) return ((double)sv[i - stride] - (double)sv[i]) / step;
+      return ((double)sv[i - stride] - (double)sv[i + stride]) / (2.0 * step);
+    };
+    gx[i] = fd(x, 1);
+    gy[i] = fd(y, 3);
+    gz[i] = fd(z, 9);
+    const double pl[5] = {gx[i], gy[i], gz[i], -1.0, -(px[i] * gx[i] + py[i] * gy[i] + pz[i] * gz[i]) + (double)sv[i]};
+    int idx = 0;
+    for (int r = 0; r < 5; ++r)
+      for (int s = r; s < 5; ++s) q[idx++] += pl[r] * pl[s];
+  }
+  double A[4][4], B[4];
+  for (int r = 0; r < 4; ++r) {
+    const int idx = ((2 * 4 + 3 - r) * r) / 2;
+    for (int s = r; s < 4; ++s) A[r][s] = A[s][r] = q[idx + s - r];
+    B[r] = -q[idx + 4 - r];
+  }
+  double w[4], V[4][4];
+  sym_eig4(A, w, V);
+  double wmax = 0.0;
+  for (int k = 0; k < 4; ++k) wmax = fmax(wmax, fabs(w[k]));
+  const double tol = 1e-12 * wmax;
+  bool singular = !(wmax > 0.0);
+  double xs[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int k = 0; k < 4; ++k) {
+    if (fabs(w[k]) <= tol) {
+      singular = true;
+      continue;
+    }
+    double proj = 0.0;
+    for (int r = 0; r < 4; ++r) proj += V[r][k] * B[r];
+    proj /= w[k];
+    for (int r = 0; r < 4; ++r) xs[r] += V[r][k] * proj;
+  }
+  const bool in_cell = xs[0] >= mn[0] && xs[0] <= mx[0] && xs[1] >= mn[1] && xs[1] <= mx[1] && xs[2] >= mn[2] &&
+                       xs[2] <= mx[2];
+  double err = 1e30;
+  float4 v = nd_v[node];
+  bool accepted = false;
+  if (in_cell && !singular) {
+    err = 0.0;
+    for (int i = 0; i < 27; ++i) {
+      const double d = gx[i] * (xs[0] - px[i]) + gy[i] * (xs[1] - py[i]) + gz[i] * (xs[2] - pz[i]) - xs[3];
+      err += d * d / (1.0 + gx[i] * gx[i] + gy[i] * gy[i] + gz[i] * gz[i]);
+    }
+    v = make_float4((float)xs[0], (float)xs[1], (float)xs[2], (float)xs[3]);
+    accepted = true;
+  }
+  if (in_cell && singular) stripe_add(counters, 6, 1ull);
+  if (accepted) {
+    v.w = a.iso - field_sum(a.g, a.P, v.x, v.y, v.z, nullptr);
+    stripe_add(counters, 7, 1ull);
+    stripe_add(counters, 5, 1ull);
+  }
+  // leaf by size keeps the zeroing (no SingleEval follows it)
+  const bool leaf_by_size = (double)(cellsize - a.radius) < 1e-8;
+  if (leaf_by_size && err / (double)cellsize < 0.0001) v.w = 0.0f;
+  nd_v[node] = v;
+  if (qef_err) qef_err[node] = (float)err;
+}
+
+void qef_level(pi_frame* f, long long lb, long long le) {
+  cudaStream_t s = f->ctx->stream;
+  const GridHost& gh = f->g;
+  QefArgs qa{GridView{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p},
+             PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p}, f->iso, f->P.radius, lb, le};
+  PI_LAUNCH(k_qef, div_up(le - lb, 64), 64, 0, s, qa, f->nd_v.p, f->nd_c.p, f->nd_type.p, f->nd_samp.p, nullptr,
+            f->dcount.p);
+}
+
+}  // namespace pisurf

@@ -136,3 +136,40 @@ def compare_meshes(o_mesh, g_mesh, radius):
                vert_maxdiff_over_r=float(d.max() / radius), vert_rmsdiff_over_r=float(np.sqrt(np.mean(d ** 2)) / radius),
                verts_off_tol=int(np.sum(d > VERT_TOL * radius)))
     return rep
+
+
+QEF_VERT_TOL = 1e-4  # QEF vertex vs the FP64 solve of the same samples, in units of r
+
+
+def qef_solve_f64(center, half, samples):
+    """TNode::NodeCalcNode (src/iso_method_ours.cpp:101-174) in float64 with the
+    library's pseudo-inverse rule: returns (x[4], in_cell, singular, err)."""
+    c = np.asarray(center, np.float32)
+    h = np.float32(half)
+    mn = c - h
+    mx = c + h
+    pts = sample_points(center, half).astype(np.float64)
+    f = np.asarray(samples, np.float64)
+    step = np.float64(np.float32(2.0) * h / np.float32(2))
+    v = f.reshape(3, 3, 3)  # [z, y, x]
+    g = np.zeros((3, 3, 3, 3))
+    for ax, axis in ((0, 2), (1, 1), (2, 0)):  # gradient component ax differentiates array axis `axis`
+        vv = np.moveaxis(v, axis, 0)
+        gg = np.empty_like(vv)
+        gg[0] = (vv[0] - vv[1]) / step
+        gg[2] = (vv[1] - vv[2]) / step
+        gg[1] = (vv[0] - vv[2]) / (2 * step)
+        g[..., ax] = np.moveaxis(gg, 0, axis)
+    g = g.reshape(27, 3)
+    pl = np.concatenate([g, -np.ones((27, 1)), (-(pts * g).sum(1) + f)[:, None]], axis=1)
+    M = pl.T @ pl
+    A = M[:4, :4]
+    B = -M[:4, 4]
+    w, V = np.linalg.eigh(A)
+    tol = 1e-12 * np.abs(w).max() if np.abs(w).max() > 0 else 0.0
+    keep = np.abs(w) > tol
+    singular = not keep.all()
+    x = V[:, keep] @ ((V[:, keep].T @ B) / w[keep])
+    in_cell = bool(np.all(x[:3] >= mn) and np.all(x[:3] <= mx))
+    err = float(np.sum((g @ x[:3] - (pts * g).sum(1) - x[3]) ** 2 / (1 + (g * g).sum(1))))
+    return x, in_cell, singular, err

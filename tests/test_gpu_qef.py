@@ -1,0 +1,102 @@
+"""GPU parity of the QEF mode (pi_params.qef = 1, the reference's
+TNode::NodeCalcNode switched on at src/surface_reconstructor.cpp:258,270).
+
+- Octree structure does not depend on the QEF: node sets and types are
+  compared as in the plain mode.
+- Leaf vertices against an FP64 solve of the same 27 samples (numpy, same
+  pseudo-inverse rule): |dx| <= QEF_VERT_TOL * r, max and RMS reported.
+- Leaf vertices against the float oracle (reference semantics, float
+  Matrix4f inverse): same acceptance except where the vertex lies within
+  1e-4 of the cell boundary or the matrix is near singular (counted).
+"""
+import numpy as np
+import pytest
+
+import parity as PR
+import pyoracle as O
+from particleisosurface_gb300 import _native as N
+from particleisosurface_gb300 import build as B
+from particleisosurface_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pair():
+    B.build()
+    O.build()
+    fr = synth.slab_and_sphere(n=6000, seed=7)
+    ctx = N.Context(0)
+    g = N.Frame(ctx, N.default_params(fr.radius, qef=True)).upload(fr.xyz).run()
+    o = O.OracleFrame(fr.xyz, fr.radius, flags=O.QEF).run()
+    yield fr, o, g
+    g.close()
+    ctx.close()
+
+
+def test_qef_octree_structure_identical(pair):
+    fr, o, g = pair
+    on = PR.node_table(o.nodes())
+    gn = PR.node_table(g.dump(N.DUMP_NODES))
+    assert set(on) == set(gn)
+    assert all(on[k][0] == gn[k][0] for k in on)
+
+
+def test_qef_vertices_match_fp64_solve(pair):
+    fr, o, g = pair
+    nodes = g.dump(N.DUMP_NODES)
+    samp = g.dump(N.DUMP_QEF_SAMPLES)
+    leaves = np.nonzero(nodes["type"] == 2)[0]
+    rng = np.random.default_rng(0)
+    pick = rng.choice(leaves, size=min(3000, len(leaves)), replace=False)
+    errs, disagree = [], 0
+    for i in pick:
+        x, in_cell, singular, err = PR.qef_solve_f64(nodes["center"][i], nodes["half"][i], samp[i])
+        acc = in_cell and not singular
+        moved = not np.array_equal(nodes["node"][i][:3], nodes["center"][i])
+        if acc != moved:
+            disagree += 1
+            continue
+        if acc:
+            errs.append(np.abs(nodes["node"][i][:3] - x[:3]).max() / fr.radius)
+    errs = np.array(errs)
+    info = g.info()
+    print("QEF vs FP64: accepted %d of %d sampled leaves, max %.3e rms %.3e (x r); acceptance differs %d; "
+          "frame accepted %d singular %d" % (len(errs), len(pick), errs.max(), np.sqrt(np.mean(errs ** 2)),
+                                             disagree, info["qef_accepted"], info["qef_singular"]))
+    assert len(errs) > 100
+    assert errs.max() <= PR.QEF_VERT_TOL
+    assert disagree <= max(2, len(pick) // 1000)
+
+
+def test_qef_leaves_match_float_reference(pair):
+    fr, o, g = pair
+    on = o.nodes()
+    A = {(int(d), int(i)): k for k, (d, i) in enumerate(zip(on["depth"], on["id"]))}
+    gn = g.dump(N.DUMP_NODES)
+    moved_o = moved_g = both = differ = 0
+    dmax = []
+    for k in np.nonzero(gn["type"] == 2)[0]:
+        j = A[(int(gn["depth"][k]), int(gn["id"][k]))]
+        mo = not np.array_equal(on["node"][j][:3], on["center"][j])
+        mg = not np.array_equal(gn["node"][k][:3], gn["center"][k])
+        moved_o += mo
+        moved_g += mg
+        if mo and mg:
+            both += 1
+            dmax.append(np.abs(on["node"][j][:3] - gn["node"][k][:3]).max() / fr.radius)
+        elif mo != mg:
+            differ += 1
+    dmax = np.array(dmax)
+    print("QEF vs float reference: moved oracle %d gpu %d both %d differ %d; vertex max %.3e rms %.3e (x r)"
+          % (moved_o, moved_g, both, differ, dmax.max(), np.sqrt(np.mean(dmax ** 2))))
+    assert both > 100
+    assert differ <= max(4, both // 200)
+    assert np.percentile(dmax, 99) <= 1e-3
+
+
+def test_qef_mesh_topology(pair):
+    fr, o, g = pair
+    rep = PR.compare_meshes(o.mesh(), g.mesh(keys=True), fr.radius)
+    print(rep)
+    assert rep["verts_only_oracle"] + rep["verts_only_gpu"] <= max(8, rep["verts_oracle"] // 1000)
