@@ -61,7 +61,151 @@ def parse():
     p.add_argument("--cpu-sample-evals", type=int, default=200_000)
     p.add_argument("--single", action="store_true",
                    help="reconstruct one frame once and print its counters (for profiler captures)")
+    p.add_argument("--workload", choices=["dam_break_1m", "batch64", "serving", "stress"], default="dam_break_1m",
+                   help="dam_break_1m: the metric's frame (default); batch64: 64 mixed frames batched vs one at "
+                        "a time; serving: Poisson stream through the request loop; stress: sheets and filaments")
+    p.add_argument("--frames", type=int, default=64, help="frames of the batch64 workload")
+    p.add_argument("--requests", type=int, default=120, help="requests of the serving workload")
+    p.add_argument("--max-n", type=int, default=4_000_000, help="largest serving request")
+    p.add_argument("--rate", type=float, default=20.0, help="serving arrival rate (requests/s)")
+    p.add_argument("--slots", type=int, default=8)
     return p.parse_args()
+
+
+def batch64(a):
+    """64 independent frames (1-6 spheres/slabs, 50k-2M particles): one at a
+    time on one stream versus all submitted to the request loop."""
+    from particleisosurface_gb300 import _native as N
+    from particleisosurface_gb300 import build as B
+    from particleisosurface_gb300 import synth
+    B.build()
+    frames = synth.batch_frames(a.frames)
+    total_n = sum(fr.n for fr in frames)
+    ctx = N.Context(0)
+    # warm-up
+    for fr in frames[:2]:
+        f = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz).run()
+        f.close()
+    t0 = time.perf_counter()
+    for fr in frames:
+        f = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz).run()
+        f.mesh()
+        f.close()
+    t_seq = time.perf_counter() - t0
+    ctx.close()
+    srv = N.Server(0, slots=a.slots, budget_bytes=0)
+    for fr in frames[:2]:
+        srv.result(srv.submit(fr.xyz, N.default_params(fr.radius)))
+    t0 = time.perf_counter()
+    tickets = [srv.submit(fr.xyz, N.default_params(fr.radius)) for fr in frames]
+    lat = [srv.result(t)[2] for t in tickets]
+    t_bat = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    print(json.dumps({
+        "metric": METRIC, "workload": "batch64", "value": len(frames) / t_bat, "unit": UNIT,
+        "one_at_a_time_frames_per_s": len(frames) / t_seq, "speedup_vs_one_at_a_time": t_seq / t_bat,
+        "frames": len(frames), "particles_total": total_n, "slots": a.slots, "max_in_flight": st["max_in_flight"],
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "timing": "host wall clock, host buffers in and out (upload, run, mesh download)",
+        "data": "synthetic (seeded unions of spheres and slabs)"}))
+
+
+def serving(a):
+    """Poisson stream of frame requests (sequences advected by swirl plus
+    gravity) replayed in real time into the request loop."""
+    import threading
+
+    from particleisosurface_gb300 import _native as N
+    from particleisosurface_gb300 import build as B
+    from particleisosurface_gb300 import synth
+    B.build()
+    reqs = synth.serving_requests(count=a.requests, n_max=a.max_n, rate_hz=a.rate)
+    base = {}
+    xyzs = []
+    for r in reqs:
+        key = r["seq"]
+        if key not in base:
+            fr = synth.mixed_frame(r["seed"], r["n"], r["radius"])
+            base[key] = fr.xyz64 / max(fr.xyz64.max(), 1e-9) * 0.98 + 0.01
+        p = synth.advect(base[key], r["w"], 0.5, 0.0, 0.01, steps=1) if r["step"] else base[key]
+        base[key] = p
+        xyzs.append(np.ascontiguousarray(p.astype(np.float32)))
+    srv = N.Server(0, slots=a.slots, budget_bytes=0)
+    srv.result(srv.submit(xyzs[0], N.default_params(reqs[0]["radius"])))  # warm-up
+    tickets = [None] * len(reqs)
+    results = [None] * len(reqs)
+
+    def collector():
+        for i in range(len(reqs)):
+            while tickets[i] is None:
+                time.sleep(0.0005)
+            results[i] = srv.result(tickets[i])[2:]
+
+    th = threading.Thread(target=collector)
+    th.start()
+    t0 = time.perf_counter()
+    for i, r in enumerate(reqs):
+        wait = r["t"] - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        tickets[i] = srv.submit(xyzs[i], N.default_params(r["radius"]))
+    th.join()
+    t_all = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    lat = np.array([x[0] for x in results])
+    print(json.dumps({
+        "metric": METRIC, "workload": "serving", "value": len(reqs) / t_all, "unit": UNIT,
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "requests": len(reqs), "arrival_rate_hz": a.rate, "n_range": [10000, a.max_n],
+        "particles_total": int(sum(x.shape[0] for x in xyzs)), "slots": a.slots,
+        "max_in_flight": st["max_in_flight"], "wall_s": t_all,
+        "data": "synthetic (seeded sequences advected by swirl plus gravity)"}))
+
+
+def stress(a):
+    """Sheets and filaments: FP32/FP64 eigen split, errors against the FP64 oracle."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+
+    from particleisosurface_gb300 import _native as N
+    from particleisosurface_gb300 import build as B
+    from particleisosurface_gb300 import synth
+    B.build()
+    O.build()
+    fr = synth.sheets_and_filaments(n=500_000)
+    ctx = N.Context(0)
+    f = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz)
+    f.run()
+    f.reset()
+    t0 = time.perf_counter()
+    f.run()
+    sec = time.perf_counter() - t0
+    info = f.info()
+    o64 = O.OracleFrame(fr.xyz, fr.radius, flags=O.FP64)
+    for s in (1, 2, 3):
+        o64.stage(s)
+    xm, G, det = o64.aniso()
+    gG = f.dump(N.DUMP_G)
+    flags = f.dump(N.DUMP_FP64_FLAGS).astype(bool)
+    eG = np.abs(gG - G).reshape(len(G), -1).max(1)
+    rng = np.random.default_rng(3)
+    pts = (fr.xyz[rng.choice(fr.n, 20000)] + rng.normal(0, 1.5 * fr.radius, (20000, 3))).astype(np.float32)
+    ms = info["max_scalar"]
+    ef = np.abs(f.eval(pts) - o64.eval(pts)) / ms
+    print(json.dumps({
+        "metric": METRIC, "workload": "stress", "value": 1.0 / sec, "unit": UNIT,
+        "particles": fr.n, "fp64_eigen_particles": int(info["fp64_eigen"]),
+        "fp32_eigen_particles": int(fr.n - info["fp64_eigen"]),
+        "G_err_vs_fp64": {"max_fp64_path": float(eG[flags].max()) if flags.any() else None,
+                          "max_fp32_path": float(eG[~flags].max()) if (~flags).any() else None,
+                          "rms": float(np.sqrt(np.mean(eG ** 2)))},
+        "field_err_vs_fp64_over_maxscalar": {"max": float(ef.max()), "rms": float(np.sqrt(np.mean(ef ** 2)))},
+        "nodes": info["num_nodes"], "vertices": info["num_vertices"],
+        "data": "synthetic (seeded sheets on planes and saddles, Bezier filaments)"}))
+    f.close()
+    ctx.close()
 
 
 def single(a):
@@ -339,7 +483,9 @@ def ours(a):
 
 def main():
     a = parse()
-    if a.single:
+    if a.workload != "dam_break_1m" and a.impl == "ours":
+        {"batch64": batch64, "serving": serving, "stress": stress}[a.workload](a)
+    elif a.single:
         single(a)
     elif a.impl == "reference":
         reference_arm(a)

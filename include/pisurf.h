@@ -199,6 +199,28 @@ int pi_hashgrid_build_noalloc(const float* d_xyz, int64_t n, float radius, int32
                               float* bounding_out6, int32_t* xyz_cell_num_out3, int64_t* cell_num_out,
                               void* stream);
 
+/* Request loop (continuous batching).  The reference reconstructs one frame
+ * per run of its driver loop (runOurs, src/main.cpp:330-405); a server keeps
+ * `slots` worker threads, each with its own stream, admits queued requests
+ * in arrival order while their estimated device footprint fits in
+ * budget_bytes (0 = no cap; one request is always admitted), runs admitted
+ * frames concurrently and keeps results in host memory until fetched.  A
+ * result equals pi_run's on the same input. */
+typedef struct pi_server pi_server;
+int pi_server_create(int device, int slots, size_t budget_bytes, pi_server** out);
+/* copies xyz[n*3]; returns a ticket */
+int pi_server_submit(pi_server* s, const pi_params* params, const float* xyz, int64_t n, uint64_t* ticket);
+int pi_server_poll(pi_server* s, uint64_t ticket, int* done);
+/* blocks until done; latency = completion - submission, queue = start - submission */
+int pi_server_wait(pi_server* s, uint64_t ticket, int64_t* nverts, int64_t* ntris, double* latency_ms,
+                   double* queue_ms);
+/* copies the mesh (0-based triangles) and releases the request */
+int pi_server_fetch(pi_server* s, uint64_t ticket, float* verts, int32_t* tris);
+int pi_server_stats(pi_server* s, int64_t* completed, int64_t* in_flight, int64_t* max_in_flight,
+                    int64_t* queued, int64_t* bytes_reserved);
+/* finishes queued requests, then stops the workers */
+int pi_server_destroy(pi_server* s);
+
 /* The dual-marching-cubes canonicalisation table the library uses
  * (include/visitorextract.h:35-293 in the reference). */
 int pi_dmc_table(int32_t* trans8x256, int8_t* flip256, int32_t* code256);

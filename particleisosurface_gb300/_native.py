@@ -326,3 +326,69 @@ class Frame:
         buf = np.empty(nb.value // np.dtype(dtype).itemsize, dtype)
         check(lib().pi_stage_dump(self.h, what, buf.ctypes.data_as(C.c_void_p), nb.value))
         return buf.reshape(shape)
+
+
+def _declare_server(L):
+    P = C.c_void_p
+    sig = {
+        "pi_server_create": (C.c_int, [C.c_int, C.c_int, C.c_size_t, C.POINTER(C.c_void_p)]),
+        "pi_server_submit": (C.c_int, [P, C.POINTER(Params), C.POINTER(C.c_float), C.c_int64,
+                                       C.POINTER(C.c_uint64)]),
+        "pi_server_poll": (C.c_int, [P, C.c_uint64, C.POINTER(C.c_int)]),
+        "pi_server_wait": (C.c_int, [P, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "pi_server_fetch": (C.c_int, [P, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_int32)]),
+        "pi_server_stats": (C.c_int, [P] + [C.POINTER(C.c_int64)] * 5),
+        "pi_server_destroy": (C.c_int, [P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+class Server:
+    """pi_server: continuous batching of frame requests on one GPU."""
+
+    def __init__(self, device=0, slots=8, budget_bytes=0):
+        _declare_server(lib())
+        h = C.c_void_p()
+        check(lib().pi_server_create(device, slots, budget_bytes, C.byref(h)))
+        self.h = h
+
+    def submit(self, xyz, params):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float32)
+        t = C.c_uint64()
+        check(lib().pi_server_submit(self.h, C.byref(params), ptr(xyz, C.c_float), xyz.shape[0], C.byref(t)))
+        return t.value
+
+    def done(self, ticket):
+        d = C.c_int()
+        check(lib().pi_server_poll(self.h, ticket, C.byref(d)))
+        return bool(d.value)
+
+    def result(self, ticket):
+        nv, nt = C.c_int64(), C.c_int64()
+        lat, q = C.c_double(), C.c_double()
+        check(lib().pi_server_wait(self.h, ticket, C.byref(nv), C.byref(nt), C.byref(lat), C.byref(q)))
+        v = np.empty((nv.value, 3), np.float32)
+        t = np.empty((nt.value, 3), np.int32)
+        check(lib().pi_server_fetch(self.h, ticket, ptr(v, C.c_float), ptr(t, C.c_int32)))
+        return v, t, lat.value, q.value
+
+    def stats(self):
+        vals = [C.c_int64() for _ in range(5)]
+        check(lib().pi_server_stats(self.h, *[C.byref(x) for x in vals]))
+        return dict(zip(["completed", "in_flight", "max_in_flight", "queued", "bytes_reserved"],
+                        [x.value for x in vals]))
+
+    def close(self):
+        if self.h:
+            lib().pi_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -110,6 +110,17 @@ __global__ void k_qef(QefArgs a, float4* __restrict__ nd_v, const float4* __rest
     for (int s = r; s < 4; ++s) A[r][s] = A[s][r] = q[idx + s - r];
     B[r] = -q[idx + 4 - r];
   }
+  // Equilibrate: the gradient rows are ~|f| / step while the w column is 1,
+  // so A's condition number exceeds what FP32 or even FP64 resolves.  With
+  // D = diag(A_ii)^-1/2 the solve is (D A D) y = D B, x = D y: the same
+  // minimiser in exact arithmetic, well conditioned unless the planes are
+  // degenerate.
+  double D[4];
+  for (int r = 0; r < 4; ++r) D[r] = A[r][r] > 0.0 ? 1.0 / sqrt(A[r][r]) : 1.0;
+  for (int r = 0; r < 4; ++r) {
+    B[r] *= D[r];
+    for (int s = 0; s < 4; ++s) A[r][s] *= D[r] * D[s];
+  }
   double w[4], V[4][4];
   sym_eig4(A, w, V);
   double wmax = 0.0;
@@ -127,6 +138,7 @@ __global__ void k_qef(QefArgs a, float4* __restrict__ nd_v, const float4* __rest
     proj /= w[k];
     for (int r = 0; r < 4; ++r) xs[r] += V[r][k] * proj;
   }
+  for (int r = 0; r < 4; ++r) xs[r] *= D[r];
   const bool in_cell = xs[0] >= mn[0] && xs[0] <= mx[0] && xs[1] >= mn[1] && xs[1] <= mx[1] && xs[2] >= mn[2] &&
                        xs[2] <= mx[2];
   double err = 1e30;

@@ -148,3 +148,180 @@ CONFIGS = {
     "dam_break": dam_break,
     "small_blob": small_blob,
 }
+
+
+def _sphere_or_slab(rng, n, radius, jitter, domain=1.0):
+    """One jittered-lattice sphere (radius 0.05-0.3) or slab in the unit box."""
+    sp = 2.0 * radius
+    if rng.random() < 0.5:
+        R = rng.uniform(0.05, 0.3)
+        c = rng.uniform(R, domain - R, size=3)
+        pts = _lattice_sphere(c, R, sp)
+    else:
+        ext = rng.uniform(0.1, 0.6, size=3)
+        ext[rng.integers(3)] = rng.uniform(2 * sp, 0.1)  # one thin axis
+        lo = rng.uniform(0.0, domain - ext)
+        pts = _lattice_box(lo, lo + ext, sp)
+    if len(pts) > n:
+        pts = pts[np.sort(rng.choice(len(pts), n, replace=False))]
+    return _jitter(pts, jitter * radius, rng)
+
+
+def mixed_frame(seed, n_target, radius=0.01, jitter=0.2) -> Frame:
+    """Batched-form frame: a seeded union of 1-6 jittered-lattice spheres and
+    slabs in a unit box.  The shapes are drawn first; the whole set is then
+    scaled about the origin (the geometry rule) until it holds n_target
+    particles, and a seeded subset of n_target is kept."""
+    rng = np.random.default_rng(seed)
+    k = int(rng.integers(1, 7))
+    shapes = [(rng.random() < 0.5, rng.random(5), int(rng.integers(3))) for _ in range(k)]
+    sp = 2.0 * radius
+
+    def build(s):
+        out = []
+        for is_sphere, u, ax in shapes:
+            if is_sphere:
+                R = (0.05 + 0.25 * u[0]) * s
+                c = (R / s + (1 - 2 * R / s) * u[1:4]) * s
+                out.append(_lattice_sphere(c, R, sp))
+            else:
+                ext = (0.1 + 0.5 * u[:3]) * s
+                ext[ax] = max(2 * sp, 0.1 * u[3] * s)
+                lo = (1 * s - ext) * u[1:4] * 0.999
+                out.append(_lattice_box(lo, lo + ext, sp))
+        pts = np.concatenate(out) if out else np.zeros((0, 3))
+        ijk = np.round(pts / sp).astype(np.int64)
+        ijk -= ijk.min(0) if len(ijk) else 0
+        m = int(ijk.max()) + 1 if len(ijk) else 1
+        key = np.unique((ijk[:, 0] * m + ijk[:, 1]) * m + ijk[:, 2])
+        return np.stack([key // (m * m), (key // m) % m, key % m], -1) * sp + \
+            (np.round(pts.min(0) / sp) * sp if len(pts) else 0.0)
+
+    # the lattice count grows as s^3: a few proportional steps reach the target
+    s = 1.0
+    for _ in range(60):
+        pts = build(s)
+        if len(pts) >= n_target:
+            break
+        s *= max(1.002, (n_target / max(len(pts), 1)) ** (1.0 / 3.0) * 1.002)
+    pts = pts[np.sort(rng.choice(len(pts), size=n_target, replace=False))]
+    pts = _jitter(pts, jitter * radius, rng)
+    return Frame(pts, radius, s, seed, "mixed_%d_%d" % (seed, n_target))
+
+
+def batch_frames(count=64, seed=100, n_min=50_000, n_max=2_000_000, radius=0.01):
+    """The batched workload: `count` frames, particle counts log-uniform in
+    [n_min, n_max]."""
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(np.log(n_min), np.log(n_max), size=count)).astype(int)
+    return [mixed_frame(seed + 1 + i, int(n), radius) for i, n in enumerate(ns)]
+
+
+def _bezier(rng, t, scale):
+    P = rng.uniform(0.1, 0.9, size=(4, 3)) * scale
+    b = ((1 - t) ** 3)[:, None] * P[0] + (3 * (1 - t) ** 2 * t)[:, None] * P[1] + \
+        (3 * (1 - t) * t ** 2)[:, None] * P[2] + (t ** 3)[:, None] * P[3]
+    return b
+
+
+def sheets_and_filaments(n=500_000, radius=0.01, seed=4) -> Frame:
+    """Precision stress: 50 % thin sheets one to two particles thick on random
+    planes and saddles z = a (x^2 - y^2), a in [0.5, 3]; 50 % filaments along
+    random cubic Bezier curves with a 1-3 particle cross-section.  Spacing 2r.
+    Near-degenerate neighbour covariances and ill-conditioned QEFs follow."""
+    rng = np.random.default_rng(seed)
+    sp = 2.0 * radius
+    n_sheet = n // 2
+    n_fil = n - n_sheet
+    scale = max(1.0, (n / 500_000) ** 0.5 * 2.0)
+    pts = []
+    # sheets: lattice patches of side L on planes or saddles
+    left = n_sheet
+    while left > 0:
+        L = rng.uniform(0.2, 0.5) * scale
+        m = int(L / sp)
+        u = (np.arange(m) - m / 2) * sp
+        uu, vv = np.meshgrid(u, u, indexing="ij")
+        layers = int(rng.integers(1, 3))
+        if rng.random() < 0.5:
+            a = rng.uniform(0.5, 3.0) / scale
+            ww = a * (uu ** 2 - vv ** 2)
+        else:
+            ww = np.zeros_like(uu)
+        patch = []
+        for l in range(layers):
+            patch.append(np.stack([uu.ravel(), vv.ravel(), ww.ravel() + l * sp], -1))
+        patch = np.concatenate(patch)
+        Q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        c = rng.uniform(0.3, 0.7, size=3) * scale
+        patch = patch @ Q.T + c
+        take = min(left, len(patch))
+        pts.append(patch[:take])
+        left -= take
+    left = n_fil
+    while left > 0:
+        length = 2.0 * scale
+        m = max(int(length / sp), 8)
+        t = np.linspace(0, 1, m)
+        line = _bezier(rng, t, scale)
+        k = int(rng.integers(1, 4))
+        offs = [np.zeros(3)] + [rng.normal(size=3) * sp for _ in range(k - 1)]
+        fil = np.concatenate([line + o for o in offs])
+        take = min(left, len(fil))
+        pts.append(fil[:take])
+        left -= take
+    pts = np.concatenate(pts)
+    pts = _jitter(pts, 0.1 * radius, rng)
+    return Frame(pts, radius, scale, seed, "sheets_filaments_%d" % n)
+
+
+def advect(xyz, w, g, t, dt, steps=1):
+    """Swirl plus gravity u = (-w (y - 0.5), w (x - 0.5), -g t), clamped to the
+    unit box (serving workload sequences)."""
+    p = xyz.copy()
+    for k in range(steps):
+        tt = t + k * dt
+        u = np.stack([-w * (p[:, 1] - 0.5), w * (p[:, 0] - 0.5), np.full(len(p), -g * tt)], -1)
+        p = np.clip(p + dt * u, 0.0, 1.0)
+    return p
+
+
+def serving_requests(count=2000, seed=500, n_min=10_000, n_max=4_000_000, rate_hz=20.0):
+    """Serving workload: `count` frame requests with Poisson arrivals at
+    `rate_hz`, grouped into time-correlated sequences of 20-200 steps; each
+    sequence has its own particle count (log-uniform), radius in
+    {0.005, 0.01, 0.02} and swirl w in [0.5, 2].  Yields dicts with the
+    arrival time and a callable that materialises the frame."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate_hz, size=count))
+    out = []
+    i = 0
+    seq = 0
+    while i < count:
+        length = int(rng.integers(20, 201))
+        n = int(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        r = float(rng.choice([0.005, 0.01, 0.02]))
+        w = float(rng.uniform(0.5, 2.0))
+        base_seed = seed * 1000 + seq
+        for k in range(min(length, count - i)):
+            out.append(dict(t=float(arrivals[i]), seq=seq, step=k, n=n, radius=r, w=w, seed=base_seed))
+            i += 1
+        seq += 1
+    return out
+
+
+def serving_frame(req, g=0.5, dt=0.01) -> Frame:
+    """Materialise one serving request: the sequence's base frame (a seeded
+    mixed frame scaled into the unit box) advected `step` times."""
+    fr = mixed_frame(req["seed"], req["n"], req["radius"])
+    p = fr.xyz64 / max(fr.xyz64.max(), 1e-9) * 0.98 + 0.01
+    if req["step"]:
+        p = advect(p, req["w"], g, 0.0, dt, steps=req["step"])
+    return Frame(p, req["radius"], fr.scale, req["seed"], "serve_%d_%d" % (req["seq"], req["step"]))
+
+
+CONFIGS.update({
+    "batch64": batch_frames,
+    "sheets_filaments": sheets_and_filaments,
+    "serving": serving_requests,
+})

@@ -143,7 +143,8 @@ QEF_VERT_TOL = 1e-4  # QEF vertex vs the FP64 solve of the same samples, in unit
 
 def qef_solve_f64(center, half, samples):
     """TNode::NodeCalcNode (src/iso_method_ours.cpp:101-174) in float64 with the
-    library's pseudo-inverse rule: returns (x[4], in_cell, singular, err)."""
+    library's rule (diagonal equilibration, eigen pseudo-inverse, relative
+    threshold 1e-12): returns (x[4], in_cell, singular, err)."""
     c = np.asarray(center, np.float32)
     h = np.float32(half)
     mn = c - h
@@ -165,11 +166,13 @@ def qef_solve_f64(center, half, samples):
     M = pl.T @ pl
     A = M[:4, :4]
     B = -M[:4, 4]
-    w, V = np.linalg.eigh(A)
+    d = np.where(np.diag(A) > 0, 1.0 / np.sqrt(np.where(np.diag(A) > 0, np.diag(A), 1.0)), 1.0)
+    As = A * d[:, None] * d[None, :]
+    w, V = np.linalg.eigh(As)
     tol = 1e-12 * np.abs(w).max() if np.abs(w).max() > 0 else 0.0
     keep = np.abs(w) > tol
     singular = not keep.all()
-    x = V[:, keep] @ ((V[:, keep].T @ B) / w[keep])
+    x = d * (V[:, keep] @ ((V[:, keep].T @ (d * B)) / w[keep]))
     in_cell = bool(np.all(x[:3] >= mn) and np.all(x[:3] <= mx))
     err = float(np.sum((g @ x[:3] - (pts * g).sum(1) - x[3]) ** 2 / (1 + (g * g).sum(1))))
     return x, in_cell, singular, err
