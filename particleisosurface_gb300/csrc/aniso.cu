@@ -38,8 +38,13 @@ __device__ __forceinline__ float d2_exact(float dx, float dy, float dz) {
   return __fadd_rn(__fmul_rn(dx, dx), __fadd_rn(__fmul_rn(dy, dy), __fmul_rn(dz, dz)));
 }
 
+// The smoothed centre x = (1 - delta) p + delta m, m = sum w p_j / sum w, is
+// formed as x = p + delta * sum w (p_j - p) / sum w: the offsets are small, so
+// the centre is kept as a float pair hi + lo with hi = fl(x) and lo the rest.
+// Coordinates of order 1 against r = 0.01 would otherwise lose ~1e-5 r to the
+// float rounding of x alone.  (c_self + c_mean == 1 exactly in float.)
 __global__ void k_xmean(GridView g, const float4* __restrict__ pos, long long n, float nI, float nI2,
-                        float inv_h3, float c_self, float c_mean, float4* __restrict__ xm) {
+                        float inv_h3, float c_mean, float4* __restrict__ xm, float4* __restrict__ xlo) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   float4 p = pos[t];
@@ -55,23 +60,29 @@ __global__ void k_xmean(GridView g, const float4* __restrict__ pos, long long n,
       for (int j = s; j < e; ++j) {
         if (j == t) continue;
         float4 q = __ldg(pos + j);
-        float d2 = d2_exact(__fsub_rn(q.x, p.x), __fsub_rn(q.y, p.y), __fsub_rn(q.z, p.z));
+        const float dx = __fsub_rn(q.x, p.x), dy2 = __fsub_rn(q.y, p.y), dz2 = __fsub_rn(q.z, p.z);
+        float d2 = d2_exact(dx, dy2, dz2);
         if (d2 >= nI2) continue;
         float w = wij_f(__fsqrt_rn(d2), nI, inv_h3);
         ws.add(w);
-        sx.add(q.x * w);
-        sy.add(q.y * w);
-        sz.add(q.z * w);
+        sx.add(dx * w);
+        sy.add(dy2 * w);
+        sz.add(dz2 * w);
       }
     }
-  float4 r = make_float4(p.x, p.y, p.z, 0.f);
+  float4 hi = make_float4(p.x, p.y, p.z, 0.f), lo = make_float4(0.f, 0.f, 0.f, 0.f);
   if (cand > 2 && ws.s > 0.f) {
-    float mx = sx.s / ws.s, my = sy.s / ws.s, mz = sz.s / ws.s;
-    r.x = __fadd_rn(__fmul_rn(p.x, c_self), __fmul_rn(mx, c_mean));
-    r.y = __fadd_rn(__fmul_rn(p.y, c_self), __fmul_rn(my, c_mean));
-    r.z = __fadd_rn(__fmul_rn(p.z, c_self), __fmul_rn(mz, c_mean));
+    const float ox = c_mean * ((sx.s - sx.c) / ws.s), oy = c_mean * ((sy.s - sy.c) / ws.s),
+                oz = c_mean * ((sz.s - sz.c) / ws.s);
+    hi.x = __fadd_rn(p.x, ox);
+    hi.y = __fadd_rn(p.y, oy);
+    hi.z = __fadd_rn(p.z, oz);
+    lo.x = __fadd_rn(__fsub_rn(p.x, hi.x), ox);
+    lo.y = __fadd_rn(__fsub_rn(p.y, hi.y), oy);
+    lo.z = __fadd_rn(__fsub_rn(p.z, hi.z), oz);
   }
-  xm[t] = r;
+  xm[t] = hi;
+  xlo[t] = lo;
 }
 
 // Cyclic Jacobi on a symmetric 3x3 (a: 00 01 02 11 12 22).  On return
@@ -137,7 +148,7 @@ __device__ __forceinline__ void g_from_eig(const T w_in[3], const T V[3][3], flo
 }
 
 __global__ void k_cov_G(GridView g, const float4* __restrict__ pos, const float4* __restrict__ xm0,
-                        float4* __restrict__ xm, long long n,
+                        const float4* __restrict__ xlo, float4* __restrict__ xm, long long n,
                         float nI, float nI2, float inv_h3, float h2, float inv_h, float sigma,
                         float4* __restrict__ ga, float4* __restrict__ gb, float* __restrict__ gfull,
                         float* __restrict__ det_out, int8_t* __restrict__ f64flag,
@@ -146,6 +157,7 @@ __global__ void k_cov_G(GridView g, const float4* __restrict__ pos, const float4
   if (t >= n) return;
   float4 p = pos[t];
   float4 xp = xm0[t];
+  const float4 lp = xlo[t];
   int cx, cy, cz;
   cell_of(g, p.x, p.y, p.z, cx, cy, cz);
   Kahan ws, c00, c01, c02, c11, c12, c22;
@@ -155,7 +167,11 @@ __global__ void k_cov_G(GridView g, const float4* __restrict__ pos, const float4
       if (!nb_row(g, cx, cy + dy, cz + dz, &s, &e)) continue;
       for (int j = s; j < e; ++j) {
         float4 q = __ldg(xm0 + j);
-        float dx = __fsub_rn(q.x, xp.x), dy2 = __fsub_rn(q.y, xp.y), dz2 = __fsub_rn(q.z, xp.z);
+        const float4 lq = __ldg(xlo + j);
+        // centre difference from the hi parts (exact for nearby centres) plus the lo parts
+        float dx = __fadd_rn(__fsub_rn(q.x, xp.x), __fsub_rn(lq.x, lp.x));
+        float dy2 = __fadd_rn(__fsub_rn(q.y, xp.y), __fsub_rn(lq.y, lp.y));
+        float dz2 = __fadd_rn(__fsub_rn(q.z, xp.z), __fsub_rn(lq.z, lp.z));
         float d2 = d2_exact(dx, dy2, dz2);
         if (d2 >= nI2) continue;
         float w = wij_f(__fsqrt_rn(d2), nI, inv_h3);
@@ -211,18 +227,19 @@ void stage_aniso(pi_frame* f) {
   const float nI2 = nI * nI;
   const float inv_h3 = (float)(1.0 / ((double)nI * nI * nI));
   const float delta = (float)0.9;
-  const float c_self = 1 - delta, c_mean = delta;
+  const float c_mean = delta;
   const float h = r * 2.0f;
   f->xm.alloc(f->ctx, s, n);
   f->nrm.alloc(f->ctx, s, n);  // holds the pass-1 centres until the normals overwrite it
   f->ga.alloc(f->ctx, s, n);
   f->gb.alloc(f->ctx, s, n);
+  f->xlo.alloc(f->ctx, s, n);
   f->gfull.alloc(f->ctx, s, n * 9);
   f->det.alloc(f->ctx, s, n);
   f->f64flag.alloc(f->ctx, s, n);
   counters_reset(f);
-  PI_LAUNCH(k_xmean, div_up(n, 128), 128, 0, s, g, f->pos.p, n, nI, nI2, inv_h3, c_self, c_mean, f->nrm.p);
-  PI_LAUNCH(k_cov_G, div_up(n, 128), 128, 0, s, g, f->pos.p, f->nrm.p, f->xm.p, n, nI, nI2, inv_h3, f->influ2,
+  PI_LAUNCH(k_xmean, div_up(n, 128), 128, 0, s, g, f->pos.p, n, nI, nI2, inv_h3, c_mean, f->nrm.p, f->xlo.p);
+  PI_LAUNCH(k_cov_G, div_up(n, 128), 128, 0, s, g, f->pos.p, f->nrm.p, f->xlo.p, f->xm.p, n, nI, nI2, inv_h3, f->influ2,
             1.0f / h, f->sigma, f->ga.p, f->gb.p, f->gfull.p, f->det.p, f->f64flag.p, f->dcount.p);
   unsigned long long c[8];
   counters_read(f, c);

@@ -30,9 +30,10 @@ struct GridView {
 
 struct PartView {
   const float4* pos;
-  const float4* xm;
+  const float4* xm;   // (centre rounded to float, cull radius^2)
   const float4* ga;
   const float4* gb;
+  const float4* xlo;  // (centre - rounded centre, 0): the low part of the centre
 };
 
 // Event counters (field evaluations, candidate pairs, ...) striped over 64
@@ -124,8 +125,9 @@ __device__ __forceinline__ float field_sum(const GridView& g, const PartView& P,
         if (e2 < x.w) {
           float4 a = __ldg(P.ga + j);
           float4 b = __ldg(P.gb + j);
+          const float4 lo = __ldg(P.xlo + j);
           float u0, u1, u2;
-          amul(a, b, dx, dyy, dzz, u0, u1, u2);
+          amul(a, b, dx - lo.x, dyy - lo.y, dzz - lo.z, u0, u1, u2);
           float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
           if (s2 < 4.0f) acc.add(b.z * bspline_s2(s2));
         }

@@ -463,7 +463,7 @@ void stage_extract(pi_frame* f) {
     f->mk.alloc(c, s, nv * 2 > 0 ? nv * 2 : 2);
     const GridHost& gh = f->g;
     BisectArgs ba{GridView{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p},
-                  PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p}, f->iso, f->P.radius / 2};
+                  PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p}, f->iso, f->P.radius / 2};
     PI_LAUNCH(k_bisect, div_up(nv, 128), 128, 0, s, ba, nv, rep.p, slotA.p, slotB.p, f->nd_v.p, f->nd_id.p, f->mv.p,
               f->mk.p, f->dcount.p);
     // 7. triangles

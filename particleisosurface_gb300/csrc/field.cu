@@ -30,8 +30,9 @@ __device__ __forceinline__ void grad_sum(const GridView& g, const PartView& P, f
         if (e2 < 0.25f * x.w) {  // |A d| < 1 needs |d| < R / 2
           float4 a = __ldg(P.ga + j);
           float4 b = __ldg(P.gb + j);
+          const float4 lo = __ldg(P.xlo + j);
           float u0, u1, u2;
-          amul(a, b, dx, dyy, dzz, u0, u1, u2);
+          amul(a, b, dx - lo.x, dyy - lo.y, dzz - lo.z, u0, u1, u2);
           float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
           if (s2 < 1.0f) {
             float om = 1.0f - s2;
@@ -79,7 +80,7 @@ static GridView gview(pi_frame* f) {
   const GridHost& gh = f->g;
   return GridView{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p};
 }
-static PartView pview(pi_frame* f) { return PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p}; }
+static PartView pview(pi_frame* f) { return PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p}; }
 
 // -6 h^5 with h = 2r (see AnisotropicInterpolateGrad in A = G / h units)
 static float grad_scale(pi_frame* f) {

@@ -74,6 +74,7 @@ struct pi_frame {
   pisurf::DBuf<uint32_t> skey;   // N, sorted key+1
   pisurf::DBuf<int> off;         // C+1 cell offsets
   pisurf::DBuf<float4> pos, xm, ga, gb, nrm;  // N, sorted order
+  pisurf::DBuf<float4> xlo;      // N, sorted order: centre minus its float rounding
   pisurf::DBuf<float> gfull;     // N*9, sorted order (dumps)
   pisurf::DBuf<float> det;       // N, sorted order (dumps)
   pisurf::DBuf<int8_t> f64flag;  // N, sorted order

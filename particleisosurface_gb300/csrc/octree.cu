@@ -245,8 +245,9 @@ __global__ void k_q_eval(QArgs a, const int* __restrict__ order, const int* __re
           if (mine && e2 < x.w) {
             const float4 ga = __ldg(a.P.ga + j);
             const float4 gb = __ldg(a.P.gb + j);
+            const float4 lo = __ldg(a.P.xlo + j);
             float u0, u1, u2;
-            amul(ga, gb, dx, dyy, dzz, u0, u1, u2);
+            amul(ga, gb, dx - lo.x, dyy - lo.y, dzz - lo.z, u0, u1, u2);
             const float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
             if (s2 < 4.0f) acc.add(gb.z * bspline_s2(s2));
           }
@@ -514,7 +515,7 @@ void stage_octree(pi_frame* f) {
   f->nNodes = 1;
   const GridHost& gh = f->g;
   GridView g{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p};
-  PartView P{f->pos.p, f->xm.p, f->ga.p, f->gb.p};
+  PartView P{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p};
   const int ekx = gh.nx + 4, eky = gh.ny + 4;
   const long long ek = (long long)ekx * eky * (gh.nz + 4) * 8;  // buckets: cell x octant
   counters_reset(f);

@@ -170,7 +170,7 @@ void qef_level(pi_frame* f, long long lb, long long le) {
   cudaStream_t s = f->ctx->stream;
   const GridHost& gh = f->g;
   QefArgs qa{GridView{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p},
-             PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p}, f->iso, f->P.radius, lb, le};
+             PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p}, f->iso, f->P.radius, lb, le};
   PI_LAUNCH(k_qef, div_up(le - lb, 64), 64, 0, s, qa, f->nd_v.p, f->nd_c.p, f->nd_type.p, f->nd_samp.p, nullptr,
             f->dcount.p);
 }
