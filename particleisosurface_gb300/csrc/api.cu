@@ -84,6 +84,7 @@ template struct DBuf<float>;
 template struct DBuf<float4>;
 template struct DBuf<int>;
 template struct DBuf<int4>;
+template struct DBuf<int2>;
 template struct DBuf<unsigned>;
 template struct DBuf<int8_t>;
 template struct DBuf<uint64_t>;

@@ -12,13 +12,17 @@
 //                reference's block of box +- 1 cell, so the verdict is the
 //                reference's.
 //   k_q_count /  the 27 lattice samples and the centre of every non-empty
-//   k_q_place    node (TNode::GenerateSampling, src/iso_method_ours.cpp:52-75)
-//                are bucketed by hash cell with an atomic counting sort; the
-//                order inside a bucket does not affect any result.
+//   k_q_dedupe   node (TNode::GenerateSampling, src/iso_method_ours.cpp:52-75)
+//                are bucketed by hash cell and octant with an atomic counting
+//                sort, and points with bit-identical coordinates (shared by
+//                neighbouring nodes) are evaluated once; the order inside a
+//                bucket does not affect any result.
 //   k_q_eval     field at the bucketed points (Evaluator::SingleEval,
-//                src/evaluator.cpp:60-87): lanes of a warp whose points share
-//                a cell walk that cell's 27-cell candidate list in lockstep,
-//                so candidate loads are broadcasts and loop bounds uniform.
+//                src/evaluator.cpp:60-87): one warp per chunk of <= 32
+//                samples of one bucket; the cell's 27-cell candidates are
+//                filtered against the chunk's bounding box into shared
+//                memory, then every lane walks the survivors (broadcast
+//                loads, uniform loop bounds).
 //   k_classify   afterSampleEval (:237-273): sign change against sample 0
 //                (ballot), leaf by size, and the normal-coherence curvature
 //                |sum n| / sum |n| computed only where the classification reads
@@ -36,6 +40,9 @@ namespace pisurf {
 enum : int8_t { T_EMPTY = 0, T_INTERNAL = 1, T_LEAF = 2, T_UNCERTAIN = 3 };
 
 constexpr int kQ = 28;  // 27 samples + the centre per node
+constexpr int kEvalWarps = 8;  // warps per block of k_q_eval
+constexpr int kCandBuf = 64;   // staged candidate records per warp
+constexpr int kChunk = 64;     // samples per chunk of k_q_eval: two per lane
 
 struct LevelArgs {
   GridView g;
@@ -162,11 +169,10 @@ __device__ __forceinline__ int ext_key(const QArgs& a, int cx, int cy, int cz) {
 }
 
 // Bucket of a sample: its hash cell (extended key) times 8 plus the octant of
-// the cell it lies in, so that a warp's points are close together.  Slots
-// within a bucket come from one warp-aggregated atomic per bucket and warp.
+// the cell it lies in, so that a warp's points are close together.  Counts
+// come from one warp-aggregated atomic per bucket and warp.
 __global__ void k_q_count(QArgs a, const float4* __restrict__ nd_c, const float4* __restrict__ nd_v,
-                          const int8_t* __restrict__ nd_type, int* __restrict__ qcnt, int* __restrict__ qkey,
-                          int* __restrict__ qslot) {
+                          const int8_t* __restrict__ nd_type, int* __restrict__ qcnt, int* __restrict__ qkey) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const long long node = a.lb + i / kQ;
@@ -186,82 +192,260 @@ __global__ void k_q_count(QArgs a, const float4* __restrict__ nd_c, const float4
   }
   const unsigned peers = __match_any_sync(0xffffffffu, k);
   const int leader = __ffs(peers) - 1;
-  int base = 0;
-  if (valid && lane == leader) base = atomicAdd(qcnt + k, __popc(peers));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (in_level) {
-    qkey[i] = k;
-    if (valid) qslot[i] = base + __popc(peers & ((1u << lane) - 1u));
-  }
+  if (valid && lane == leader) atomicAdd(qcnt + k, __popc(peers));
+  if (in_level) qkey[i] = k;
 }
 
-__global__ void k_q_place(long long n, const int* __restrict__ qkey, const int* __restrict__ qslot,
-                          const int* __restrict__ qoff, int* __restrict__ order) {
+__device__ __forceinline__ uint32_t hash3(float x, float y, float z) {
+  uint32_t h = __float_as_uint(x) * 0x9E3779B1u ^ __float_as_uint(y) * 0x85EBCA77u ^
+               __float_as_uint(z) * 0xC2B2AE3Du;
+  h ^= h >> 15;
+  h *= 0x2C1B3C6Du;
+  h ^= h >> 12;
+  return h;
+}
+
+// Neighbouring nodes share lattice points, and most shared samples have the
+// same float coordinates bit for bit (about 2.4 per point on liquid
+// surfaces).  Equal coordinates give equal field values (same cell, same
+// candidates, same summation order), so each distinct point is evaluated
+// once.  Equal points share a bucket; bucket k owns hash slots
+// [2 qoff[k], 2 qoff[k+1]) and a point's first inserter becomes its
+// representative.  On a dense level representatives get consecutive places
+// in the bucket's range of `order` and every kChunk-th place starts a chunk
+// (bucket, place); on a sparse level they are listed compactly in `order`
+// and *nchunks counts them.
+__global__ void k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c, const float4* __restrict__ nd_v,
+                           const int* __restrict__ qkey, const int* __restrict__ qoff, unsigned* __restrict__ hslot,
+                           int* __restrict__ ucnt, int* __restrict__ rep, int* __restrict__ order,
+                           int2* __restrict__ chunks, int* __restrict__ nchunks, int dense) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int k = qkey[i];
-  if (k >= 0) order[qoff[k] + qslot[i]] = (int)i;
+  const int lane = threadIdx.x & 31;
+  const int k = i < n ? qkey[i] : -1;
+  bool head = false, uniq = false;
+  int place = 0;
+  if (k >= 0) {
+    float qx, qy, qz;
+    const long long node = a.lb + i / kQ;
+    sample_point(nd_c[node], nd_v[node], (int)(i % kQ), qx, qy, qz);
+    const long long base = 2LL * qoff[k];
+    const uint32_t m = 2u * (uint32_t)(qoff[k + 1] - qoff[k]);
+    uint32_t pos = __umulhi(hash3(qx, qy, qz), m);
+    int r = (int)i;
+    for (uint32_t t = 0; t < m; ++t) {  // the region is at most half full
+      unsigned cur = hslot[base + pos];
+      if (cur == 0u) {
+        cur = atomicCAS(hslot + base + pos, 0u, (unsigned)i + 1u);
+        if (cur == 0u) break;  // first inserter: i represents the point
+      }
+      const long long j = (long long)cur - 1;
+      const long long nj = a.lb + j / kQ;
+      float px, py, pz;
+      sample_point(nd_c[nj], nd_v[nj], (int)(j % kQ), px, py, pz);
+      if (__float_as_uint(px) == __float_as_uint(qx) && __float_as_uint(py) == __float_as_uint(qy) &&
+          __float_as_uint(pz) == __float_as_uint(qz)) {
+        r = (int)j;
+        break;
+      }
+      pos = pos + 1u == m ? 0u : pos + 1u;
+    }
+    rep[i] = r;
+    uniq = r == (int)i;
+  }
+  if (!dense) {
+    // sparse level: representatives go to a compact list, one thread each
+    const unsigned um = __ballot_sync(0xffffffffu, uniq);
+    if (um == 0u) return;
+    const int ul = __ffs(um) - 1;
+    int ub = 0;
+    if (lane == ul) ub = atomicAdd(nchunks, __popc(um));
+    ub = __shfl_sync(0xffffffffu, ub, ul);
+    if (uniq) order[ub + __popc(um & ((1u << lane) - 1u))] = (int)i;
+    return;
+  }
+  // dense level: places for the representatives, one atomic per bucket and warp
+  const unsigned um = __ballot_sync(0xffffffffu, uniq);
+  const unsigned peers = __match_any_sync(0xffffffffu, uniq ? k : -1) & um;
+  if (uniq) {
+    const int leader = __ffs(peers) - 1;
+    int b0 = 0;
+    if (lane == leader) b0 = atomicAdd(ucnt + k, __popc(peers));
+    b0 = __shfl_sync(peers, b0, leader);
+    place = b0 + __popc(peers & ((1u << lane) - 1u));
+    order[qoff[k] + place] = (int)i;
+    head = place % kChunk == 0;
+  }
+  const unsigned hm = __ballot_sync(0xffffffffu, head);
+  if (hm == 0u) return;
+  const int hl = __ffs(hm) - 1;
+  int cb = 0;
+  if (lane == hl) cb = atomicAdd(nchunks, __popc(hm));
+  cb = __shfl_sync(0xffffffffu, cb, hl);
+  if (head) chunks[cb + __popc(hm & ((1u << lane) - 1u))] = make_int2(k, place);
 }
 
-__global__ void k_q_eval(QArgs a, const int* __restrict__ order, const int* __restrict__ total_ptr,
-                         const float4* __restrict__ nd_c, const float4* __restrict__ nd_v, float* __restrict__ qval,
-                         unsigned long long* __restrict__ counters) {
+// Order-preserving map of a float onto a signed int (for warp min / max).
+__device__ __forceinline__ int fkey(float v) {
+  const int i = __float_as_int(v);
+  return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float fkey_inv(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff); }
+
+
+// Field at the samples of one chunk per warp (persistent, grid-stride over
+// the chunks); lane l holds samples l and l + 32 of the chunk.  All samples
+// of a chunk share a hash cell, hence the 27-cell candidate list of
+// Evaluator::SingleEval.  The warp tests 32 candidates at a time against the
+// chunk's bounding box: a candidate whose support radius R (|G d| < 2h needs
+// |d| < R, stored as R^2 * 1.002) does not reach the box contributes to no
+// sample.  Survivors' records are staged in shared memory in candidate order
+// and every lane walks them, so each sample's compensated sum sees the
+// in-support terms in candidate order.
+__global__ void __launch_bounds__(32 * kEvalWarps, 3) k_q_eval(QArgs a, const int* __restrict__ order,
+                                                            const int* __restrict__ qoff,
+                                                            const int* __restrict__ ucnt,
+                                                            const int2* __restrict__ chunks,
+                                                            const int* __restrict__ nchunks_ptr,
+                                                            const float4* __restrict__ nd_c,
+                                                            const float4* __restrict__ nd_v,
+                                                            float* __restrict__ qval,
+                                                            unsigned long long* __restrict__ counters) {
+  __shared__ float4 s_x[kEvalWarps][kCandBuf], s_a[kEvalWarps][kCandBuf], s_b[kEvalWarps][kCandBuf],
+      s_l[kEvalWarps][kCandBuf];
   const int lane = threadIdx.x & 31;
-  const long long wbase = ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
-  const long long total = *total_ptr;
-  if (wbase >= total) return;
-  const long long idx = wbase + lane;
-  const bool active = idx < total;
-  int q = 0, cx = 0, cy = 0, cz = 0, key = -1;
-  float qx = 0.f, qy = 0.f, qz = 0.f;
-  if (active) {
-    q = order[idx];
-    const long long node = a.lb + q / kQ;
-    sample_point(nd_c[node], nd_v[node], q % kQ, qx, qy, qz);
-    cell_of(a.g, qx, qy, qz, cx, cy, cz);
-    key = ext_key(a, cx, cy, cz);
-  }
-  Kahan acc;
+  const int wib = threadIdx.x >> 5;
+  float4* cx4 = s_x[wib];
+  float4* ca4 = s_a[wib];
+  float4* cb4 = s_b[wib];
+  float4* cl4 = s_l[wib];
+  const unsigned lt = (1u << lane) - 1u;
+  const int nchunks = *nchunks_ptr;
+  const int nwarps = gridDim.x * kEvalWarps;
   long long pairs = 0;
-  unsigned todo = __ballot_sync(0xffffffffu, active);
-  while (todo) {
-    const int leader = __ffs(todo) - 1;
-    const int lkey = __shfl_sync(0xffffffffu, key, leader);
-    const unsigned grp = __ballot_sync(0xffffffffu, active && key == lkey);
-    const int gx = __shfl_sync(0xffffffffu, cx, leader);
-    const int gy = __shfl_sync(0xffffffffu, cy, leader);
-    const int gz = __shfl_sync(0xffffffffu, cz, leader);
-    const bool mine = (grp >> lane) & 1u;
+  for (int ci = blockIdx.x * kEvalWarps + wib; ci < nchunks; ci += nwarps) {
+    const int2 ch = chunks[ci];
+    const int len = min(kChunk, __ldg(ucnt + ch.x) - ch.y);
+    const int* ord = order + __ldg(qoff + ch.x) + ch.y;
+    const bool act0 = lane < len, act1 = lane + 32 < len;
+    const bool two = len > 32;  // warp-uniform
+    int q0 = 0, q1 = 0;
+    float x0 = 0.f, y0 = 0.f, z0 = 0.f, x1 = 0.f, y1 = 0.f, z1 = 0.f;
+    if (act0) {
+      q0 = ord[lane];
+      const long long node = a.lb + q0 / kQ;
+      sample_point(nd_c[node], nd_v[node], q0 % kQ, x0, y0, z0);
+    }
+    if (act1) {
+      q1 = ord[lane + 32];
+      const long long node = a.lb + q1 / kQ;
+      sample_point(nd_c[node], nd_v[node], q1 % kQ, x1, y1, z1);
+    }
+    int cx, cy, cz;
+    cell_of(a.g, __shfl_sync(0xffffffffu, x0, 0), __shfl_sync(0xffffffffu, y0, 0),
+            __shfl_sync(0xffffffffu, z0, 0), cx, cy, cz);
+    // bounding box of the chunk's samples
+    const int kmin = 0x7fffffff, kmax = (int)0x80000000;
+    const float blx = fkey_inv(__reduce_min_sync(0xffffffffu, min(act0 ? fkey(x0) : kmin, act1 ? fkey(x1) : kmin)));
+    const float bly = fkey_inv(__reduce_min_sync(0xffffffffu, min(act0 ? fkey(y0) : kmin, act1 ? fkey(y1) : kmin)));
+    const float blz = fkey_inv(__reduce_min_sync(0xffffffffu, min(act0 ? fkey(z0) : kmin, act1 ? fkey(z1) : kmin)));
+    const float bhx = fkey_inv(__reduce_max_sync(0xffffffffu, max(act0 ? fkey(x0) : kmax, act1 ? fkey(x1) : kmax)));
+    const float bhy = fkey_inv(__reduce_max_sync(0xffffffffu, max(act0 ? fkey(y0) : kmax, act1 ? fkey(y1) : kmax)));
+    const float bhz = fkey_inv(__reduce_max_sync(0xffffffffu, max(act0 ? fkey(z0) : kmax, act1 ? fkey(z1) : kmax)));
+    // compensated sums (Kahan), updated only for in-support terms
+    float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
+    int nc = 0;
+    auto flush = [&]() {
+      __syncwarp();
+#pragma unroll 2
+      for (int t = 0; t < nc; ++t) {
+        const float4 x = cx4[t], ga = ca4[t], gb = cb4[t], lo = cl4[t];
+        {
+          float u0, u1, u2;
+          amul(ga, gb, (x0 - x.x) - lo.x, (y0 - x.y) - lo.y, (z0 - x.z) - lo.z, u0, u1, u2);
+          const float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
+          const float y = __fsub_rn(gb.z * bspline_s2(s2), c0);
+          const float tt = __fadd_rn(s0, y);
+          const float cn = __fsub_rn(__fsub_rn(tt, s0), y);
+          const bool hit = act0 && s2 < 4.0f;
+          s0 = hit ? tt : s0;
+          c0 = hit ? cn : c0;
+        }
+        if (two) {
+          float u0, u1, u2;
+          amul(ga, gb, (x1 - x.x) - lo.x, (y1 - x.y) - lo.y, (z1 - x.z) - lo.z, u0, u1, u2);
+          const float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
+          const float y = __fsub_rn(gb.z * bspline_s2(s2), c1);
+          const float tt = __fadd_rn(s1, y);
+          const float cn = __fsub_rn(__fsub_rn(tt, s1), y);
+          const bool hit = act1 && s2 < 4.0f;
+          s1 = hit ? tt : s1;
+          c1 = hit ? cn : c1;
+        }
+      }
+      __syncwarp();
+      nc = 0;
+    };
     for (int dz = -1; dz <= 1; ++dz)
       for (int dy = -1; dy <= 1; ++dy) {
         int s, e;
-        if (!nb_row(a.g, gx, gy + dy, gz + dz, &s, &e)) continue;
-        if (mine) pairs += e - s;
-#pragma unroll 2
-        for (int j = s; j < e; ++j) {
-          const float4 x = __ldg(a.P.xm + j);
-          const float dx = qx - x.x, dyy = qy - x.y, dzz = qz - x.z;
-          const float e2 = fmaf(dx, dx, fmaf(dyy, dyy, dzz * dzz));
-          if (mine && e2 < x.w) {
-            const float4 ga = __ldg(a.P.ga + j);
-            const float4 gb = __ldg(a.P.gb + j);
-            const float4 lo = __ldg(a.P.xlo + j);
-            float u0, u1, u2;
-            amul(ga, gb, dx - lo.x, dyy - lo.y, dzz - lo.z, u0, u1, u2);
-            const float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
-            if (s2 < 4.0f) acc.add(gb.z * bspline_s2(s2));
+        if (!nb_row(a.g, cx, cy + dy, cz + dz, &s, &e)) continue;
+        pairs += (long long)(e - s) * ((act0 ? 1 : 0) + (act1 ? 1 : 0));
+        for (int j0 = s; j0 < e; j0 += 32) {
+          const int j = j0 + lane;
+          bool pass = false;
+          float4 x;
+          if (j < e) {
+            x = __ldg(a.P.xm + j);
+            const float ex = fmaxf(fmaxf(blx - x.x, x.x - bhx), 0.f);
+            const float ey = fmaxf(fmaxf(bly - x.y, x.y - bhy), 0.f);
+            const float ez = fmaxf(fmaxf(blz - x.z, x.z - bhz), 0.f);
+            pass = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < x.w;
           }
+          const unsigned pm = __ballot_sync(0xffffffffu, pass);
+          if (pass) {
+            const int p = nc + __popc(pm & lt);
+            cx4[p] = x;
+            ca4[p] = __ldg(a.P.ga + j);
+            cb4[p] = __ldg(a.P.gb + j);
+            cl4[p] = __ldg(a.P.xlo + j);
+          }
+          nc += __popc(pm);
+          if (nc > kCandBuf - 32) flush();
         }
       }
-    todo &= ~grp;
+    flush();
+    if (act0) qval[q0] = a.iso - s0;
+    if (act1) qval[q1] = a.iso - s1;
   }
-  if (active) qval[q] = a.iso - acc.s;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
-  if (lane == 0) stripe_add(counters, 1, (unsigned long long)pairs);
+  if (lane == 0 && pairs) stripe_add(counters, 1, (unsigned long long)pairs);
 }
 
-__global__ void k_classify(LevelArgs a, const float* __restrict__ qval, const float4* __restrict__ nd_c,
+// Sparse levels (a few distinct samples per bucket): one thread per distinct
+// sample, each walking its own 27-cell candidate list (field_sum, the same
+// tests and summation order as k_q_eval).
+__global__ void __launch_bounds__(256, 4) k_q_eval_thread(QArgs a, const int* __restrict__ list,
+                                                       const int* __restrict__ count_ptr,
+                                                       const float4* __restrict__ nd_c,
+                                                       const float4* __restrict__ nd_v, float* __restrict__ qval,
+                                                       unsigned long long* __restrict__ counters) {
+  const int n = *count_ptr;
+  long long pairs = 0;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int q = list[t];
+    const long long node = a.lb + q / kQ;
+    float qx, qy, qz;
+    sample_point(nd_c[node], nd_v[node], q % kQ, qx, qy, qz);
+    qval[q] = a.iso - field_sum(a.g, a.P, qx, qy, qz, &pairs);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+  if ((threadIdx.x & 31) == 0 && pairs) stripe_add(counters, 1, (unsigned long long)pairs);
+}
+
+__global__ void k_classify(LevelArgs a, const float* __restrict__ qval, const int* __restrict__ rep,
+                           const float4* __restrict__ nd_c,
                            float4* __restrict__ nd_v, int8_t* __restrict__ nd_type, int8_t* __restrict__ nd_sc,
                            float* __restrict__ nd_curv, float* __restrict__ nd_samp, int qef, int curv_known,
                            unsigned long long* __restrict__ counters) {
@@ -270,7 +454,7 @@ __global__ void k_classify(LevelArgs a, const float* __restrict__ qval, const fl
   if (node >= a.le) return;
   if (nd_type[node] != T_UNCERTAIN) return;  // warp-uniform
   const long long qb = (node - a.lb) * kQ;
-  const float val = lane < kQ ? qval[qb + lane] : 0.f;
+  const float val = lane < kQ ? qval[rep[qb + lane]] : 0.f;
   // GridEval sign change against sample 0, ">= 0" (src/evaluator.cpp:169-172)
   const unsigned pos_mask = __ballot_sync(0xffffffffu, lane < 27 && val >= 0.f);
   const bool origin = pos_mask & 1u;
@@ -519,9 +703,20 @@ void stage_octree(pi_frame* f) {
   const int ekx = gh.nx + 4, eky = gh.ny + 4;
   const long long ek = (long long)ekx * eky * (gh.nz + 4) * 8;  // buckets: cell x octant
   counters_reset(f);
-  DBuf<int> flag, qcnt, qkey, qslot, order;
+  DBuf<int> flag, qcnt, qkey, rep, order, ucnt;
+  DBuf<unsigned> hslot;
+  DBuf<int2> chunks;
   DBuf<float> qval;
-  qcnt.alloc(ctx, s, ek + 1);
+  qcnt.alloc(ctx, s, ek + 2);  // bucket counts, total, chunk count
+  ucnt.alloc(ctx, s, ek);      // distinct points per bucket
+  static thread_local int eval_occ[64] = {0};
+  const int dev = ctx->device & 63;
+  if (eval_occ[dev] == 0) {
+    int nb = 0;
+    PI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_q_eval, 32 * kEvalWarps, 0));
+    eval_occ[dev] = nb > 0 ? nb : 1;
+  }
+  const int eval_blocks = ctx->smCount * eval_occ[dev];
   long long lb = 0, le = 1;
   bool known = false;  // emptiness and curvature of this level settled by the parents' scan
   for (int depth = 0;; ++depth) {
@@ -536,20 +731,32 @@ void stage_octree(pi_frame* f) {
       const long long qn = nl * kQ;
       if (f->tmp.n < scan_tmp_ints(ek + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(ek + 1));
       qkey.alloc(ctx, s, qn);
-      qslot.alloc(ctx, s, qn);
+      rep.alloc(ctx, s, qn);
+      hslot.alloc(ctx, s, 2 * qn);
       qval.alloc(ctx, s, qn);
       order.alloc(ctx, s, qn);
-      PI_CUDA(cudaMemsetAsync(qcnt.p, 0, sizeof(int) * (ek + 1), s));
+      chunks.alloc(ctx, s, qn);
+      PI_CUDA(cudaMemsetAsync(qcnt.p, 0, sizeof(int) * (ek + 2), s));
+      PI_CUDA(cudaMemsetAsync(ucnt.p, 0, sizeof(int) * ek, s));
+      PI_CUDA(cudaMemsetAsync(hslot.p, 0, sizeof(unsigned) * 2 * qn, s));
       QArgs qa{g, P, f->iso, lb, le, ekx, eky};
-      PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p,
-                qslot.p);
+      PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
       exclusive_scan_i32(qcnt.p, qcnt.p, ek + 1, nullptr, f->tmp.p, s);
-      PI_LAUNCH(k_q_place, div_up(qn, 256), 256, 0, s, qn, qkey.p, qslot.p, qcnt.p, order.p);
+      // the deepest level (node size r, samples r/2 apart) holds tens of
+      // distinct samples per bucket; coarser levels hold a few
+      const int dense = depth == f->dmax ? 1 : 0;
+      PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
+                ucnt.p, rep.p, order.p, chunks.p, qcnt.p + ek + 1, dense);
       prof_begin(ctx, s);
-      PI_LAUNCH(k_q_eval, div_up(div_up(qn, 32), wpb), 32 * wpb, 0, s, qa, order.p, qcnt.p + ek, f->nd_c.p,
-                f->nd_v.p, qval.p, f->dcount.p);
+      if (dense)
+        PI_LAUNCH(k_q_eval, (int)std::min<long long>(eval_blocks, div_up(qn, 32 * kEvalWarps)), 32 * kEvalWarps, 0,
+                  s, qa, order.p, qcnt.p, ucnt.p, chunks.p, qcnt.p + ek + 1, f->nd_c.p, f->nd_v.p, qval.p,
+                  f->dcount.p);
+      else
+        PI_LAUNCH(k_q_eval_thread, (int)std::min<long long>((long long)ctx->smCount * 8, div_up(qn, 256)), 256, 0,
+                  s, qa, order.p, qcnt.p + ek + 1, f->nd_c.p, f->nd_v.p, qval.p, f->dcount.p);
       prof_end(ctx, s, -1, -1);
-      PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, f->nd_c.p, f->nd_v.p, f->nd_type.p,
+      PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p, f->nd_type.p,
                 f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p);
       if (f->P.qef) qef_level(f, lb, le);
     }
