@@ -399,6 +399,25 @@ def ours(a):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
 
+    # ---- the same frame with the per-leaf FP64 QEF solve switched on ----
+    pq = N.default_params(fr.radius)
+    pq.qef = 1
+    fq = N.Frame(ctx, pq).upload(fr.xyz)
+    for _ in range(a.warmup):
+        fq.reset().run()
+    evq = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    barrier()
+    for k in range(a.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xff)
+        evq[k][0].record(stream)
+        fq.reset().run()
+        evq[k][1].record(stream)
+    barrier()
+    qef_ms = float(np.mean([s.elapsed_time(e) for s, e in evq]))
+    qinfo = fq.info()
+    fq.close()
+
     # ---- end to end through the C ABI with pinned host buffers: e2e ----
     xyz_h = torch.from_numpy(fr.xyz).pin_memory()
     mv = int(info["num_vertices"] * 1.5) + 1024
@@ -452,13 +471,17 @@ def ours(a):
             "e2e": {"value": world * 1000.0 / e2e_ms, "unit": UNIT, "h2d_bytes_per_step": 12 * fr.n,
                     "d2h_bytes_per_step": 12 * int(nv.value) + 12 * int(nt.value)},
             "clocks": ck,
+            "qef_on": {"ms_per_step": qef_ms, "frames_per_s": world * 1000.0 / qef_ms,
+                       "field_evals_per_frame": qinfo["field_evals"],
+                       "candidate_pairs_per_frame": qinfo["candidate_pairs"],
+                       "qef_vertices_accepted": qinfo["qef_accepted"]},
         }
         # dominant kernel: field evaluation at octree samples (k_q_eval)
         if kt["ms"] > 0 and kt["launches"] > 0:
             achieved = kt["pairs"] * FLOPS_PER_PAIR / (kt["ms"] / 1000.0) / 1e12
             sm_mhz = ck.get("sm_max_mhz") or 2070.0
             peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-            line["roofline"] = {"kernel": "k_q_eval (field evaluation at octree samples)", "bound": "fp32",
+            line["roofline"] = {"kernel": "k_q_eval_thread + k_q_eval (field evaluation at octree samples)", "bound": "fp32",
                                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                                 "traffic": None,
                                 "peak_source": "nominal FP32: 152 SMs x 128 lanes x 2 flop x max SM clock "

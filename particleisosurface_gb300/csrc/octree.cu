@@ -53,6 +53,7 @@ struct LevelArgs {
   float radius;
   long long lb, le;  // node range of the level
   int big;           // depth < D_min
+  PartView P;
 };
 
 __device__ __forceinline__ float warp_sum(float v) {
@@ -444,6 +445,35 @@ __global__ void __launch_bounds__(256, 4) k_q_eval_thread(QArgs a, const int* __
   if ((threadIdx.x & 31) == 0 && pairs) stripe_add(counters, 1, (unsigned long long)pairs);
 }
 
+// Leaves by size without QEF: afterSampleEval (src/surface_reconstructor.cpp:
+// 247-255) makes every node of size r a LEAF whose value is SingleEval at its
+// position; the 27 lattice samples of GridEval only set a sign-change flag
+// that nothing reads there (they feed NodeCalcNode, i.e. QEF mode only), so
+// only the node position is evaluated.  The node's signchange stays 0.
+__global__ void __launch_bounds__(256, 4) k_leaf_level(LevelArgs a, const float4* __restrict__ nd_c,
+                                                       float4* __restrict__ nd_v, int8_t* __restrict__ nd_type,
+                                                       unsigned long long* __restrict__ counters) {
+  long long pairs = 0, evals = 0;
+  for (long long node = a.lb + (long long)blockIdx.x * blockDim.x + threadIdx.x; node < a.le;
+       node += (long long)gridDim.x * blockDim.x) {
+    if (nd_type[node] != T_UNCERTAIN) continue;
+    float4 v = nd_v[node];
+    v.w = a.iso - field_sum(a.g, a.P, v.x, v.y, v.z, &pairs);
+    nd_v[node] = v;
+    nd_type[node] = T_LEAF;
+    ++evals;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+    evals += __shfl_xor_sync(0xffffffffu, evals, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (pairs) stripe_add(counters, 1, (unsigned long long)pairs);
+    if (evals) stripe_add(counters, 0, (unsigned long long)evals);
+  }
+}
+
 __global__ void k_classify(LevelArgs a, const float* __restrict__ qval, const int* __restrict__ rep,
                            const float4* __restrict__ nd_c,
                            float4* __restrict__ nd_v, int8_t* __restrict__ nd_type, int8_t* __restrict__ nd_sc,
@@ -723,11 +753,17 @@ void stage_octree(pi_frame* f) {
     f->levelBegin.push_back(lb);
     const long long nl = le - lb;
     LevelArgs la{g, f->pos.p, f->nrm.p, f->P.radius * f->P.smooth_factor, f->iso, f->P.radius, lb, le,
-                 depth < f->dmin ? 1 : 0};
+                 depth < f->dmin ? 1 : 0, P};
+    // every node of the level has half size rootH / 2^depth (children halve exactly)
+    const float cell_d = 2.0f * std::ldexp(f->rootH, -depth);
+    const bool leaf_level = (double)(cell_d - f->P.radius) < 1e-8;
     const int wpb = 8;  // warps per block
     if (!known)
       PI_LAUNCH(k_empty, div_up(nl, wpb), 32 * wpb, 0, s, la, f->nd_c.p, f->nd_v.p, f->nd_type.p, f->nd_curv.p);
-    if (depth >= f->dmin) {
+    if (depth >= f->dmin && leaf_level && !f->P.qef) {
+      PI_LAUNCH(k_leaf_level, (int)std::min<long long>((long long)ctx->smCount * 8, div_up(nl, 256)), 256, 0, s, la,
+                f->nd_c.p, f->nd_v.p, f->nd_type.p, f->dcount.p);
+    } else if (depth >= f->dmin) {
       const long long qn = nl * kQ;
       if (f->tmp.n < scan_tmp_ints(ek + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(ek + 1));
       qkey.alloc(ctx, s, qn);
