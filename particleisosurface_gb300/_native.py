@@ -15,6 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libpisurf.so")
 
 PI_OK = 0
+PI_OK, PI_ERR_INVALID, PI_ERR_CUDA, PI_ERR_NOMEM, PI_ERR_STATE, PI_ERR_LIMIT = 0, -1, -2, -3, -4, -5
 ERRORS = {-1: "PI_ERR_INVALID", -2: "PI_ERR_CUDA", -3: "PI_ERR_NOMEM", -4: "PI_ERR_STATE", -5: "PI_ERR_LIMIT"}
 
 DUMP_KEYS, DUMP_INDEX_LIST, DUMP_CELL_OFFSETS, DUMP_XMEANS, DUMP_G, DUMP_DET, DUMP_NORMALS, DUMP_NODES, \

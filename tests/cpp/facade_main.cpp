@@ -1,0 +1,93 @@
+// Host program written against the reference's C++ API (the calls of
+// runOurs, src/main.cpp:330-405), compiled against include/pisurf.hpp.
+//   facade_main <xyz float32 file> <n> <radius> <out.obj>
+// Prints one JSON line; exits 3 when no CUDA device is usable (the library
+// has no CPU fallback).
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <vector>
+
+#include "pisurf.hpp"
+
+int main(int argc, char** argv) {
+  if (argc != 5) {
+    std::fprintf(stderr, "usage: %s xyz.f32 n radius out.obj\n", argv[0]);
+    return 2;
+  }
+  const long n = std::atol(argv[2]);
+  const float radius = (float)std::atof(argv[3]);
+  std::vector<float> raw((size_t)n * 3);
+  std::ifstream in(argv[1], std::ios::binary);
+  in.read(reinterpret_cast<char*>(raw.data()), (std::streamsize)(raw.size() * sizeof(float)));
+  if (!in) {
+    std::fprintf(stderr, "cannot read %s\n", argv[1]);
+    return 2;
+  }
+  std::vector<pisurf::Vector3f> particles((size_t)n);
+  for (long i = 0; i < n; ++i) particles[i] = pisurf::Vector3f(raw[3 * i], raw[3 * i + 1], raw[3 * i + 2]);
+  std::vector<float> radiuses((size_t)n, radius);
+
+  Mesh mesh;
+  try {
+    SurfReconstructor constructor(particles, radiuses, &mesh, radius);
+    constructor.Run(1.9f, 2.0f);
+    writeObjFile(mesh, argv[4]);
+
+    std::shared_ptr<Evaluator> ev = constructor.getEvaluator();
+    std::shared_ptr<HashGrid> hg = constructor.getHashGrid();
+    float s0 = 0.f;
+    pisurf::Vector3f g0;
+    ev->SingleEvalWithGrad(particles[0], s0, g0);
+    std::vector<int> nb;
+    hg->GetPIdxList(particles[0], nb);
+    std::array<int, 3> xyz;
+    hg->CalcXYZIdx(particles[0], xyz);
+    const long long key0 = hg->CalcCellHash(xyz);
+    std::vector<int> inbox;
+    hg->GetInBoxParticles(pisurf::Vector3f(hg->Bounding[0], hg->Bounding[2], hg->Bounding[4]),
+                          pisurf::Vector3f(hg->Bounding[1], hg->Bounding[3], hg->Bounding[5]), inbox);
+
+    // GridEval over the root node's 27-point lattice (TNode::GenerateSampling)
+    std::shared_ptr<TNode> root = constructor.getRoot();
+    float samples[27 * 4], grads[27 * 3];
+    for (int z = 0; z <= 2; ++z)
+      for (int y = 0; y <= 2; ++y)
+        for (int x = 0; x <= 2; ++x) {
+          const int i = z * 9 + y * 3 + x;
+          const int t[3] = {x, y, z};
+          for (int c = 0; c < 3; ++c) {
+            const float lo = root->center[c] - root->half_length, hi = root->center[c] + root->half_length;
+            samples[i * 4 + c] = (1 - float(t[c]) / 2) * lo + (float(t[c]) / 2) * hi;
+          }
+          samples[i * 4 + 3] = 0.f;
+        }
+    bool signchange = false;
+    ev->GridEval(samples, grads, 2 * root->half_length, signchange, 2);
+
+    // walk the octree
+    long leaves = 0, nodes = 0;
+    std::vector<std::shared_ptr<TNode>> stack{root};
+    while (!stack.empty()) {
+      auto t = stack.back();
+      stack.pop_back();
+      ++nodes;
+      if (t->is_leaf()) {
+        if (t->type == pisurf::LEAF) ++leaves;
+        continue;
+      }
+      for (auto& c : t->children)
+        if (c) stack.push_back(c);
+    }
+    std::printf(
+        "{\"vertices\": %u, \"triangles\": %u, \"depth_max\": %d, \"depth_min\": %d, \"iso\": %.9g, "
+        "\"max_scalar\": %.9g, \"scalar0\": %.9g, \"neighbors0\": %zu, \"key0\": %lld, \"in_box\": %zu, "
+        "\"grid_sign_change\": %d, \"nodes\": %ld, \"leaves\": %ld}\n",
+        mesh.verticesNum, mesh.trianglesNum, constructor.getDepthMax(), constructor.getDepthMin(), ev->getIsoValue(),
+        ev->getMaxScalar(), s0, nb.size(), key0, inbox.size(), signchange ? 1 : 0, nodes, leaves);
+  } catch (const pisurf::Error& e) {
+    std::printf("{\"error\": %d, \"message\": \"%s\"}\n", e.code(), e.what());
+    return e.code() == PI_ERR_CUDA ? 3 : 1;
+  }
+  return 0;
+}

@@ -47,3 +47,19 @@ def test_budget_admission_serialises_large_requests():
     st = srv.stats()
     srv.close()
     assert st["completed"] == 4 and st["max_in_flight"] == 1, st
+
+
+def test_failed_request_reports_its_error_and_others_complete():
+    B.build()
+    good = synth.small_blob(n=3000, seed=43)
+    bad = N.default_params(good.radius)
+    bad.max_depth = 2  # the frame needs a deeper octree: PI_ERR_LIMIT inside the worker
+    srv = N.Server(0, slots=2, budget_bytes=0)
+    t_bad = srv.submit(good.xyz, bad)
+    t_good = srv.submit(good.xyz, N.default_params(good.radius))
+    with pytest.raises(N.PiError) as ei:
+        srv.result(t_bad)
+    assert ei.value.code == N.PI_ERR_LIMIT
+    v, t, lat, q = srv.result(t_good)
+    srv.close()
+    assert len(v) > 0 and len(t) > 0
