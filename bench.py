@@ -127,9 +127,12 @@ def serving(a):
         key = r["seq"]
         if key not in base:
             fr = synth.mixed_frame(r["seed"], r["n"], r["radius"])
-            base[key] = fr.xyz64 / max(fr.xyz64.max(), 1e-9) * 0.98 + 0.01
-        p = synth.advect(base[key], r["w"], 0.5, 0.0, 0.01, steps=1) if r["step"] else base[key]
-        base[key] = p
+            base[key] = (fr.xyz64, fr.scale)
+        p, sc = base[key]
+        if r["step"]:
+            p = synth.advect(p, r["w"], synth.SERVE_G, (r["step"] - 1) * synth.SERVE_DT, synth.SERVE_DT, steps=1,
+                             scale=sc)
+        base[key] = (p, sc)
         xyzs.append(np.ascontiguousarray(p.astype(np.float32)))
     srv = N.Server(0, slots=a.slots, budget_bytes=0)
     srv.result(srv.submit(xyzs[0], N.default_params(reqs[0]["radius"])))  # warm-up

@@ -5,18 +5,21 @@
 // (VisitorExtract::on_vert, src/visitorextract.cpp:229-256).  Those vertices
 // are exactly the corners of leaves that lie strictly inside the root box, so
 // here they are enumerated in parallel:
-//   1. every leaf emits its interior corners (integer lattice at D_max);
-//      sort + unique gives the dual vertices;
+//   1. every leaf marks its interior corners (integer lattice at D_max) in
+//      a Morton-indexed lattice bitmap (sort + unique above D_max = 10); the
+//      set bits in index order are the dual vertices, in Z order;
 //   2. per vertex, the leaf containing each of the 8 octants is found by
 //      descending from the root; sign code, table[256] -> canonical case;
 //   3. per non-trivial cell, the case triangles (src/visitorextract.cpp:95-199)
 //      name leaf pairs; mesh vertices are deduplicated by the sorted leaf-id
-//      pair, as Mesh::insert_vert keys them (src/global.cpp:13-32);
+//      pair, as Mesh::insert_vert keys them (src/global.cpp:13-32), the
+//      first (lowest) slot of a key winning, through a hash table in L2;
 //   4. one thread per mesh vertex bisects its leaf-to-leaf segment down to
 //      r/2 with a field evaluation per step and interpolates with the 0.1/0.9
 //      snap (calc_vertices, src/visitorextract.cpp:47-84);
 //   5. triangles are oriented by the table's flip and deduplicated by their
-//      sorted vertex triple (Mesh::insert_tri, src/global.cpp:34-53).
+//      sorted vertex triple, the first generated winning (Mesh::insert_tri,
+//      src/global.cpp:34-53).
 // The output order differs from the reference's traversal order; the mesh is
 // the same set of vertices (by leaf-id pair) and triangles.
 #include <algorithm>
@@ -94,6 +97,165 @@ __global__ void k_corner_keys(const int* __restrict__ leaves, long long nl, cons
     key = (1ull << (3 * B)) - 1ull;
   keys[t] = key;
   vals[t] = (uint32_t)t;
+}
+
+// Morton code of three coordinates of up to 10 bits each.
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+  v &= 0x3ffu;
+  v = (v | (v << 16)) & 0x030000ffu;
+  v = (v | (v << 8)) & 0x0300f00fu;
+  v = (v | (v << 4)) & 0x030c30c3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+__device__ __forceinline__ uint32_t compact3(uint32_t v) {
+  v &= 0x09249249u;
+  v = (v | (v >> 2)) & 0x030c30c3u;
+  v = (v | (v >> 4)) & 0x0300f00fu;
+  v = (v | (v >> 8)) & 0x030000ffu;
+  v = (v | (v >> 16)) & 0x3ffu;
+  return v;
+}
+
+// Interior leaf corners (coordinates 1 .. 2^D_max - 1) as bits of a lattice
+// bitmap indexed by the Morton code of (x - 1, y - 1, z - 1): 2^(3 D_max)
+// bits, 16 MB at D_max = 9.  The set bits in index order are the unique
+// corners in Z order, which keeps the later per-vertex work spatially
+// coherent (as the reference's recursive traversal is).
+__global__ void k_corner_mark(const int* __restrict__ leaves, long long nl, const int4* __restrict__ nd_org,
+                              int full, unsigned* __restrict__ bits) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nl * 8) return;
+  const int4 o = nd_org[leaves[t >> 3]];
+  const int k = (int)(t & 7);
+  const int x = o.x + ((k & 1) ? o.w : 0), y = o.y + ((k & 2) ? o.w : 0), z = o.z + ((k & 4) ? o.w : 0);
+  if (x <= 0 || x >= full || y <= 0 || y >= full || z <= 0 || z >= full) return;
+  const uint32_t idx = spread3((uint32_t)(x - 1)) | (spread3((uint32_t)(y - 1)) << 1) |
+                       (spread3((uint32_t)(z - 1)) << 2);
+  const unsigned bit = 1u << (idx & 31);
+  unsigned* w = bits + (idx >> 5);
+  if (!(__ldg(w) & bit)) atomicOr(w, bit);
+}
+
+__global__ void k_bitmap_count(const unsigned* __restrict__ bits, long long nw, int* __restrict__ cnt) {
+  long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w < nw) cnt[w] = __popc(bits[w]);
+  if (w == nw) cnt[w] = 0;
+}
+
+__global__ void k_bitmap_keys(const unsigned* __restrict__ bits, long long nw, const int* __restrict__ off, int B,
+                              uint64_t* __restrict__ out) {
+  long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nw) return;
+  unsigned b = bits[w];
+  int o = off[w];
+  while (b) {
+    const int i = __ffs(b) - 1;
+    b &= b - 1;
+    const uint32_t idx = ((uint32_t)w << 5) | (uint32_t)i;
+    const uint64_t x = compact3(idx) + 1, y = compact3(idx >> 1) + 1, z = compact3(idx >> 2) + 1;
+    out[o++] = (x << (2 * B)) | (y << B) | z;
+  }
+}
+
+__device__ __forceinline__ uint32_t mix64to32(uint64_t k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  k ^= k >> 33;
+  return (uint32_t)k;
+}
+
+// Deduplication by key with "first insertion wins" (Mesh::insert_vert /
+// insert_tri, src/global.cpp:13-53): an open-addressing table of slot + 1
+// per distinct key keeps the lowest slot (atomicMin), keys are compared
+// through the slots' own key arrays.  The table has more entries than
+// slots, so a probe always ends.
+__global__ void k_vkey_insert(long long ns, const uint64_t* __restrict__ khi, const uint64_t* __restrict__ klo,
+                              uint32_t mask, unsigned* __restrict__ tab, uint32_t* __restrict__ where) {
+  long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= ns) return;
+  const uint64_t lo = klo[s], hi = khi ? khi[s] : 0ull;
+  uint32_t h = mix64to32(lo ^ (hi * 0x9E3779B97F4A7C15ull)) & mask;
+  for (uint32_t t = 0; t <= mask; ++t) {
+    unsigned cur = tab[h];
+    if (cur == 0u) {
+      cur = atomicCAS(tab + h, 0u, (unsigned)s + 1u);
+      if (cur == 0u) break;
+    }
+    const long long o = (long long)cur - 1;
+    if (klo[o] == lo && (!khi || khi[o] == hi)) {
+      atomicMin(tab + h, (unsigned)s + 1u);
+      break;
+    }
+    h = (h + 1u) & mask;
+  }
+  where[s] = h;
+}
+
+// Triangles: the sorted vertex triple of the oriented triangle is the key.
+__device__ __forceinline__ void sorted3(const int* o, int& s0, int& s1, int& s2) {
+  const int a = o[0], b = o[1], c = o[2];
+  s0 = min(a, min(b, c));
+  s2 = max(a, max(b, c));
+  s1 = a + b + c - s0 - s2;
+}
+
+__global__ void k_tri_insert(long long nt, const int* __restrict__ otri, uint32_t mask, unsigned* __restrict__ tab,
+                             uint32_t* __restrict__ where) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  int s0, s1, s2;
+  sorted3(otri + 3 * t, s0, s1, s2);
+  uint32_t h = mix64to32(((uint64_t)(uint32_t)s0 << 42) ^ ((uint64_t)(uint32_t)s1 << 21) ^ (uint64_t)(uint32_t)s2 ^
+                         ((uint64_t)(uint32_t)s0 >> 22) * 0x9E3779B97F4A7C15ull) &
+               mask;
+  for (uint32_t i = 0; i <= mask; ++i) {
+    unsigned cur = tab[h];
+    if (cur == 0u) {
+      cur = atomicCAS(tab + h, 0u, (unsigned)t + 1u);
+      if (cur == 0u) break;
+    }
+    int o0, o1, o2;
+    sorted3(otri + 3 * ((long long)cur - 1), o0, o1, o2);
+    if (o0 == s0 && o1 == s1 && o2 == s2) {
+      atomicMin(tab + h, (unsigned)t + 1u);
+      break;
+    }
+    h = (h + 1u) & mask;
+  }
+  where[t] = h;
+}
+
+// flag[s] = 1 where slot s is its key's first (lowest) slot
+__global__ void k_first_flag(long long n, const unsigned* __restrict__ tab, const uint32_t* __restrict__ where,
+                             int* __restrict__ flag) {
+  long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n) flag[s] = tab[where[s]] == (unsigned)s + 1u ? 1 : 0;
+  if (s == n) flag[s] = 0;
+}
+
+// slot -> vertex (numbered in order of first slots); vertex -> its first slot
+__global__ void k_vertex_map(long long ns, const unsigned* __restrict__ tab, const uint32_t* __restrict__ where,
+                             const int* __restrict__ rank, int* __restrict__ slot_vertex, int* __restrict__ rep) {
+  long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= ns) return;
+  const long long first = (long long)tab[where[s]] - 1;
+  const int v = rank[first];
+  slot_vertex[s] = v;
+  if (first == s) rep[v] = (int)s;
+}
+
+__global__ void k_tri_write(long long nt, const int* __restrict__ rank, const int* __restrict__ otri,
+                            int* __restrict__ out) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  const int o = rank[t];
+  if (rank[t + 1] == o) return;
+  out[3 * o] = otri[3 * t];
+  out[3 * o + 1] = otri[3 * t + 1];
+  out[3 * o + 2] = otri[3 * t + 2];
 }
 
 __global__ void k_unique_flag(const uint64_t* __restrict__ keys, long long n, uint64_t invalid,
@@ -194,29 +356,6 @@ __global__ void k_tri_slots(long long nu, const int* __restrict__ cells, const i
   }
 }
 
-// group starts of a sorted (hi, lo) key sequence
-__global__ void k_group_flag(const uint64_t* __restrict__ hs, const uint64_t* __restrict__ ls, long long n,
-                             int* __restrict__ flag) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i > n) return;
-  if (i == n) {
-    flag[i] = 0;
-    return;
-  }
-  bool start = i == 0 || ls[i] != ls[i - 1] || (hs && hs[i] != hs[i - 1]);
-  flag[i] = start ? 1 : 0;
-}
-
-__global__ void k_vertex_map(const uint32_t* __restrict__ perm, const int* __restrict__ scan, long long n,
-                             int* __restrict__ slot_vertex, int* __restrict__ rep) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int start = scan[i + 1] - scan[i];
-  const int vid = scan[i] + start - 1;
-  slot_vertex[perm[i]] = vid;
-  if (start) rep[vid] = (int)perm[i];
-}
-
 struct BisectArgs {
   GridView g;
   PartView P;
@@ -271,98 +410,21 @@ __global__ void k_bisect(BisectArgs a, long long nv, const int* __restrict__ rep
   stripe_add(counters, 4, (unsigned long long)pairs);
 }
 
-// Oriented triangle (Mesh::insert_tri argument order) and its sorted-triple key.
-__global__ void k_tri_keys(long long nt, const int* __restrict__ slot_vertex, const int8_t* __restrict__ tflip,
-                           int vbits, int packed, int* __restrict__ otri, uint64_t* __restrict__ khi,
-                           uint64_t* __restrict__ klo) {
+// Oriented triangle in Mesh::insert_tri argument order.
+__global__ void k_tri_orient(long long nt, const int* __restrict__ slot_vertex, const int8_t* __restrict__ tflip,
+                             int* __restrict__ otri) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nt) return;
-  int a = slot_vertex[3 * t], b = slot_vertex[3 * t + 1], c = slot_vertex[3 * t + 2];
-  int o0 = a, o1 = b, o2 = c;
-  if (!tflip[t]) {
-    o0 = c;
-    o2 = a;
-  }
-  otri[3 * t] = o0;
-  otri[3 * t + 1] = o1;
-  otri[3 * t + 2] = o2;
-  int s0 = min(a, min(b, c)), s2 = max(a, max(b, c));
-  int s1 = a + b + c - s0 - s2;
-  if (packed) {
-    klo[t] = ((uint64_t)s0 << (2 * vbits)) | ((uint64_t)s1 << vbits) | (uint64_t)s2;
-  } else {
-    khi[t] = (uint64_t)s0;
-    klo[t] = ((uint64_t)s1 << 32) | (uint64_t)s2;
-  }
+  const int a = slot_vertex[3 * t], b = slot_vertex[3 * t + 1], c = slot_vertex[3 * t + 2];
+  otri[3 * t] = tflip[t] ? a : c;
+  otri[3 * t + 1] = b;
+  otri[3 * t + 2] = tflip[t] ? c : a;
 }
 
-__global__ void k_tri_write(const uint32_t* __restrict__ perm, const int* __restrict__ scan, long long n,
-                            const int* __restrict__ otri, int* __restrict__ out) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if (scan[i + 1] - scan[i]) {
-    const int t = (int)perm[i];
-    const int o = scan[i];
-    out[3 * o] = otri[3 * t];
-    out[3 * o + 1] = otri[3 * t + 1];
-    out[3 * o + 2] = otri[3 * t + 2];
-  }
-}
-
-__global__ void k_gather_u64(const uint64_t* __restrict__ src, const uint32_t* __restrict__ perm, long long n,
-                             uint64_t* __restrict__ dst) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) dst[i] = src[perm[i]];
-}
-
-__global__ void k_pack2(const uint64_t* __restrict__ hi, const uint64_t* __restrict__ lo, long long n,
-                        int lo_bits, uint64_t* __restrict__ out) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = (hi[i] << lo_bits) | lo[i];
-}
-
-static int bits_of(unsigned long long v) {
-  int b = 0;
-  while (b < 64 && (b == 64 ? false : (1ull << b) <= v)) ++b;
-  return b < 1 ? 1 : b;
-}
-
-// Stable sort of n keys given as (hi, lo) words (hi may be null); on return
-// perm holds the source index of each sorted position and hs/ls the sorted
-// words (hs unused when hi is null).
-static void sort_keys(pi_frame* f, const uint64_t* hi, const uint64_t* lo, long long n, int hi_bits, int lo_bits,
-                      DBuf<uint32_t>& perm, DBuf<uint64_t>& hs, DBuf<uint64_t>& ls) {
-  pi_ctx* c = f->ctx;
-  cudaStream_t s = c->stream;
-  DBuf<uint64_t> k1, k2;
-  DBuf<uint32_t> v1, v2;
-  k1.alloc(c, s, n);
-  k2.alloc(c, s, n);
-  v1.alloc(c, s, n);
-  v2.alloc(c, s, n);
-  DBuf<int> tmp;
-  tmp.alloc(c, s, radix_tmp_ints(n));
-  iota_u32(v1.p, n, s);
-  uint64_t *kp = k1.p, *ka = k2.p;
-  uint32_t *vp = v1.p, *va = v2.p;
-  if (!hi) {
-    PI_CUDA(cudaMemcpyAsync(k1.p, lo, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, s));
-    radix_sort_u64(&kp, &vp, &ka, &va, n, lo_bits, tmp.p, s);
-  } else {
-    PI_CUDA(cudaMemcpyAsync(k1.p, lo, sizeof(uint64_t) * n, cudaMemcpyDeviceToDevice, s));
-    radix_sort_u64(&kp, &vp, &ka, &va, n, lo_bits, tmp.p, s);
-    PI_LAUNCH(k_gather_u64, div_up(n, 256), 256, 0, s, hi, vp, n, ka);
-    std::swap(kp, ka);
-    radix_sort_u64(&kp, &vp, &ka, &va, n, hi_bits, tmp.p, s);
-  }
-  perm.alloc(c, s, n);
-  PI_CUDA(cudaMemcpyAsync(perm.p, vp, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s));
-  ls.alloc(c, s, n);
-  PI_LAUNCH(k_gather_u64, div_up(n, 256), 256, 0, s, lo, perm.p, n, ls.p);
-  if (hi) {
-    hs.alloc(c, s, n);
-    PI_LAUNCH(k_gather_u64, div_up(n, 256), 256, 0, s, hi, perm.p, n, hs.p);
-  }
+static uint32_t table_mask(long long n) {
+  uint32_t m = 1;
+  while ((long long)m < n + 1) m <<= 1;
+  return m - 1;
 }
 
 static int read_int(pi_frame* f, const int* d) {
@@ -390,16 +452,32 @@ void stage_extract(pi_frame* f) {
   // 2. dual vertices = unique interior leaf corners
   const int B = f->dmax + 1;
   const int full = 1 << f->dmax;
-  const uint64_t invalid = (1ull << (3 * B)) - 1ull;
   const long long nk = nl * 8;
-  DBuf<uint64_t> keys, keys2, uverts;
-  DBuf<uint32_t> vals, vals2;
-  keys.alloc(c, s, nk);
-  keys2.alloc(c, s, nk);
-  vals.alloc(c, s, nk);
-  vals2.alloc(c, s, nk);
-  PI_LAUNCH(k_corner_keys, div_up(nk, 256), 256, 0, s, leaves.p, nl, f->nd_org.p, full, B, keys.p, vals.p);
-  {
+  DBuf<uint64_t> uverts;
+  long long nu = 0;
+  if (f->dmax <= 10) {
+    const long long nw = div_up(1LL << (3 * f->dmax), 32);
+    DBuf<unsigned> bits;
+    DBuf<int> cnt;
+    bits.alloc(c, s, nw);
+    cnt.alloc(c, s, nw + 1);
+    if (tmp.n < scan_tmp_ints(nw + 1)) tmp.alloc(c, s, scan_tmp_ints(nw + 1));
+    PI_CUDA(cudaMemsetAsync(bits.p, 0, sizeof(unsigned) * nw, s));
+    PI_LAUNCH(k_corner_mark, div_up(nk, 256), 256, 0, s, leaves.p, nl, f->nd_org.p, full, bits.p);
+    PI_LAUNCH(k_bitmap_count, div_up(nw + 1, 256), 256, 0, s, bits.p, nw, cnt.p);
+    exclusive_scan_i32(cnt.p, cnt.p, nw + 1, nullptr, tmp.p, s);
+    nu = read_int(f, cnt.p + nw);
+    uverts.alloc(c, s, nu > 0 ? nu : 1);
+    PI_LAUNCH(k_bitmap_keys, div_up(nw, 256), 256, 0, s, bits.p, nw, cnt.p, B, uverts.p);
+  } else {
+    const uint64_t invalid = (1ull << (3 * B)) - 1ull;
+    DBuf<uint64_t> keys, keys2;
+    DBuf<uint32_t> vals, vals2;
+    keys.alloc(c, s, nk);
+    keys2.alloc(c, s, nk);
+    vals.alloc(c, s, nk);
+    vals2.alloc(c, s, nk);
+    PI_LAUNCH(k_corner_keys, div_up(nk, 256), 256, 0, s, leaves.p, nl, f->nd_org.p, full, B, keys.p, vals.p);
     DBuf<int> rtmp;
     rtmp.alloc(c, s, radix_tmp_ints(nk));
     uint64_t *kp = keys.p, *ka = keys2.p;
@@ -409,91 +487,95 @@ void stage_extract(pi_frame* f) {
     uf.alloc(c, s, nk + 1);
     PI_LAUNCH(k_unique_flag, div_up(nk + 1, 256), 256, 0, s, kp, nk, invalid, uf.p);
     exclusive_scan_i32(uf.p, uf.p, nk + 1, nullptr, tmp.p, s);
-    const long long nu = read_int(f, uf.p + nk);
+    nu = read_int(f, uf.p + nk);
     uverts.alloc(c, s, nu > 0 ? nu : 1);
     PI_LAUNCH(k_unique_write, div_up(nk, 256), 256, 0, s, kp, uf.p, nk, invalid, uverts.p);
-    keys.release();
-    keys2.release();
-    vals.release();
-    vals2.release();
-    // 3. dual cells
-    DBuf<int> cells, procs, toff;
-    cells.alloc(c, s, nu * 8 > 0 ? nu * 8 : 1);
-    procs.alloc(c, s, nu > 0 ? nu : 1);
-    toff.alloc(c, s, nu + 1);
-    counters_reset(f);
-    PI_LAUNCH(k_dual, div_up(nu + 1, 128), 128, 0, s, uverts.p, nu, B, f->nd_child.p, f->nd_org.p, f->nd_v.p,
-              cells.p, procs.p, toff.p, f->dcount.p);
-    exclusive_scan_i32(toff.p, toff.p, nu + 1, nullptr, tmp.p, s);
-    const long long nt0 = read_int(f, toff.p + nu);
-    // 4. triangle slots and vertex keys
-    const int id_bits = 3 * f->dmax;
-    const int packed = (2 * id_bits <= 64) ? 1 : 0;
-    const long long ns = 3 * nt0;
-    DBuf<int> slotA, slotB;
-    DBuf<uint64_t> khi, klo;
-    DBuf<int8_t> tflip;
-    slotA.alloc(c, s, ns > 0 ? ns : 1);
-    slotB.alloc(c, s, ns > 0 ? ns : 1);
-    klo.alloc(c, s, ns > 0 ? ns : 1);
-    if (!packed) khi.alloc(c, s, ns > 0 ? ns : 1);
-    tflip.alloc(c, s, nt0 > 0 ? nt0 : 1);
-    PI_LAUNCH(k_tri_slots, div_up(nu, 128), 128, 0, s, nu, cells.p, procs.p, toff.p, f->nd_id.p, id_bits, packed,
-              slotA.p, slotB.p, khi.p, klo.p, tflip.p);
-    cells.release();
-    procs.release();
-    toff.release();
-    uverts.release();
-    // 5. unique mesh vertices
-    DBuf<uint32_t> perm;
-    DBuf<uint64_t> hs, ls;
-    sort_keys(f, packed ? nullptr : khi.p, klo.p, ns, id_bits, packed ? 2 * id_bits : id_bits, perm, hs, ls);
-    DBuf<int> vf, slot_vertex, rep;
-    vf.alloc(c, s, ns + 1);
-    if (tmp.n < scan_tmp_ints(ns + 1)) tmp.alloc(c, s, scan_tmp_ints(ns + 1));
-    PI_LAUNCH(k_group_flag, div_up(ns + 1, 256), 256, 0, s, packed ? nullptr : hs.p, ls.p, ns, vf.p);
-    exclusive_scan_i32(vf.p, vf.p, ns + 1, nullptr, tmp.p, s);
-    const long long nv = read_int(f, vf.p + ns);
-    slot_vertex.alloc(c, s, ns > 0 ? ns : 1);
-    rep.alloc(c, s, nv > 0 ? nv : 1);
-    PI_LAUNCH(k_vertex_map, div_up(ns, 256), 256, 0, s, perm.p, vf.p, ns, slot_vertex.p, rep.p);
-    // 6. vertex positions by bisection
-    f->nV = nv;
-    f->mv.alloc(c, s, nv * 3 > 0 ? nv * 3 : 3);
-    f->mk.alloc(c, s, nv * 2 > 0 ? nv * 2 : 2);
-    const GridHost& gh = f->g;
-    BisectArgs ba{GridView{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p},
-                  PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p}, f->iso, f->P.radius / 2};
-    PI_LAUNCH(k_bisect, div_up(nv, 128), 128, 0, s, ba, nv, rep.p, slotA.p, slotB.p, f->nd_v.p, f->nd_id.p, f->mv.p,
-              f->mk.p, f->dcount.p);
-    // 7. triangles
-    const int vbits = bits_of((unsigned long long)(nv > 0 ? nv : 1));
-    const int tpacked = (3 * vbits <= 64) ? 1 : 0;
-    DBuf<int> otri;
-    DBuf<uint64_t> thi, tlo;
-    otri.alloc(c, s, nt0 * 3 > 0 ? nt0 * 3 : 3);
-    tlo.alloc(c, s, nt0 > 0 ? nt0 : 1);
-    if (!tpacked) thi.alloc(c, s, nt0 > 0 ? nt0 : 1);
-    PI_LAUNCH(k_tri_keys, div_up(nt0, 256), 256, 0, s, nt0, slot_vertex.p, tflip.p, vbits, tpacked, otri.p, thi.p,
-              tlo.p);
-    DBuf<uint32_t> tperm;
-    DBuf<uint64_t> ths, tls;
-    sort_keys(f, tpacked ? nullptr : thi.p, tlo.p, nt0, vbits, tpacked ? 3 * vbits : 64, tperm, ths, tls);
-    DBuf<int> tf;
-    tf.alloc(c, s, nt0 + 1);
-    PI_LAUNCH(k_group_flag, div_up(nt0 + 1, 256), 256, 0, s, tpacked ? nullptr : ths.p, tls.p, nt0, tf.p);
-    exclusive_scan_i32(tf.p, tf.p, nt0 + 1, nullptr, tmp.p, s);
-    const long long nt = read_int(f, tf.p + nt0);
-    f->nT = nt;
-    f->mt.alloc(c, s, nt * 3 > 0 ? nt * 3 : 3);
-    PI_LAUNCH(k_tri_write, div_up(nt0, 256), 256, 0, s, tperm.p, tf.p, nt0, otri.p, f->mt.p);
-    unsigned long long bc[8];
-    counters_read(f, bc);
-    f->nDual = (long long)bc[2];
-    f->bisectEvals = (long long)bc[3];
-    f->fieldEvals += (long long)bc[3];
-    f->pairs += (long long)bc[4];
   }
+  // 3. dual cells
+  DBuf<int> cells, procs, toff;
+  cells.alloc(c, s, nu * 8 > 0 ? nu * 8 : 1);
+  procs.alloc(c, s, nu > 0 ? nu : 1);
+  toff.alloc(c, s, nu + 1);
+  if (tmp.n < scan_tmp_ints(nu + 1)) tmp.alloc(c, s, scan_tmp_ints(nu + 1));
+  counters_reset(f);
+  PI_LAUNCH(k_dual, div_up(nu + 1, 128), 128, 0, s, uverts.p, nu, B, f->nd_child.p, f->nd_org.p, f->nd_v.p,
+            cells.p, procs.p, toff.p, f->dcount.p);
+  exclusive_scan_i32(toff.p, toff.p, nu + 1, nullptr, tmp.p, s);
+  const long long nt0 = read_int(f, toff.p + nu);
+  // 4. triangle slots and vertex keys (sorted leaf-id pairs)
+  const int id_bits = 3 * f->dmax;
+  const int packed = (2 * id_bits <= 64) ? 1 : 0;
+  const long long ns = 3 * nt0;
+  DBuf<int> slotA, slotB;
+  DBuf<uint64_t> khi, klo;
+  DBuf<int8_t> tflip;
+  slotA.alloc(c, s, ns > 0 ? ns : 1);
+  slotB.alloc(c, s, ns > 0 ? ns : 1);
+  klo.alloc(c, s, ns > 0 ? ns : 1);
+  if (!packed) khi.alloc(c, s, ns > 0 ? ns : 1);
+  tflip.alloc(c, s, nt0 > 0 ? nt0 : 1);
+  PI_LAUNCH(k_tri_slots, div_up(nu, 128), 128, 0, s, nu, cells.p, procs.p, toff.p, f->nd_id.p, id_bits, packed,
+            slotA.p, slotB.p, khi.p, klo.p, tflip.p);
+  cells.release();
+  procs.release();
+  toff.release();
+  uverts.release();
+  // 5. unique mesh vertices: first slot of each key, numbered in slot order
+  DBuf<unsigned> vtab;
+  DBuf<uint32_t> vwhere;
+  DBuf<int> vrank, slot_vertex, rep;
+  const uint32_t vmask = table_mask(ns);
+  vtab.alloc(c, s, (size_t)vmask + 1);
+  vwhere.alloc(c, s, ns > 0 ? ns : 1);
+  vrank.alloc(c, s, ns + 1);
+  if (tmp.n < scan_tmp_ints(ns + 1)) tmp.alloc(c, s, scan_tmp_ints(ns + 1));
+  PI_CUDA(cudaMemsetAsync(vtab.p, 0, sizeof(unsigned) * ((size_t)vmask + 1), s));
+  PI_LAUNCH(k_vkey_insert, div_up(ns, 256), 256, 0, s, ns, packed ? nullptr : khi.p, klo.p, vmask, vtab.p,
+            vwhere.p);
+  PI_LAUNCH(k_first_flag, div_up(ns + 1, 256), 256, 0, s, ns, vtab.p, vwhere.p, vrank.p);
+  exclusive_scan_i32(vrank.p, vrank.p, ns + 1, nullptr, tmp.p, s);
+  const long long nv = read_int(f, vrank.p + ns);
+  slot_vertex.alloc(c, s, ns > 0 ? ns : 1);
+  rep.alloc(c, s, nv > 0 ? nv : 1);
+  PI_LAUNCH(k_vertex_map, div_up(ns, 256), 256, 0, s, ns, vtab.p, vwhere.p, vrank.p, slot_vertex.p, rep.p);
+  vtab.release();
+  vwhere.release();
+  vrank.release();
+  khi.release();
+  klo.release();
+  // 6. vertex positions by bisection
+  f->nV = nv;
+  f->mv.alloc(c, s, nv * 3 > 0 ? nv * 3 : 3);
+  f->mk.alloc(c, s, nv * 2 > 0 ? nv * 2 : 2);
+  const GridHost& gh = f->g;
+  BisectArgs ba{GridView{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p},
+                PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p}, f->iso, f->P.radius / 2};
+  PI_LAUNCH(k_bisect, div_up(nv, 128), 128, 0, s, ba, nv, rep.p, slotA.p, slotB.p, f->nd_v.p, f->nd_id.p, f->mv.p,
+            f->mk.p, f->dcount.p);
+  // 7. triangles: first of each sorted vertex triple, in generation order
+  DBuf<int> otri, trank;
+  DBuf<unsigned> ttab;
+  DBuf<uint32_t> twhere;
+  otri.alloc(c, s, nt0 * 3 > 0 ? nt0 * 3 : 3);
+  PI_LAUNCH(k_tri_orient, div_up(nt0, 256), 256, 0, s, nt0, slot_vertex.p, tflip.p, otri.p);
+  const uint32_t tmask = table_mask(nt0);
+  ttab.alloc(c, s, (size_t)tmask + 1);
+  twhere.alloc(c, s, nt0 > 0 ? nt0 : 1);
+  trank.alloc(c, s, nt0 + 1);
+  PI_CUDA(cudaMemsetAsync(ttab.p, 0, sizeof(unsigned) * ((size_t)tmask + 1), s));
+  PI_LAUNCH(k_tri_insert, div_up(nt0, 256), 256, 0, s, nt0, otri.p, tmask, ttab.p, twhere.p);
+  PI_LAUNCH(k_first_flag, div_up(nt0 + 1, 256), 256, 0, s, nt0, ttab.p, twhere.p, trank.p);
+  exclusive_scan_i32(trank.p, trank.p, nt0 + 1, nullptr, tmp.p, s);
+  const long long nt = read_int(f, trank.p + nt0);
+  f->nT = nt;
+  f->mt.alloc(c, s, nt * 3 > 0 ? nt * 3 : 3);
+  PI_LAUNCH(k_tri_write, div_up(nt0, 256), 256, 0, s, nt0, trank.p, otri.p, f->mt.p);
+  unsigned long long bc[8];
+  counters_read(f, bc);
+  f->nDual = (long long)bc[2];
+  f->bisectEvals = (long long)bc[3];
+  f->fieldEvals += (long long)bc[3];
+  f->pairs += (long long)bc[4];
 }
 
 }  // namespace pisurf

@@ -275,15 +275,23 @@ def sheets_and_filaments(n=500_000, radius=0.01, seed=4) -> Frame:
     return Frame(pts, radius, scale, seed, "sheets_filaments_%d" % n)
 
 
-def advect(xyz, w, g, t, dt, steps=1):
-    """Swirl plus gravity u = (-w (y - 0.5), w (x - 0.5), -g t), clamped to the
-    unit box (serving workload sequences)."""
-    p = xyz.copy()
+def advect(xyz, w, g, t, dt, steps=1, scale=1.0):
+    """Swirl plus gravity u = (-w (y - 0.5), w (x - 0.5), -g t) in the unit box
+    scaled by `scale` (the geometry rule scales the domain with the particle
+    count), integrated `steps` explicit steps from time t and clamped to the
+    box (serving workload sequences)."""
+    p = xyz / scale
     for k in range(steps):
         tt = t + k * dt
         u = np.stack([-w * (p[:, 1] - 0.5), w * (p[:, 0] - 0.5), np.full(len(p), -g * tt)], -1)
         p = np.clip(p + dt * u, 0.0, 1.0)
-    return p
+    return p * scale
+
+
+SERVE_G = 0.5     # gravity of the serving sequences (box units / time^2)
+SERVE_DT = 0.002  # time step between frames of a sequence: 200 steps move
+                  # particles by a few percent of the box instead of
+                  # collapsing them onto the floor
 
 
 def serving_requests(count=2000, seed=500, n_min=10_000, n_max=4_000_000, rate_hz=20.0):
@@ -310,13 +318,13 @@ def serving_requests(count=2000, seed=500, n_min=10_000, n_max=4_000_000, rate_h
     return out
 
 
-def serving_frame(req, g=0.5, dt=0.01) -> Frame:
+def serving_frame(req, g=SERVE_G, dt=SERVE_DT) -> Frame:
     """Materialise one serving request: the sequence's base frame (a seeded
-    mixed frame scaled into the unit box) advected `step` times."""
+    mixed frame at spacing 2r in its scaled unit box) advected `step` steps."""
     fr = mixed_frame(req["seed"], req["n"], req["radius"])
-    p = fr.xyz64 / max(fr.xyz64.max(), 1e-9) * 0.98 + 0.01
+    p = fr.xyz64
     if req["step"]:
-        p = advect(p, req["w"], g, 0.0, dt, steps=req["step"])
+        p = advect(p, req["w"], g, 0.0, dt, steps=req["step"], scale=fr.scale)
     return Frame(p, req["radius"], fr.scale, req["seed"], "serve_%d_%d" % (req["seq"], req["step"]))
 
 
