@@ -110,22 +110,27 @@ __global__ void k_empty(LevelArgs a, const float4* __restrict__ nd_c, float4* __
   const int lane = threadIdx.x & 31;
   if (node >= a.le) return;
   const GrownBox b = grown_box(a.g, nd_c[node], a.expand);
-  // rows of the cell block, 32 particles at a time; stop at the first hit
+  // the block's rows (z, y) are spread over the lanes; each lane stops at the
+  // first particle inside, the warp at the first batch of rows with a hit
   bool found = false;
-  if (b.x0 <= b.x1) {
-    for (int z = b.z0; z <= b.z1 && !found; ++z)
-      for (int y = b.y0; y <= b.y1 && !found; ++y) {
+  if (b.x0 <= b.x1 && b.y0 <= b.y1 && b.z0 <= b.z1) {
+    const int nyb = b.y1 - b.y0 + 1;
+    const int rows = (b.z1 - b.z0 + 1) * nyb;
+    for (int r0 = 0; r0 < rows && !found; r0 += 32) {
+      const int r = r0 + lane;
+      bool hit = false;
+      if (r < rows) {
+        const int z = b.z0 + r / nyb, y = b.y0 + r % nyb;
         const long long base = ((long long)z * a.g.ny + y) * a.g.nx;
         const int s = __ldg(a.g.off + base + b.x0), e = __ldg(a.g.off + base + b.x1 + 1);
-        for (int j0 = s; j0 < e; j0 += 32) {
-          const int j = j0 + lane;
-          const bool in = j < e && inside(b, __ldg(a.pos + j));
-          if (__any_sync(0xffffffffu, in)) {
-            found = true;
+        for (int j = s; j < e; ++j)
+          if (inside(b, __ldg(a.pos + j))) {
+            hit = true;
             break;
           }
-        }
       }
+      found = __any_sync(0xffffffffu, hit);
+    }
   }
   if (lane == 0) {
     if (!found) {
@@ -161,6 +166,7 @@ struct QArgs {
   float iso;
   long long lb, le;
   int ekx, eky;  // extended key strides (nx + 4, ny + 4)
+  int octants;   // 1: buckets are cell octants, 0: whole cells
 };
 
 // Hash cell of a point as a key over the grid grown by 2 cells on each side
@@ -188,7 +194,7 @@ __global__ void k_q_count(QArgs a, const float4* __restrict__ nd_c, const float4
     const float fx = __fdiv_rn(__fsub_rn(qx, a.g.b0), a.g.cell) - (float)cx;
     const float fy = __fdiv_rn(__fsub_rn(qy, a.g.b2), a.g.cell) - (float)cy;
     const float fz = __fdiv_rn(__fsub_rn(qz, a.g.b4), a.g.cell) - (float)cz;
-    const int oct = (fx >= 0.5f ? 1 : 0) | (fy >= 0.5f ? 2 : 0) | (fz >= 0.5f ? 4 : 0);
+    const int oct = a.octants ? ((fx >= 0.5f ? 1 : 0) | (fy >= 0.5f ? 2 : 0) | (fz >= 0.5f ? 4 : 0)) : 0;
     k = ext_key(a, cx, cy, cz) * 8 + oct;
   }
   const unsigned peers = __match_any_sync(0xffffffffu, k);
@@ -583,7 +589,7 @@ __global__ void k_spawn(long long lb, long long le, long long cbase, const int* 
 // tested against the children's float bounds exactly as the child itself
 // would compute them (checkEmptyAndCalcCurv, src/surface_reconstructor.cpp:
 // 152-222).  One warp per parent; lane k writes child k.
-__global__ void k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict__ rank, int child_depth,
+__global__ void k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict__ rank, int child_depth, int curv,
                              float4* __restrict__ nd_c, float4* __restrict__ nd_v, uint64_t* __restrict__ nd_id,
                              int* __restrict__ nd_parent, int* __restrict__ nd_child, int8_t* nd_type,
                              int8_t* __restrict__ nd_depth, int8_t* __restrict__ nd_sc, float* __restrict__ nd_curv,
@@ -625,8 +631,14 @@ __global__ void k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict
 #pragma unroll
   for (int k = 0; k < 8; ++k) sum[k][0] = sum[k][1] = sum[k][2] = sum[k][3] = 0.f;
   if (pb.x0 <= pb.x1) {
-    for (int z = pb.z0; z <= pb.z1; ++z)
+    bool all8 = false;
+    for (int z = pb.z0; z <= pb.z1 && !all8; ++z)
       for (int y = pb.y0; y <= pb.y1; ++y) {
+        // emptiness only: stop once all eight children hold a particle
+        if (!curv && __reduce_or_sync(0xffffffffu, found) == 0xffu) {
+          all8 = true;
+          break;
+        }
         const long long base = ((long long)z * a.g.ny + y) * a.g.nx;
         const int s = __ldg(a.g.off + base + pb.x0), en = __ldg(a.g.off + base + pb.x1 + 1);
         for (int j = s + lane; j < en; j += 32) {
@@ -640,6 +652,7 @@ __global__ void k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict
             for (int k = 0; k < 8; ++k)
               if (((mx >> (k & 1)) & 1) && ((my >> ((k >> 1) & 1)) & 1) && ((mz >> ((k >> 2) & 1)) & 1)) m8 |= 1u << k;
             found |= m8;
+            if (!curv) continue;
             const float4 nv = __ldg(a.nrm + j);
 #pragma unroll
             for (int k = 0; k < 8; ++k)
@@ -677,7 +690,9 @@ __global__ void k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict
     nd_type[b + k] = nonempty ? T_UNCERTAIN : T_EMPTY;
     nd_depth[b + k] = (int8_t)child_depth;
     nd_sc[b + k] = 0;
-    nd_curv[b + k] = (mine[3] == 0.f) ? 1.0f : sqrtf(mine[0] * mine[0] + mine[1] * mine[1] + mine[2] * mine[2]) / mine[3];
+    nd_curv[b + k] = !curv ? -1.0f
+                     : (mine[3] == 0.f) ? 1.0f
+                                        : sqrtf(mine[0] * mine[0] + mine[1] * mine[1] + mine[2] * mine[2]) / mine[3];
     nd_org[b + k] = make_int4(po.x + ((k & 1) ? hs : 0), po.y + ((k & 2) ? hs : 0), po.z + ((k & 4) ? hs : 0), hs);
   }
 }
@@ -775,12 +790,13 @@ void stage_octree(pi_frame* f) {
       PI_CUDA(cudaMemsetAsync(qcnt.p, 0, sizeof(int) * (ek + 2), s));
       PI_CUDA(cudaMemsetAsync(ucnt.p, 0, sizeof(int) * ek, s));
       PI_CUDA(cudaMemsetAsync(hslot.p, 0, sizeof(unsigned) * 2 * qn, s));
-      QArgs qa{g, P, f->iso, lb, le, ekx, eky};
+      // the leaf level (node size r, samples r/2 apart) holds about 50
+      // distinct samples per cell octant, the level above about 50 per cell;
+      // coarser levels hold a few per cell
+      const int dense = depth >= f->dmax - 1 ? 1 : 0;
+      QArgs qa{g, P, f->iso, lb, le, ekx, eky, depth == f->dmax ? 1 : 0};
       PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
       exclusive_scan_i32(qcnt.p, qcnt.p, ek + 1, nullptr, f->tmp.p, s);
-      // the deepest level (node size r, samples r/2 apart) holds tens of
-      // distinct samples per bucket; coarser levels hold a few
-      const int dense = depth == f->dmax ? 1 : 0;
       PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
                 ucnt.p, rep.p, order.p, chunks.p, qcnt.p + ek + 1, dense);
       prof_begin(ctx, s);
@@ -808,7 +824,12 @@ void stage_octree(pi_frame* f) {
     ensure_nodes(f, le + newn);
     known = nint > 0 && depth + 1 >= f->dmin && depth < f->dmax;
     if (known) {
-      PI_LAUNCH(k_spawn_scan, div_up(nl, wpb), 32 * wpb, 0, s, la, le, flag.p, depth + 1, f->nd_c.p, f->nd_v.p,
+      // leaves by size never read their curvature (afterSampleEval returns
+      // before the curvature test), so their parents only settle emptiness
+      const float cell_child = 2.0f * std::ldexp(f->rootH, -(depth + 1));
+      const int child_curv = (double)(cell_child - f->P.radius) < 1e-8 ? 0 : 1;
+      PI_LAUNCH(k_spawn_scan, div_up(nl, wpb), 32 * wpb, 0, s, la, le, flag.p, depth + 1, child_curv, f->nd_c.p,
+                f->nd_v.p,
                 f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p, f->nd_curv.p,
                 f->nd_org.p);
     } else {
