@@ -59,6 +59,7 @@ def parse():
     p.add_argument("--n", type=int, default=1_000_000)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-evals", type=int, default=200_000)
+    p.add_argument("--qef", action="store_true", help="with --single: per-leaf QEF vertices on")
     p.add_argument("--single", action="store_true",
                    help="reconstruct one frame once and print its counters (for profiler captures)")
     p.add_argument("--workload", choices=["dam_break_1m", "batch64", "serving", "stress"], default="dam_break_1m",
@@ -217,10 +218,12 @@ def single(a):
     B.build()
     fr = make_frame(a.n)
     ctx = N.Context(0)
-    f = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz).run()
+    p = N.default_params(fr.radius)
+    p.qef = 1 if a.qef else 0
+    f = N.Frame(ctx, p).upload(fr.xyz).run()
     info = f.info()
     print(json.dumps({k: info[k] for k in ("num_nodes", "num_vertices", "num_triangles", "field_evals",
-                                           "candidate_pairs", "stage_ms")}))
+                                           "candidate_pairs", "stage_ms", "qef_accepted")}))
     f.close()
     ctx.close()
 

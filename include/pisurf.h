@@ -68,9 +68,10 @@ typedef struct pi_frame_info {
   float stage_ms[8];        /* device time of upload, hash, aniso, normals, octree, qef,
                                extract, download */
   int64_t qef_accepted;     /* leaves whose QEF vertex lies in the cell (qef mode) */
-  int64_t qef_singular;     /* leaves whose normal matrix is singular and whose
-                               pseudo-inverse point lies in the cell; rejected, as
-                               the reference's non-finite inverse is */
+  int64_t qef_singular;     /* leaves whose equilibrated normal matrix is singular
+                               (an eigenvalue below 1e-12 of the largest); their
+                               vertex is rejected, as the reference's non-finite
+                               inverse is */
 } pi_frame_info;
 
 /* Parity dumps (pi_stage_dump).  Arrays are in original particle order unless

@@ -8,12 +8,13 @@
 //   leaf by criteria:  node = QEF vertex if it lies in the cell, value
 //                      f(node) (the later SingleEval undoes the zeroing).
 // Gradients are the finite differences of GridEval (src/evaluator.cpp:293-359)
-// over the 27 samples.  Accumulation and solve are FP64; the solve is a
-// pseudo-inverse through a Jacobi eigen-decomposition of the symmetric 4x4
-// normal matrix.  Where that matrix is singular the reference's
-// Matrix4f::inverse yields non-finite values and the vertex is rejected; the
-// pseudo-inverse gives a finite point, which is still rejected here, and the
-// number of such nodes is counted.
+// over the 27 samples.  Accumulation and solve are FP64; the solve follows
+// the pseudo-inverse rule of a Jacobi eigen-decomposition of the equilibrated
+// symmetric 4x4 normal matrix (eigenvalues below 1e-12 of the largest are
+// dropped), decided by LDL^T bounds where they settle it.  Where that matrix
+// is singular the reference's Matrix4f::inverse yields non-finite values and
+// the vertex is rejected; so is it here, and the number of singular leaves is
+// counted.
 #include "device.cuh"
 #include "internal.h"
 
@@ -68,6 +69,41 @@ struct QefArgs {
   long long lb, le;
 };
 
+// LDL^T factorisation of the symmetric 4x4 A (no pivoting) and, when every
+// pivot is at least `floor`, the inverse A^-1 = L^-T diag(1/d) L^-1.
+// Returns 0 if a pivot is below `floor`, 1 otherwise.
+__device__ int ldlt_inverse4(const double A[4][4], double floor, double Ai[4][4]) {
+  double L[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+  double d[4], id[4];
+  for (int j = 0; j < 4; ++j) {
+    double dj = A[j][j];
+    for (int k = 0; k < j; ++k) dj -= L[j][k] * L[j][k] * d[k];
+    if (!(dj >= floor)) return 0;
+    d[j] = dj;
+    id[j] = 1.0 / dj;
+    for (int i = j + 1; i < 4; ++i) {
+      double l = A[i][j];
+      for (int k = 0; k < j; ++k) l -= L[i][k] * L[j][k] * d[k];
+      L[i][j] = l * id[j];
+    }
+  }
+  // M = L^-1 (unit lower triangular)
+  double M[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+  for (int i = 1; i < 4; ++i)
+    for (int j = 0; j < i; ++j) {
+      double v = -L[i][j];
+      for (int k = j + 1; k < i; ++k) v -= L[i][k] * M[k][j];
+      M[i][j] = v;
+    }
+  for (int r = 0; r < 4; ++r)
+    for (int c = r; c < 4; ++c) {
+      double v = 0.0;
+      for (int k = c; k < 4; ++k) v += M[k][r] * id[k] * M[k][c];
+      Ai[r][c] = Ai[c][r] = v;
+    }
+  return 1;
+}
+
 // counters: 5 QEF vertices accepted, 6 singular systems, 7 field evaluations
 __global__ void k_qef(QefArgs a, float4* __restrict__ nd_v, const float4* __restrict__ nd_c,
                       const int8_t* __restrict__ nd_type, const float* __restrict__ nd_samp,
@@ -81,79 +117,135 @@ __global__ void k_qef(QefArgs a, float4* __restrict__ nd_v, const float4* __rest
   const float mn[3] = {__fsub_rn(c.x, h), __fsub_rn(c.y, h), __fsub_rn(c.z, h)};
   const float mx[3] = {__fadd_rn(c.x, h), __fadd_rn(c.y, h), __fadd_rn(c.z, h)};
   const float* sv = nd_samp + node * 27;
+  // GridEval's finite differences (src/evaluator.cpp:185-240), in FP64 by
+  // multiplication with the reciprocal steps
+  const double i1 = 1.0 / (double)step, i2 = 1.0 / (2.0 * (double)step);
   double q[15];
+#pragma unroll
   for (int k = 0; k < 15; ++k) q[k] = 0.0;
-  double gx[27], gy[27], gz[27], px[27], py[27], pz[27];
   for (int i = 0; i < 27; ++i) {
     const int x = i % 3, y = (i / 3) % 3, z = i / 9;
-    // sample position (GenerateSampling) and GridEval finite differences
+    // sample position (GenerateSampling)
     const float t[3] = {x * 0.5f, y * 0.5f, z * 0.5f};
-    px[i] = __fadd_rn(__fmul_rn(1.0f - t[0], mn[0]), __fmul_rn(t[0], mx[0]));
-    py[i] = __fadd_rn(__fmul_rn(1.0f - t[1], mn[1]), __fmul_rn(t[1], mx[1]));
-    pz[i] = __fadd_rn(__fmul_rn(1.0f - t[2], mn[2]), __fmul_rn(t[2], mx[2]));
+    const double px = __fadd_rn(__fmul_rn(1.0f - t[0], mn[0]), __fmul_rn(t[0], mx[0]));
+    const double py = __fadd_rn(__fmul_rn(1.0f - t[1], mn[1]), __fmul_rn(t[1], mx[1]));
+    const double pz = __fadd_rn(__fmul_rn(1.0f - t[2], mn[2]), __fmul_rn(t[2], mx[2]));
     auto fd = [&](int d, int stride) {
-      if (d == 0) return ((double)sv[i] - (double)sv[i + stride]) / step;
-      if (d == 2) return ((double)sv[i - stride] - (double)sv[i]) / step;
-      return ((double)sv[i - stride] - (double)sv[i + stride]) / (2.0 * step);
+      if (d == 0) return ((double)sv[i] - (double)sv[i + stride]) * i1;
+      if (d == 2) return ((double)sv[i - stride] - (double)sv[i]) * i1;
+      return ((double)sv[i - stride] - (double)sv[i + stride]) * i2;
     };
-    gx[i] = fd(x, 1);
-    gy[i] = fd(y, 3);
-    gz[i] = fd(z, 9);
-    const double pl[5] = {gx[i], gy[i], gz[i], -1.0, -(px[i] * gx[i] + py[i] * gy[i] + pz[i] * gz[i]) + (double)sv[i]};
+    const double gx = fd(x, 1), gy = fd(y, 3), gz = fd(z, 9);
+    // plane [g, -1, f - p.g] (NodeCalcNode) accumulated as QEFNormal::combineSelf
+    const double pl[5] = {gx, gy, gz, -1.0, -(px * gx + py * gy + pz * gz) + (double)sv[i]};
     int idx = 0;
+#pragma unroll
     for (int r = 0; r < 5; ++r)
-      for (int s = r; s < 5; ++s) q[idx++] += pl[r] * pl[s];
+#pragma unroll
+      for (int s2 = r; s2 < 5; ++s2) q[idx++] += pl[r] * pl[s2];
   }
   double A[4][4], B[4];
+#pragma unroll
   for (int r = 0; r < 4; ++r) {
     const int idx = ((2 * 4 + 3 - r) * r) / 2;
-    for (int s = r; s < 4; ++s) A[r][s] = A[s][r] = q[idx + s - r];
+#pragma unroll
+    for (int s2 = r; s2 < 4; ++s2) A[r][s2] = A[s2][r] = q[idx + s2 - r];
     B[r] = -q[idx + 4 - r];
   }
   // Equilibrate: the gradient rows are ~|f| / step while the w column is 1,
   // so A's condition number exceeds what FP32 or even FP64 resolves.  With
   // D = diag(A_ii)^-1/2 the solve is (D A D) y = D B, x = D y: the same
   // minimiser in exact arithmetic, well conditioned unless the planes are
-  // degenerate.
+  // degenerate.  Afterwards every non-zero diagonal entry is 1, so the
+  // largest eigenvalue lies in [1, 4] (or A = 0).
   double D[4];
+#pragma unroll
   for (int r = 0; r < 4; ++r) D[r] = A[r][r] > 0.0 ? 1.0 / sqrt(A[r][r]) : 1.0;
+#pragma unroll
   for (int r = 0; r < 4; ++r) {
     B[r] *= D[r];
-    for (int s = 0; s < 4; ++s) A[r][s] *= D[r] * D[s];
+#pragma unroll
+    for (int s2 = 0; s2 < 4; ++s2) A[r][s2] *= D[r] * D[s2];
   }
-  double w[4], V[4][4];
-  sym_eig4(A, w, V);
-  double wmax = 0.0;
-  for (int k = 0; k < 4; ++k) wmax = fmax(wmax, fabs(w[k]));
-  const double tol = 1e-12 * wmax;
-  bool singular = !(wmax > 0.0);
+  // Pseudo-inverse rule: eigenvalues at most 1e-12 * max |eigenvalue| are
+  // dropped, and a system with a dropped eigenvalue counts as singular (the
+  // reference's Matrix4f::inverse gives non-finite values there and the
+  // vertex is rejected).  Decided without an eigen-decomposition where the
+  // bounds settle it: the smallest eigenvalue is at most every LDL^T pivot,
+  // and at least 1 / ||A^-1||_F, while the largest lies in [1, trace].
+  const double tr = A[0][0] + A[1][1] + A[2][2] + A[3][3];
+  bool singular, solved = false;
   double xs[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int k = 0; k < 4; ++k) {
-    if (fabs(w[k]) <= tol) {
-      singular = true;
-      continue;
+  double Ai[4][4];
+  const int ok = tr > 0.0 ? ldlt_inverse4(A, 1e-12, Ai) : 0;
+  if (!(tr > 0.0) || !ok) {
+    singular = true;  // a pivot below 1e-12 <= 1e-12 * max eigenvalue
+    solved = true;
+  } else {
+    double f2 = 0.0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int s2 = 0; s2 < 4; ++s2) f2 += Ai[r][s2] * Ai[r][s2];
+    const double t = 1e-12 * tr;
+    singular = false;
+    if (f2 * t * t < 1.0) {  // smallest eigenvalue > 1e-12 * trace >= tolerance
+#pragma unroll
+      for (int r = 0; r < 4; ++r) xs[r] = Ai[r][0] * B[0] + Ai[r][1] * B[1] + Ai[r][2] * B[2] + Ai[r][3] * B[3];
+      solved = true;
     }
-    double proj = 0.0;
-    for (int r = 0; r < 4; ++r) proj += V[r][k] * B[r];
-    proj /= w[k];
-    for (int r = 0; r < 4; ++r) xs[r] += V[r][k] * proj;
   }
-  for (int r = 0; r < 4; ++r) xs[r] *= D[r];
-  const bool in_cell = xs[0] >= mn[0] && xs[0] <= mx[0] && xs[1] >= mn[1] && xs[1] <= mx[1] && xs[2] >= mn[2] &&
-                       xs[2] <= mx[2];
-  double err = 1e30;
+  if (!solved) {
+    // borderline conditioning: the eigen-decomposition decides
+    double w[4], V[4][4];
+    sym_eig4(A, w, V);
+    double wmax = 0.0;
+    for (int k = 0; k < 4; ++k) wmax = fmax(wmax, fabs(w[k]));
+    const double tol = 1e-12 * wmax;
+    singular = !(wmax > 0.0);
+    for (int k = 0; k < 4; ++k) {
+      if (fabs(w[k]) <= tol) {
+        singular = true;
+        continue;
+      }
+      double proj = 0.0;
+      for (int r = 0; r < 4; ++r) proj += V[r][k] * B[r];
+      proj /= w[k];
+      for (int r = 0; r < 4; ++r) xs[r] += V[r][k] * proj;
+    }
+  }
   float4 v = nd_v[node];
+  float err = 1e30f;
   bool accepted = false;
-  if (in_cell && !singular) {
-    err = 0.0;
-    for (int i = 0; i < 27; ++i) {
-      const double d = gx[i] * (xs[0] - px[i]) + gy[i] * (xs[1] - py[i]) + gz[i] * (xs[2] - pz[i]) - xs[3];
-      err += d * d / (1.0 + gx[i] * gx[i] + gy[i] * gy[i] + gz[i] * gz[i]);
+  if (!singular) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) xs[r] *= D[r];
+    const bool in_cell = xs[0] >= mn[0] && xs[0] <= mx[0] && xs[1] >= mn[1] && xs[1] <= mx[1] &&
+                         xs[2] >= mn[2] && xs[2] <= mx[2];
+    if (in_cell) {
+      v = make_float4((float)xs[0], (float)xs[1], (float)xs[2], (float)xs[3]);
+      // calcErrorDMC (src/iso_method_ours.cpp:40-50) with GridEval's float
+      // gradients, float as in the reference
+      err = 0.0f;
+      for (int i = 0; i < 27; ++i) {
+        const int x = i % 3, y = (i / 3) % 3, z = i / 9;
+        const float px = __fadd_rn(__fmul_rn(1.0f - x * 0.5f, mn[0]), __fmul_rn(x * 0.5f, mx[0]));
+        const float py = __fadd_rn(__fmul_rn(1.0f - y * 0.5f, mn[1]), __fmul_rn(y * 0.5f, mx[1]));
+        const float pz = __fadd_rn(__fmul_rn(1.0f - z * 0.5f, mn[2]), __fmul_rn(z * 0.5f, mx[2]));
+        auto fdf = [&](int d, int stride) {
+          if (d == 0) return (sv[i] - sv[i + stride]) / step;
+          if (d == 2) return (sv[i - stride] - sv[i]) / step;
+          return (sv[i - stride] - sv[i + stride]) / (step * 2);
+        };
+        const float gx = fdf(x, 1), gy = fdf(y, 3), gz = fdf(z, 9);
+        const float d = gx * (v.x - px) + gy * (v.y - py) + gz * (v.z - pz) - v.w;
+        err += d * d / (1.0f + gx * gx + gy * gy + gz * gz);
+      }
+      accepted = true;
     }
-    v = make_float4((float)xs[0], (float)xs[1], (float)xs[2], (float)xs[3]);
-    accepted = true;
+  } else {
+    stripe_add(counters, 6, 1ull);
   }
-  if (in_cell && singular) stripe_add(counters, 6, 1ull);
   if (accepted) {
     v.w = a.iso - field_sum(a.g, a.P, v.x, v.y, v.z, nullptr);
     stripe_add(counters, 7, 1ull);
@@ -161,9 +253,9 @@ __global__ void k_qef(QefArgs a, float4* __restrict__ nd_v, const float4* __rest
   }
   // leaf by size keeps the zeroing (no SingleEval follows it)
   const bool leaf_by_size = (double)(cellsize - a.radius) < 1e-8;
-  if (leaf_by_size && err / (double)cellsize < 0.0001) v.w = 0.0f;
+  if (leaf_by_size && err / cellsize < 0.0001f) v.w = 0.0f;
   nd_v[node] = v;
-  if (qef_err) qef_err[node] = (float)err;
+  if (qef_err) qef_err[node] = err;
 }
 
 void qef_level(pi_frame* f, long long lb, long long le) {
