@@ -48,6 +48,10 @@ FLOPS_PER_PAIR = 38
 # frame, counted by a full oracle run of it (oracle/pi_oracle.cpp counters).
 ORACLE_FIELD_EVALS = 147191991
 ORACLE_PAIRS = 7205138892
+# dram__bytes_read.sum + dram__bytes_write.sum of the field-evaluation launches
+# of one 1M-particle frame (k_q_eval_thread x2, k_q_eval), one ncu capture;
+# see profiles/k_q_eval_dam_break.md
+FIELD_DRAM_BYTES_PER_FRAME = 383026432
 
 
 def parse():
@@ -56,7 +60,7 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--n", type=int, default=1_000_000)
+    p.add_argument("--n", "--particles", dest="n", type=int, default=1_000_000)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-evals", type=int, default=200_000)
     p.add_argument("--qef", action="store_true", help="with --single: per-leaf QEF vertices on")
@@ -94,6 +98,35 @@ def batch64(a):
         f.close()
     t_seq = time.perf_counter() - t0
     ctx.close()
+    # device-resident form: the 64 frames stay uploaded; one at a time on one
+    # context versus spread over `slots` contexts (own streams) driven by as
+    # many host threads (the C calls release the GIL)
+    import threading
+    ctxs = [N.Context(0) for _ in range(a.slots)]
+    res = [N.Frame(ctxs[k % a.slots], N.default_params(fr.radius)).upload(fr.xyz) for k, fr in enumerate(frames)]
+    for f in res[:2]:
+        f.reset().run()
+    t0 = time.perf_counter()
+    for f in res:
+        f.reset().run()  # returns once the frame is done
+    t_res_seq = time.perf_counter() - t0
+
+    def work(k):
+        for f in res[k::a.slots]:
+            f.reset().run()
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=work, args=(k,)) for k in range(a.slots)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    t_res_con = time.perf_counter() - t0
+    for f in res:
+        f.close()
+    for c in ctxs:
+        c.close()
+
     srv = N.Server(0, slots=a.slots, budget_bytes=0)
     for fr in frames[:2]:
         srv.result(srv.submit(fr.xyz, N.default_params(fr.radius)))
@@ -106,6 +139,11 @@ def batch64(a):
     print(json.dumps({
         "metric": METRIC, "workload": "batch64", "value": len(frames) / t_bat, "unit": UNIT,
         "one_at_a_time_frames_per_s": len(frames) / t_seq, "speedup_vs_one_at_a_time": t_seq / t_bat,
+        "resident": {"one_at_a_time_frames_per_s": len(frames) / t_res_seq,
+                     "concurrent_frames_per_s": len(frames) / t_res_con,
+                     "speedup": t_res_seq / t_res_con,
+                     "timing": "host wall clock around pi_run on device-resident frames (pi_run returns when "
+                               "its frame is done)"},
         "frames": len(frames), "particles_total": total_n, "slots": a.slots, "max_in_flight": st["max_in_flight"],
         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
         "timing": "host wall clock, host buffers in and out (upload, run, mesh download)",
@@ -226,6 +264,41 @@ def single(a):
                                            "candidate_pairs", "stage_ms", "qef_accepted")}))
     f.close()
     ctx.close()
+
+
+def fp32_gemm_tflops(torch, n=8192, reps=5):
+    """Measured FP32 denominator: cuBLAS SGEMM n^3 with TF32 off (FFMA pipe),
+    best of `reps`, CUDA events."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        a = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        b = torch.randn(n, n, device="cuda", dtype=torch.float32)
+        torch.matmul(a, b)
+        best = 1e30
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        del a, b
+        return 2.0 * n ** 3 / (best / 1000.0) / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def rank_max(x, world):
+    """Max of a per-rank number over all ranks (timings: the slowest rank sets
+    the step time).  Host-side gloo collective; frames never leave their GPU."""
+    if world == 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def dist_env():
@@ -399,11 +472,7 @@ def ours(a):
     ctx.profile(False)
     step_ms = [s.elapsed_time(e) for s, e in ev]
     info = f.info()
-    ms = float(np.mean(step_ms))
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = rank_max(float(np.mean(step_ms)), world)
 
     # ---- the same frame with the per-leaf FP64 QEF solve switched on ----
     pq = N.default_params(fr.radius)
@@ -420,7 +489,7 @@ def ours(a):
         fq.reset().run()
         evq[k][1].record(stream)
     barrier()
-    qef_ms = float(np.mean([s.elapsed_time(e) for s, e in evq]))
+    qef_ms = rank_max(float(np.mean([s.elapsed_time(e) for s, e in evq])), world)
     qinfo = fq.info()
     fq.close()
 
@@ -450,11 +519,7 @@ def ours(a):
         e2e_step()
         ev2[k][1].record(stream)
     barrier()
-    e2e_ms = float(np.mean([s.elapsed_time(e) for s, e in ev2]))
-    if world > 1:
-        t = torch.tensor([e2e_ms], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = rank_max(float(np.mean([s.elapsed_time(e) for s, e in ev2])), world)
 
     if rank == 0:
         evals = info["field_evals"]
@@ -486,12 +551,17 @@ def ours(a):
         if kt["ms"] > 0 and kt["launches"] > 0:
             achieved = kt["pairs"] * FLOPS_PER_PAIR / (kt["ms"] / 1000.0) / 1e12
             sm_mhz = ck.get("sm_max_mhz") or 2070.0
-            peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-            line["roofline"] = {"kernel": "k_q_eval_thread + k_q_eval (field evaluation at octree samples)", "bound": "fp32",
+            nominal = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+            peak = fp32_gemm_tflops(torch)
+            line["roofline"] = {"kernel": "k_q_eval_thread + k_q_eval (field evaluation at octree samples)",
+                                "bound": "fp32",
                                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                                "traffic": None,
-                                "peak_source": "nominal FP32: 152 SMs x 128 lanes x 2 flop x max SM clock "
-                                               "(MEASURED_PEAKS.json has no FP32 figure)",
+                                "traffic": FIELD_DRAM_BYTES_PER_FRAME if fr.n == 1_000_000 else None,
+                                "traffic_per": "frame (the same launches), ncu capture in "
+                                               "profiles/k_q_eval_dam_break.md",
+                                "peak_source": "measured in this run: cuBLAS FP32 GEMM 8192^3, TF32 off, best of 5 "
+                                               "(MEASURED_PEAKS.json has HBM and bf16 figures only)",
+                                "nominal_fp32_peak": nominal, "frac_of_nominal": achieved / nominal,
                                 "kernel_ms_per_step": kt["ms"] / a.steps,
                                 "launches_per_step": kt["launches"] / a.steps}
         if not a.no_cpu_baseline and world == 1:

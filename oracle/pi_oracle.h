@@ -10,6 +10,15 @@
  * The oracle keeps the reference's data structures on purpose (std::map cell
  * table, per-query std::vector candidate lists, OpenMP tasks per octree node,
  * string-keyed mesh maps) so that its run time is the reference's.
+ *
+ * Parity unpinned: the reference cannot be compiled in this environment (it
+ * needs Eigen 3.4, HDF5, VTK and MPI, and Windows-only headers) and ships no
+ * tests, golden vectors or fixtures, so no output of the reference itself
+ * checks this restatement.  Pinned: the DMC case table and triangle lists
+ * against digests of the reference's source tables (tests/golden), and the
+ * known-answer tests of tests/test_oracle.py.  Eigen's JacobiSVD,
+ * determinant and inverse are restated (Jacobi SVD of the symmetric
+ * covariance, cofactor determinant, adjugate inverse).
  */
 #ifndef PI_ORACLE_H
 #define PI_ORACLE_H
