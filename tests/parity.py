@@ -69,6 +69,7 @@ def compare_octrees(o_nodes, g_nodes, oracle, max_scalar, depth_min):
     B = node_table(g_nodes)
     rep = dict(nodes_oracle=len(A), nodes_gpu=len(B), type_mismatch=0, explained=0, unexplained=[],
                leaf_value_maxdiff=0.0, compared=0)
+    far_pos, far_gpu = [], []
     skip_prefix = set()
 
     def under_skipped(key):
@@ -102,10 +103,16 @@ def compare_octrees(o_nodes, g_nodes, oracle, max_scalar, depth_min):
                 rep["unexplained"].append(("type", key, ta, tb, ca, cb, sa, sb))
             continue
         if ta == 2:
-            rep["leaf_value_maxdiff"] = max(rep["leaf_value_maxdiff"], abs(float(na[3]) - float(nb[3])))
+            dv = abs(float(na[3]) - float(nb[3]))
+            rep["leaf_value_maxdiff"] = max(rep["leaf_value_maxdiff"], dv)
+            if dv > FIELD_TOL * max_scalar:
+                far_pos.append(np.asarray(nb[:3], np.float32))
+                far_gpu.append(float(nb[3]))
     for key in B:
         if key not in A and not under_skipped(key):
             rep["unexplained"].append(("extra", key))
+    rep["leaf_far_pos"] = np.array(far_pos, np.float32).reshape(-1, 3)
+    rep["leaf_far_gpu"] = np.array(far_gpu)
     return rep
 
 

@@ -22,6 +22,10 @@ pytestmark = pytest.mark.gpu
 CASES = {
     "blob2k": lambda: synth.small_blob(n=2000, seed=3),
     "slab6k": lambda: synth.slab_and_sphere(n=6000, seed=7),
+    # the CPU-runnable single frame: 20,000 particles on a slab and a sphere, r = 0.025
+    "slab_sphere_20k": lambda: synth.slab_and_sphere(n=20000, seed=1),
+    # the precision-stress geometry (thin sheets, filaments) at a parity size
+    "sheets_20k": lambda: synth.sheets_and_filaments(n=20000, seed=9),
 }
 
 
@@ -148,7 +152,9 @@ def test_field_and_gradient_within_tolerance(ctx, name):
     print(name, "field err vs FP64: gpu max %.3e rms %.3e | float oracle max %.3e rms %.3e"
           % (e_gpu.max(), np.sqrt(np.mean(e_gpu ** 2)), e_ref.max(), np.sqrt(np.mean(e_ref ** 2))))
     assert e_gpu.max() <= PR.FIELD_TOL_FP64
-    assert np.abs(sg - so).max() <= PR.FIELD_TOL * ms
+    # against the float oracle: its own error against FP64 plus ours (on thin
+    # sheets the reference's float SVD is ~1e-4 * MaxScalar off FP64)
+    assert np.all(np.abs(sg - so) <= np.maximum(PR.FIELD_TOL * ms, np.abs(so - s64) + PR.FIELD_TOL_FP64 * ms))
     assert np.abs(gg - go).max() <= PR.NORMAL_TOL * max(np.abs(go).max(), 1e-30)
 
 
@@ -157,10 +163,20 @@ def test_octree_identical_except_near_iso(ctx, name):
     fr, o, g = run_pair(ctx, name)
     rep = PR.compare_octrees(o.nodes(), g.dump(N.DUMP_NODES), o, o.scalars()["max_scalar"],
                              o.depths()["depth_min"])
-    print(name, {k: v for k, v in rep.items() if k != "unexplained"}, rep["unexplained"][:5])
+    print(name, {k: v for k, v in rep.items() if k not in ("unexplained", "leaf_far_pos", "leaf_far_gpu")},
+          rep["unexplained"][:5])
     assert not rep["unexplained"]
     assert rep["explained"] <= max(2, rep["compared"] // 10000)
-    assert rep["leaf_value_maxdiff"] <= PR.FIELD_TOL * o.scalars()["max_scalar"]
+    ms = o.scalars()["max_scalar"]
+    if rep["leaf_value_maxdiff"] > PR.FIELD_TOL * ms:
+        # leaves where the float oracle and the library differ by more than
+        # FIELD_TOL: the library must then be within FIELD_TOL_FP64 of FP64
+        pos, vg = rep["leaf_far_pos"], rep["leaf_far_gpu"]
+        v64 = fp64_oracle(name).eval(pos)
+        err = np.abs(vg - v64) / ms
+        print(name, "%d leaves beyond FIELD_TOL of the float oracle; library vs FP64 max %.3e"
+              % (len(pos), err.max()))
+        assert err.max() <= PR.FIELD_TOL_FP64
 
 
 @pytest.mark.parametrize("name", list(CASES))
