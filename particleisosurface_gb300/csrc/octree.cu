@@ -589,11 +589,14 @@ __global__ void k_spawn(long long lb, long long le, long long cbase, const int* 
 // tested against the children's float bounds exactly as the child itself
 // would compute them (checkEmptyAndCalcCurv, src/surface_reconstructor.cpp:
 // 152-222).  One warp per parent; lane k writes child k.
-__global__ void k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict__ rank, int child_depth, int curv,
-                             float4* __restrict__ nd_c, float4* __restrict__ nd_v, uint64_t* __restrict__ nd_id,
-                             int* __restrict__ nd_parent, int* __restrict__ nd_child, int8_t* nd_type,
-                             int8_t* __restrict__ nd_depth, int8_t* __restrict__ nd_sc, float* __restrict__ nd_curv,
-                             int4* __restrict__ nd_org) {
+template <bool CURV>
+__global__ void __launch_bounds__(256) k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict__ rank,
+                                                    int child_depth, float4* __restrict__ nd_c,
+                                                    float4* __restrict__ nd_v, uint64_t* __restrict__ nd_id,
+                                                    int* __restrict__ nd_parent, int* __restrict__ nd_child,
+                                                    int8_t* nd_type, int8_t* __restrict__ nd_depth,
+                                                    int8_t* __restrict__ nd_sc, float* __restrict__ nd_curv,
+                                                    int4* __restrict__ nd_org) {
   const long long i = a.lb + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (i >= a.le) return;
@@ -617,45 +620,63 @@ __global__ void k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict
       chi[ax][bit] = __fadd_rn(__fadd_rn(c, hc), e);
     }
   // the parent's grown box is the union: low child's lo to high child's hi
-  GrownBox pb;
-  pb.lox = clo[0][0], pb.loy = clo[1][0], pb.loz = clo[2][0];
-  pb.hix = chi[0][1], pb.hiy = chi[1][1], pb.hiz = chi[2][1];
-  pb.x0 = max(cell_coord(pb.lox, a.g.b0, a.g.cell, a.g.nx), 0);
-  pb.y0 = max(cell_coord(pb.loy, a.g.b2, a.g.cell, a.g.ny), 0);
-  pb.z0 = max(cell_coord(pb.loz, a.g.b4, a.g.cell, a.g.nz), 0);
-  pb.x1 = min(cell_coord(pb.hix, a.g.b0, a.g.cell, a.g.nx), a.g.nx - 1);
-  pb.y1 = min(cell_coord(pb.hiy, a.g.b2, a.g.cell, a.g.ny), a.g.ny - 1);
-  pb.z1 = min(cell_coord(pb.hiz, a.g.b4, a.g.cell, a.g.nz), a.g.nz - 1);
+  const int x0 = max(cell_coord(clo[0][0], a.g.b0, a.g.cell, a.g.nx), 0);
+  const int y0 = max(cell_coord(clo[1][0], a.g.b2, a.g.cell, a.g.ny), 0);
+  const int z0 = max(cell_coord(clo[2][0], a.g.b4, a.g.cell, a.g.nz), 0);
+  const int x1 = min(cell_coord(chi[0][1], a.g.b0, a.g.cell, a.g.nx), a.g.nx - 1);
+  const int y1 = min(cell_coord(chi[1][1], a.g.b2, a.g.cell, a.g.ny), a.g.ny - 1);
+  const int z1 = min(cell_coord(chi[2][1], a.g.b4, a.g.cell, a.g.nz), a.g.nz - 1);
   unsigned found = 0;
-  float sum[8][4];
+  float sum[CURV ? 8 : 1][4];
 #pragma unroll
-  for (int k = 0; k < 8; ++k) sum[k][0] = sum[k][1] = sum[k][2] = sum[k][3] = 0.f;
-  if (pb.x0 <= pb.x1) {
-    bool all8 = false;
-    for (int z = pb.z0; z <= pb.z1 && !all8; ++z)
-      for (int y = pb.y0; y <= pb.y1; ++y) {
-        // emptiness only: stop once all eight children hold a particle
-        if (!curv && __reduce_or_sync(0xffffffffu, found) == 0xffu) {
-          all8 = true;
-          break;
-        }
+  for (int k = 0; k < (CURV ? 8 : 1); ++k) sum[k][0] = sum[k][1] = sum[k][2] = sum[k][3] = 0.f;
+  if (x0 <= x1 && y0 <= y1 && z0 <= z1) {
+    const int nyb = y1 - y0 + 1;
+    const int rows = (z1 - z0 + 1) * nyb;
+    // rows of the block, 32 at a time: lane r holds row r's particle range;
+    // the concatenated ranges are then walked 32 particles at a time
+    for (int r0 = 0; r0 < rows; r0 += 32) {
+      if (!CURV && __reduce_or_sync(0xffffffffu, found) == 0xffu) break;  // all eight children non-empty
+      const int r = r0 + lane;
+      int rs = 0, rl = 0;
+      if (r < rows) {
+        const int z = z0 + r / nyb, y = y0 + r % nyb;
         const long long base = ((long long)z * a.g.ny + y) * a.g.nx;
-        const int s = __ldg(a.g.off + base + pb.x0), en = __ldg(a.g.off + base + pb.x1 + 1);
-        for (int j = s + lane; j < en; j += 32) {
-          const float4 p = __ldg(a.pos + j);
-          const int mx = ((p.x > clo[0][0] && p.x < chi[0][0]) ? 1 : 0) | ((p.x > clo[0][1] && p.x < chi[0][1]) ? 2 : 0);
-          const int my = ((p.y > clo[1][0] && p.y < chi[1][0]) ? 1 : 0) | ((p.y > clo[1][1] && p.y < chi[1][1]) ? 2 : 0);
-          const int mz = ((p.z > clo[2][0] && p.z < chi[2][0]) ? 1 : 0) | ((p.z > clo[2][1] && p.z < chi[2][1]) ? 2 : 0);
-          if (mx && my && mz) {
-            unsigned m8 = 0;
+        rs = __ldg(a.g.off + base + x0);
+        rl = __ldg(a.g.off + base + x1 + 1) - rs;
+      }
+      int incl = rl;
 #pragma unroll
-            for (int k = 0; k < 8; ++k)
-              if (((mx >> (k & 1)) & 1) && ((my >> ((k >> 1) & 1)) & 1) && ((mz >> ((k >> 2) & 1)) & 1)) m8 |= 1u << k;
-            found |= m8;
-            if (!curv) continue;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      const int excl = incl - rl;
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      const int nr = min(32, rows - r0);
+      for (int t0 = 0; t0 < total; t0 += 32) {
+        if (!CURV && t0 > 0 && __reduce_or_sync(0xffffffffu, found) == 0xffu) break;
+        const int t = t0 + lane;
+        // row of element t: the last row whose start is <= t
+        int rr = 0;
+        for (int k = 1; k < nr; ++k)
+          if (__shfl_sync(0xffffffffu, excl, k) <= t) rr = k;
+        const int j = __shfl_sync(0xffffffffu, rs, rr) + (t - __shfl_sync(0xffffffffu, excl, rr));
+        if (t >= total) continue;
+        const float4 p = __ldg(a.pos + j);
+        const int mx = ((p.x > clo[0][0] && p.x < chi[0][0]) ? 1 : 0) | ((p.x > clo[0][1] && p.x < chi[0][1]) ? 2 : 0);
+        const int my = ((p.y > clo[1][0] && p.y < chi[1][0]) ? 1 : 0) | ((p.y > clo[1][1] && p.y < chi[1][1]) ? 2 : 0);
+        const int mz = ((p.z > clo[2][0] && p.z < chi[2][0]) ? 1 : 0) | ((p.z > clo[2][1] && p.z < chi[2][1]) ? 2 : 0);
+        if (mx && my && mz) {
+          unsigned m8 = 0;
+#pragma unroll
+          for (int k = 0; k < 8; ++k)
+            if (((mx >> (k & 1)) & 1) && ((my >> ((k >> 1) & 1)) & 1) && ((mz >> ((k >> 2) & 1)) & 1)) m8 |= 1u << k;
+          found |= m8;
+          if (CURV) {
             const float4 nv = __ldg(a.nrm + j);
 #pragma unroll
-            for (int k = 0; k < 8; ++k)
+            for (int k = 0; k < (CURV ? 8 : 1); ++k)
               if ((m8 >> k) & 1u) {
                 sum[k][0] += nv.x;
                 sum[k][1] += nv.y;
@@ -665,16 +686,19 @@ __global__ void k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict
           }
         }
       }
+    }
   }
   found = __reduce_or_sync(0xffffffffu, found);
   float mine[4] = {0.f, 0.f, 0.f, 0.f};
+  if (CURV) {
 #pragma unroll
-  for (int k = 0; k < 8; ++k)
+    for (int k = 0; k < (CURV ? 8 : 1); ++k)
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const float t = warp_sum(sum[k][q]);
-      if (lane == k) mine[q] = t;
-    }
+      for (int q = 0; q < 4; ++q) {
+        const float t = warp_sum(sum[k][q]);
+        if (lane == k) mine[q] = t;
+      }
+  }
   if (lane == 0) nd_child[i] = (int)b;
   if (lane < 8) {
     const int k = lane;
@@ -690,7 +714,7 @@ __global__ void k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict
     nd_type[b + k] = nonempty ? T_UNCERTAIN : T_EMPTY;
     nd_depth[b + k] = (int8_t)child_depth;
     nd_sc[b + k] = 0;
-    nd_curv[b + k] = !curv ? -1.0f
+    nd_curv[b + k] = !CURV ? -1.0f
                      : (mine[3] == 0.f) ? 1.0f
                                         : sqrtf(mine[0] * mine[0] + mine[1] * mine[1] + mine[2] * mine[2]) / mine[3];
     nd_org[b + k] = make_int4(po.x + ((k & 1) ? hs : 0), po.y + ((k & 2) ? hs : 0), po.z + ((k & 4) ? hs : 0), hs);
@@ -828,10 +852,14 @@ void stage_octree(pi_frame* f) {
       // before the curvature test), so their parents only settle emptiness
       const float cell_child = 2.0f * std::ldexp(f->rootH, -(depth + 1));
       const int child_curv = (double)(cell_child - f->P.radius) < 1e-8 ? 0 : 1;
-      PI_LAUNCH(k_spawn_scan, div_up(nl, wpb), 32 * wpb, 0, s, la, le, flag.p, depth + 1, child_curv, f->nd_c.p,
-                f->nd_v.p,
-                f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p, f->nd_curv.p,
-                f->nd_org.p);
+      if (child_curv)
+        PI_LAUNCH(k_spawn_scan<true>, div_up(nl, wpb), 32 * wpb, 0, s, la, le, flag.p, depth + 1, f->nd_c.p,
+                  f->nd_v.p, f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p,
+                  f->nd_curv.p, f->nd_org.p);
+      else
+        PI_LAUNCH(k_spawn_scan<false>, div_up(nl, wpb), 32 * wpb, 0, s, la, le, flag.p, depth + 1, f->nd_c.p,
+                  f->nd_v.p, f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p,
+                  f->nd_curv.p, f->nd_org.p);
     } else {
       PI_LAUNCH(k_spawn, div_up(nl, 256), 256, 0, s, lb, le, le, flag.p, f->nd_type.p, depth + 1, f->nd_c.p,
                 f->nd_v.p, f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p,
