@@ -66,7 +66,7 @@ def parse():
     p.add_argument("--qef", action="store_true", help="with --single: per-leaf QEF vertices on")
     p.add_argument("--single", action="store_true",
                    help="reconstruct one frame once and print its counters (for profiler captures)")
-    p.add_argument("--workload", choices=["dam_break_1m", "batch64", "serving", "stress"], default="dam_break_1m",
+    p.add_argument("--workload", choices=["dam_break_1m", "batch64", "serving", "stress", "grid"], default="dam_break_1m",
                    help="dam_break_1m: the metric's frame (default); batch64: 64 mixed frames batched vs one at "
                         "a time; serving: Poisson stream through the request loop; stress: sheets and filaments")
     p.add_argument("--frames", type=int, default=64, help="frames of the batch64 workload")
@@ -148,6 +148,104 @@ def batch64(a):
         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
         "timing": "host wall clock, host buffers in and out (upload, run, mesh download)",
         "data": "synthetic (seeded unions of spheres and slabs)"}))
+
+
+def grid(a):
+    """UniformGrid (the reference's dense-grid mode) on the 1M-particle frame:
+    the field on the lattice of spacing r over the particles' box.  value =
+    lattice points per second with the particles resident and the lattice
+    written to device memory; e2e = the same through pi_grid_sample into a
+    pinned host buffer (device-to-host copy of the values inside the region)."""
+    import ctypes as C
+
+    import torch
+
+    from particleisosurface_gb300 import _native as N
+    from particleisosurface_gb300 import build as B
+    B.build()
+    fr = make_frame(a.n)
+    ctx = N.Context(0)
+    f = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz)
+    f.hashgrid().aniso().normals()
+    dims, box, npts = f.grid_dims()
+    stream = torch.cuda.ExternalStream(N.lib().pi_ctx_stream(ctx.h), device=0)
+    d_out = torch.empty(npts, device="cuda", dtype=torch.float32)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(a.warmup):
+        f.grid_sample_device(d_out.data_ptr(), npts)
+    ctx.profile(True)
+    ctx.kernel_time()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    clocks = Clocks(0)
+    torch.cuda.synchronize()
+    clocks.start()
+    for k in range(a.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xff)
+        ev[k][0].record(stream)
+        f.grid_sample_device(d_out.data_ptr(), npts)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    kt = ctx.kernel_time()
+    ctx.profile(False)
+    ms = float(np.mean([s0.elapsed_time(e1) for s0, e1 in ev]))
+    info = f.info()
+    host = torch.empty(npts, dtype=torch.float32).pin_memory()
+    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    for k in range(a.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 0xff)
+        ev2[k][0].record(stream)
+        N.check(N.lib().pi_grid_sample(f.h, C.cast(host.data_ptr(), C.POINTER(C.c_float)), npts))
+        ev2[k][1].record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = float(np.mean([s0.elapsed_time(e1) for s0, e1 in ev2]))
+    vals = host.numpy()
+    pairs = info["grid_pairs"]
+    achieved = pairs * FLOPS_PER_PAIR / (kt["ms"] / a.steps / 1000.0) / 1e12
+    peak = fp32_gemm_tflops(torch)
+    line = {
+        "metric": METRIC, "workload": "grid", "value": npts / (ms / 1000.0), "unit": "lattice points/s",
+        "ms_per_step": ms, "steps": a.steps, "warmup": a.warmup, "higher_is_better": True,
+        "config": {"workload": WORKLOAD + "; UniformGrid lattice, spacing r", "dims": [int(d) for d in dims],
+                   "points": int(npts), "l2": "512 MiB buffer written between steps"},
+        "candidate_pairs_per_step": pairs, "kernel_ms_per_step": kt["ms"] / a.steps,
+        "e2e": {"value": npts / (e2e_ms / 1000.0), "unit": "lattice points/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 4 * int(npts)},
+        "roofline": {"kernel": "k_grid_eval", "bound": "fp32", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak,
+                     "peak_source": "measured in this run: cuBLAS FP32 GEMM 8192^3, TF32 off"},
+        "clocks": ck, "values_min_max": [float(vals.min()), float(vals.max())],
+        "data": "synthetic (seeded dam-break column + spray)"}
+    if not a.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle as O
+        O.build()
+        nthreads = os.cpu_count() or 1
+        O.set_threads(nthreads)
+        o = O.OracleFrame(fr.xyz, fr.radius)
+        for s in (1, 2, 3):
+            o.stage(s)
+        rng = np.random.default_rng(7)
+        m = min(a.cpu_sample_evals, int(npts))
+        pick = rng.choice(int(npts), m, replace=False)
+        zz, yy, xx = np.unravel_index(pick, (int(dims[2]), int(dims[1]), int(dims[0])))
+        f32 = np.float32
+
+        def coord(ax, i):
+            st = f32(int(dims[ax]) - 1)
+            return (f32(st - i.astype(f32)) / st) * box[2 * ax] + (i.astype(f32) / st) * box[2 * ax + 1]
+
+        pts = np.stack([coord(0, xx), coord(1, yy), coord(2, zz)], -1).astype(np.float32)
+        t0 = time.perf_counter()
+        o.eval(pts)
+        te = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": m / te, "unit": "lattice points/s", "cores": nthreads, "kind": "port",
+                                "sample": "oracle SingleEval at %d random lattice points of the same grid" % m}
+    print(json.dumps(line))
+    f.close()
+    ctx.close()
 
 
 def serving(a):
@@ -584,7 +682,7 @@ def ours(a):
 def main():
     a = parse()
     if a.workload != "dam_break_1m" and a.impl == "ours":
-        {"batch64": batch64, "serving": serving, "stress": stress}[a.workload](a)
+        {"batch64": batch64, "serving": serving, "stress": stress, "grid": grid}[a.workload](a)
     elif a.single:
         single(a)
     elif a.impl == "reference":

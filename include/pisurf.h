@@ -72,6 +72,7 @@ typedef struct pi_frame_info {
                                (an eigenvalue below 1e-12 of the largest); their
                                vertex is rejected, as the reference's non-finite
                                inverse is */
+  int64_t grid_pairs;       /* candidate pairs of the last uniform-grid sampling */
 } pi_frame_info;
 
 /* Parity dumps (pi_stage_dump).  Arrays are in original particle order unless
@@ -165,6 +166,20 @@ int pi_hashgrid_in_box(pi_frame* f, const float* box1, const float* box2, int32_
 
 int pi_stage_dump_size(const pi_frame* f, int what, size_t* bytes);
 int pi_stage_dump(pi_frame* f, int what, void* host_buf, size_t bytes);
+
+/* UniformGrid (src/marching.cpp), the reference's dense-grid mode: the field
+ * on a lattice of spacing r over the particles' box grown as in
+ * UniformGrid::resizeRootBoxConstR (:42-55), values as gridSampling (:72-93)
+ * computes them (SingleEval, x fastest).  pi_grid_dims needs the hash grid
+ * (box6 = lattice min/max per axis, origin = box6[0], box6[2], box6[4]);
+ * the sampling needs pi_normals_compute (iso value).  values/d_values must
+ * hold npoints floats (PI_ERR_LIMIT otherwise).  pi_grid_write_vti writes the
+ * samples as a VTK XML image ("scalars", raw appended Float32), the file the
+ * reference writes through VTK (:160-185). */
+int pi_grid_dims(pi_frame* f, int32_t* dims3, float* box6, int64_t* npoints);
+int pi_grid_sample(pi_frame* f, float* values, int64_t cap);
+int pi_grid_sample_device(pi_frame* f, float* d_values, int64_t cap);
+int pi_grid_write_vti(pi_frame* f, const char* path);
 
 /* One call, host in / host out: upload, Run, download (the e2e path of a
  * frame).  verts/tris must hold max_verts / max_tris entries; the actual

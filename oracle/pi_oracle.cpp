@@ -703,6 +703,7 @@ struct FrameBase {
   double seconds[6] = {0, 0, 0, 0, 0, 0};
   HashGrid grid;
   float BoundingBox[6];
+  float RawBox[6];  // loadRootBox's box before resizeRootBoxConstR (UniformGrid reads it)
   bool single_layer = false;
   int DEPTH_MAX = 6, DEPTH_MIN = 5;
   float RootHalfLength = 0;
@@ -748,6 +749,7 @@ struct Frame : FrameBase {
     }
     single_layer = (BoundingBox[0] == BoundingBox[1] || BoundingBox[2] == BoundingBox[3] ||
                     BoundingBox[4] == BoundingBox[5]);
+    for (int i = 0; i < 6; ++i) RawBox[i] = BoundingBox[i];
   }
 
   // src/surface_reconstructor.cpp:97-122
@@ -1449,6 +1451,61 @@ int pio_eval(pio_frame* h, const float* pts, int64_t m, double* scalar, double* 
     return 0;
   });
 }
+// UniformGrid::resizeRootBoxConstR (src/marching.cpp:42-55) on the
+// loadRootBox box: per axis resizeLen = ceil(length / r) r + 4 r around the
+// centre, steps = int(resizeLen / r), dims = steps + 1.
+static void uniform_grid_box(const FrameBase& f, float box[6], int steps[3], int dims[3]) {
+  for (int i = 0; i < 3; i++) {
+    float center = (f.RawBox[i * 2] + f.RawBox[i * 2 + 1]) / 2;
+    float length = f.RawBox[i * 2 + 1] - f.RawBox[i * 2];
+    float resizeLen = std::ceil(length / f.radius) * f.radius + f.radius * 4;
+    box[i * 2] = center - resizeLen / 2;
+    box[i * 2 + 1] = center + resizeLen / 2;
+    steps[i] = int(resizeLen / (f.radius));
+    dims[i] = steps[i] + 1;
+  }
+}
+
+int pio_uniform_grid(const pio_frame* h, float* box6, int32_t* steps3, int32_t* dims3) {
+  const FrameBase& f = *h->f;
+  if (f.stage_done < 1) return -1;
+  float box[6];
+  int steps[3], dims[3];
+  uniform_grid_box(f, box, steps, dims);
+  for (int i = 0; i < 6; ++i) box6[i] = box[i];
+  for (int i = 0; i < 3; ++i) {
+    steps3[i] = steps[i];
+    dims3[i] = dims[i];
+  }
+  return 0;
+}
+
+// UniformGrid::gridSampling (src/marching.cpp:72-93): SingleEval at every
+// lattice point, x fastest; point = (steps - x) / steps * min + x / steps * max.
+int pio_grid_sample(pio_frame* h, double* out, int64_t n) {
+  if (h->f->stage_done < 3) return -1;
+  float box[6];
+  int steps[3], dims[3];
+  uniform_grid_box(*h->f, box, steps, dims);
+  const int64_t total = (int64_t)dims[0] * dims[1] * dims[2];
+  if (n < total) return -2;
+  return with(h, [&](auto& f) {
+    const float minV[3] = {box[0], box[2], box[4]}, maxV[3] = {box[1], box[3], box[5]};
+#pragma omp parallel for
+    for (int64_t i = 0; i < total; i++) {
+      const int z = (int)(i / (dims[0] * dims[1]));
+      const int y = (int)((i % (dims[0] * dims[1])) / dims[0]);
+      const int x = (int)((i % (dims[0] * dims[1])) % dims[0]);
+      const float p[3] = {
+          float(steps[0] - x) / float(steps[0]) * minV[0] + float(x) / float(steps[0]) * maxV[0],
+          float(steps[1] - y) / float(steps[1]) * minV[1] + float(y) / float(steps[1]) * maxV[1],
+          float(steps[2] - z) / float(steps[2]) * minV[2] + float(z) / float(steps[2]) * maxV[2]};
+      out[i] = (double)f.ev.SingleEval(p);
+    }
+    return 0;
+  });
+}
+
 int64_t pio_num_nodes(const pio_frame* h) {
   return withc(h, [&](const auto& f) { return (int64_t)f.nodes.size(); });
 }

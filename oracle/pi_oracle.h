@@ -89,6 +89,12 @@ int pio_write_obj(const pio_frame* f, const char* path);
 /* the oracle's own dual-marching-cubes tables, for table tests */
 int pio_dmc_table(int32_t* trans8x256, int8_t* flip256, int32_t* code256);
 
+/* UniformGrid (src/marching.cpp): the sampling lattice of the loadRootBox box
+ * resized by resizeRootBoxConstR, and SingleEval at every lattice point (x
+ * fastest); pio_grid_sample needs stage 3. */
+int pio_uniform_grid(const pio_frame* f, float* box6, int32_t* steps3, int32_t* dims3);
+int pio_grid_sample(pio_frame* f, double* out, int64_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -66,6 +66,8 @@ def lib():
             "pio_mesh_get": (C.c_int, [P, fp, C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]),
             "pio_write_obj": (C.c_int, [P, C.c_char_p]),
             "pio_dmc_table": (C.c_int, [C.POINTER(C.c_int32), C.POINTER(C.c_int8), C.POINTER(C.c_int32)]),
+            "pio_uniform_grid": (C.c_int, [P, fp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+            "pio_grid_sample": (C.c_int, [P, dp, i64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -208,6 +210,25 @@ class OracleFrame:
         if rc:
             raise RuntimeError("oracle eval before normals stage")
         return (s, g) if grad else s
+
+    def uniform_grid(self):
+        """UniformGrid's lattice: box (6), steps (3), dims (3)."""
+        box = np.zeros(6, np.float32)
+        steps = np.zeros(3, np.int32)
+        dims = np.zeros(3, np.int32)
+        rc = lib().pio_uniform_grid(self.h, _p(box, C.c_float), _p(steps, C.c_int32), _p(dims, C.c_int32))
+        if rc:
+            raise RuntimeError("oracle uniform grid before stage 1")
+        return box, steps, dims
+
+    def grid_sample(self):
+        """UniformGrid::gridSampling: values[dims[2], dims[1], dims[0]] (float64)."""
+        box, steps, dims = self.uniform_grid()
+        out = np.zeros(int(dims[0]) * int(dims[1]) * int(dims[2]))
+        rc = lib().pio_grid_sample(self.h, _p(out, C.c_double), out.size)
+        if rc:
+            raise RuntimeError("oracle grid sampling before stage 3")
+        return out.reshape(int(dims[2]), int(dims[1]), int(dims[0]))
 
     def nodes(self):
         m = lib().pio_num_nodes(self.h)

@@ -42,7 +42,8 @@ class FrameInfo(C.Structure):
                 ("num_leaves", C.c_int64), ("num_empty", C.c_int64), ("num_dual_cells", C.c_int64),
                 ("num_vertices", C.c_int64), ("num_triangles", C.c_int64), ("field_evals", C.c_int64),
                 ("candidate_pairs", C.c_int64), ("bisection_evals", C.c_int64), ("fp64_eigen", C.c_int64),
-                ("stage_ms", C.c_float * 8), ("qef_accepted", C.c_int64), ("qef_singular", C.c_int64)]
+                ("stage_ms", C.c_float * 8), ("qef_accepted", C.c_int64), ("qef_singular", C.c_int64),
+                ("grid_pairs", C.c_int64)]
 
     def as_dict(self):
         out = {}
@@ -92,6 +93,10 @@ def _declare(L):
         "pi_mesh_get": (C.c_int, [P, fp, C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]),
         "pi_mesh_write_obj": (C.c_int, [P, C.c_char_p]),
         "pi_eval_field": (C.c_int, [P, fp, i64, fp, fp]),
+        "pi_grid_dims": (C.c_int, [P, C.POINTER(C.c_int32), fp, pi64]),
+        "pi_grid_sample": (C.c_int, [P, fp, i64]),
+        "pi_grid_sample_device": (C.c_int, [P, C.c_void_p, i64]),
+        "pi_grid_write_vti": (C.c_int, [P, C.c_char_p]),
         "pi_hashgrid_neighbors": (C.c_int, [P, fp, i64, pi64, C.POINTER(C.c_int32), i64, pi64]),
         "pi_hashgrid_in_box": (C.c_int, [P, fp, fp, C.POINTER(C.c_int32), i64, pi64]),
         "pi_stage_dump_size": (C.c_int, [P, C.c_int, C.POINTER(C.c_size_t)]),
@@ -287,6 +292,27 @@ class Frame:
         check(lib().pi_eval_field(self.h, ptr(pts, C.c_float), m, ptr(s, C.c_float),
                                   ptr(g, C.c_float) if grad else None))
         return (s, g) if grad else s
+
+    def grid_dims(self):
+        """UniformGrid lattice: dims (x, y, z), box (min/max per axis), point count."""
+        dims = np.zeros(3, np.int32)
+        box = np.zeros(6, np.float32)
+        n = C.c_int64()
+        check(lib().pi_grid_dims(self.h, ptr(dims, C.c_int32), ptr(box, C.c_float), C.byref(n)))
+        return dims, box, n.value
+
+    def grid_sample(self):
+        """UniformGrid::gridSampling: values[dims z, y, x] (float32)."""
+        dims, box, n = self.grid_dims()
+        out = np.empty(n, np.float32)
+        check(lib().pi_grid_sample(self.h, ptr(out, C.c_float), n))
+        return out.reshape(int(dims[2]), int(dims[1]), int(dims[0]))
+
+    def grid_sample_device(self, d_ptr, cap):
+        check(lib().pi_grid_sample_device(self.h, C.c_void_p(d_ptr), cap))
+
+    def write_vti(self, path):
+        check(lib().pi_grid_write_vti(self.h, path.encode()))
 
     def neighbors(self, pts):
         pts = np.ascontiguousarray(pts, dtype=np.float32)

@@ -498,6 +498,7 @@ int pi_frame_info_get(const pi_frame* f, pi_frame_info* o) {
   for (int k = 0; k < 8; ++k) o->stage_ms[k] = f->stage_ms[k];
   o->qef_accepted = f->qefAccepted;
   o->qef_singular = f->qefSingular;
+  o->grid_pairs = f->gridPairs;
   PI_API_END
 }
 
@@ -555,6 +556,98 @@ int pi_eval_field(pi_frame* f, const float* pts, int64_t m, float* scalar, float
   PI_CUDA(cudaMemcpyAsync(scalar, dv.p, sizeof(float) * m, cudaMemcpyDeviceToHost, s));
   if (grad) PI_CUDA(cudaMemcpyAsync(grad, dg.p, sizeof(float) * 3 * m, cudaMemcpyDeviceToHost, s));
   PI_CUDA(cudaStreamSynchronize(s));
+  PI_API_END
+}
+
+int pi_grid_dims(pi_frame* f, int32_t* dims3, float* box6, int64_t* npoints) {
+  PI_API_BEGIN
+  PI_CHECK(f && dims3, "bad arguments");
+  need(f, 2);
+  float box[6];
+  int steps[3], dims[3];
+  uniform_grid_host(f, box, steps, dims);
+  for (int i = 0; i < 3; ++i) dims3[i] = dims[i];
+  if (box6)
+    for (int i = 0; i < 6; ++i) box6[i] = box[i];
+  if (npoints) *npoints = (int64_t)dims[0] * dims[1] * dims[2];
+  PI_API_END
+}
+
+int pi_grid_sample_device(pi_frame* f, float* d_values, int64_t cap) {
+  PI_API_BEGIN
+  PI_CHECK(f && d_values, "bad arguments");
+  need(f, 4);
+  set_device(f->ctx);
+  const long long total = grid_sample(f, d_values, cap);
+  if (total > cap) throw std::length_error("value buffer too small for the lattice");
+  PI_API_END
+}
+
+int pi_grid_sample(pi_frame* f, float* values, int64_t cap) {
+  PI_API_BEGIN
+  PI_CHECK(f && values, "bad arguments");
+  need(f, 4);
+  set_device(f->ctx);
+  cudaStream_t s = f->ctx->stream;
+  const long long total = grid_sample(f, nullptr, 0);
+  if (total > cap) throw std::length_error("value buffer too small for the lattice");
+  DBuf<float> dv;
+  dv.alloc(f->ctx, s, total);
+  grid_sample(f, dv.p, total);
+  PI_CUDA(cudaMemcpyAsync(values, dv.p, sizeof(float) * total, cudaMemcpyDeviceToHost, s));
+  PI_CUDA(cudaStreamSynchronize(s));
+  PI_API_END
+}
+
+int pi_grid_write_vti(pi_frame* f, const char* path) {
+  PI_API_BEGIN
+  PI_CHECK(f && path, "bad arguments");
+  need(f, 4);
+  set_device(f->ctx);
+  float box[6];
+  int steps[3], dims[3];
+  uniform_grid_host(f, box, steps, dims);
+  const long long total = (long long)dims[0] * dims[1] * dims[2];
+  std::vector<float> v((size_t)total);
+  {
+    cudaStream_t s = f->ctx->stream;
+    DBuf<float> dv;
+    dv.alloc(f->ctx, s, total);
+    grid_sample(f, dv.p, total);
+    PI_CUDA(cudaMemcpyAsync(v.data(), dv.p, sizeof(float) * total, cudaMemcpyDeviceToHost, s));
+    PI_CUDA(cudaStreamSynchronize(s));
+  }
+  FILE* fp = std::fopen(path, "wb");
+  if (!fp) throw std::invalid_argument(std::string("cannot open ") + path);
+  const float r = f->P.radius;
+  std::fprintf(fp,
+               "<?xml version=\"1.0\"?>\n"
+               "<VTKFile type=\"ImageData\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n"
+               "  <ImageData WholeExtent=\"0 %d 0 %d 0 %d\" Origin=\"%.9g %.9g %.9g\" Spacing=\"%.9g %.9g %.9g\">\n"
+               "    <Piece Extent=\"0 %d 0 %d 0 %d\">\n"
+               "      <PointData Scalars=\"scalars\">\n"
+               "        <DataArray type=\"Float32\" Name=\"scalars\" format=\"appended\" offset=\"0\"/>\n"
+               "      </PointData>\n"
+               "    </Piece>\n"
+               "  </ImageData>\n"
+               "  <AppendedData encoding=\"raw\">\n_",
+               dims[0] - 1, dims[1] - 1, dims[2] - 1, box[0], box[2], box[4], r, r, r, dims[0] - 1, dims[1] - 1,
+               dims[2] - 1);
+  const uint64_t nbytes = sizeof(float) * (uint64_t)total;
+  unsigned char hdr[8];
+  for (int k = 0; k < 8; ++k) hdr[k] = (unsigned char)((nbytes >> (8 * k)) & 0xffu);
+  std::fwrite(hdr, 1, 8, fp);
+  std::vector<unsigned char> le((size_t)nbytes);
+  for (long long i = 0; i < total; ++i) {
+    uint32_t u;
+    std::memcpy(&u, &v[(size_t)i], 4);
+    for (int k = 0; k < 4; ++k) le[(size_t)i * 4 + k] = (unsigned char)((u >> (8 * k)) & 0xffu);
+  }
+  std::fwrite(le.data(), 1, le.size(), fp);
+  std::fprintf(fp, "\n  </AppendedData>\n</VTKFile>\n");
+  const bool ok = std::ferror(fp) == 0;
+  std::fclose(fp);
+  if (!ok) throw std::invalid_argument(std::string("write failed: ") + path);
   PI_API_END
 }
 

@@ -109,6 +109,7 @@ struct pi_frame {
   // counters
   long long fieldEvals = 0, pairs = 0, bisectEvals = 0, fp64Count = 0, nLeaves = 0, nEmpty = 0;
   long long qefAccepted = 0, qefSingular = 0;
+  long long gridPairs = 0;  // candidate pairs of the last uniform-grid sampling
   pisurf::DBuf<unsigned long long> dcount;  // device counters
   cudaEvent_t ev[9] = {};
   float stage_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -124,6 +125,10 @@ void stage_normals(pi_frame* f);
 void stage_octree(pi_frame* f);
 void stage_extract(pi_frame* f);
 void qef_level(pi_frame* f, long long lb, long long le);
+// UniformGrid: lattice of the loadRootBox box; sampling into d_out (device,
+// x fastest) when cap holds it; returns the number of lattice points.
+void uniform_grid_host(const pi_frame* f, float box[6], int steps[3], int dims[3]);
+long long grid_sample(pi_frame* f, float* d_out, long long cap);
 void eval_points(pi_frame* f, const float* d_pts, long long m, float* d_val, float* d_grad);
 long long neighbors(pi_frame* f, const float* h_pts, long long m, long long* h_off, int* h_idx,
                     long long cap);

@@ -32,6 +32,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "chunk.cuh"
 #include "device.cuh"
 #include "internal.h"
 
@@ -41,7 +42,6 @@ enum : int8_t { T_EMPTY = 0, T_INTERNAL = 1, T_LEAF = 2, T_UNCERTAIN = 3 };
 
 constexpr int kQ = 28;  // 27 samples + the centre per node
 constexpr int kEvalWarps = 8;  // warps per block of k_q_eval
-constexpr int kCandBuf = 64;   // staged candidate records per warp
 constexpr int kChunk = 64;     // samples per chunk of k_q_eval: two per lane
 
 struct LevelArgs {
@@ -291,14 +291,6 @@ __global__ void k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c
   if (head) chunks[cb + __popc(hm & ((1u << lane) - 1u))] = make_int2(k, place);
 }
 
-// Order-preserving map of a float onto a signed int (for warp min / max).
-__device__ __forceinline__ int fkey(float v) {
-  const int i = __float_as_int(v);
-  return i >= 0 ? i : i ^ 0x7fffffff;
-}
-__device__ __forceinline__ float fkey_inv(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff); }
-
-
 // Field at the samples of one chunk per warp (persistent, grid-stride over
 // the chunks); lane l holds samples l and l + 32 of the chunk.  All samples
 // of a chunk share a hash cell, hence the 27-cell candidate list of
@@ -321,11 +313,7 @@ __global__ void __launch_bounds__(32 * kEvalWarps, 3) k_q_eval(QArgs a, const in
       s_l[kEvalWarps][kCandBuf];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  float4* cx4 = s_x[wib];
-  float4* ca4 = s_a[wib];
-  float4* cb4 = s_b[wib];
-  float4* cl4 = s_l[wib];
-  const unsigned lt = (1u << lane) - 1u;
+  const ChunkStage st{s_x[wib], s_a[wib], s_b[wib], s_l[wib]};
   const int nchunks = *nchunks_ptr;
   const int nwarps = gridDim.x * kEvalWarps;
   long long pairs = 0;
@@ -333,96 +321,27 @@ __global__ void __launch_bounds__(32 * kEvalWarps, 3) k_q_eval(QArgs a, const in
     const int2 ch = chunks[ci];
     const int len = min(kChunk, __ldg(ucnt + ch.x) - ch.y);
     const int* ord = order + __ldg(qoff + ch.x) + ch.y;
-    const bool act0 = lane < len, act1 = lane + 32 < len;
-    const bool two = len > 32;  // warp-uniform
-    int q0 = 0, q1 = 0;
-    float x0 = 0.f, y0 = 0.f, z0 = 0.f, x1 = 0.f, y1 = 0.f, z1 = 0.f;
-    if (act0) {
-      q0 = ord[lane];
-      const long long node = a.lb + q0 / kQ;
-      sample_point(nd_c[node], nd_v[node], q0 % kQ, x0, y0, z0);
-    }
-    if (act1) {
-      q1 = ord[lane + 32];
-      const long long node = a.lb + q1 / kQ;
-      sample_point(nd_c[node], nd_v[node], q1 % kQ, x1, y1, z1);
+    int q[2] = {0, 0};
+    float x[2] = {0.f, 0.f}, y[2] = {0.f, 0.f}, z[2] = {0.f, 0.f};
+    bool act[2], slots[2];
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+      act[m] = lane + 32 * m < len;
+      slots[m] = len > 32 * m;  // warp-uniform
+      if (act[m]) {
+        q[m] = ord[lane + 32 * m];
+        const long long node = a.lb + q[m] / kQ;
+        sample_point(nd_c[node], nd_v[node], q[m] % kQ, x[m], y[m], z[m]);
+      }
     }
     int cx, cy, cz;
-    cell_of(a.g, __shfl_sync(0xffffffffu, x0, 0), __shfl_sync(0xffffffffu, y0, 0),
-            __shfl_sync(0xffffffffu, z0, 0), cx, cy, cz);
-    // bounding box of the chunk's samples
-    const int kmin = 0x7fffffff, kmax = (int)0x80000000;
-    const float blx = fkey_inv(__reduce_min_sync(0xffffffffu, min(act0 ? fkey(x0) : kmin, act1 ? fkey(x1) : kmin)));
-    const float bly = fkey_inv(__reduce_min_sync(0xffffffffu, min(act0 ? fkey(y0) : kmin, act1 ? fkey(y1) : kmin)));
-    const float blz = fkey_inv(__reduce_min_sync(0xffffffffu, min(act0 ? fkey(z0) : kmin, act1 ? fkey(z1) : kmin)));
-    const float bhx = fkey_inv(__reduce_max_sync(0xffffffffu, max(act0 ? fkey(x0) : kmax, act1 ? fkey(x1) : kmax)));
-    const float bhy = fkey_inv(__reduce_max_sync(0xffffffffu, max(act0 ? fkey(y0) : kmax, act1 ? fkey(y1) : kmax)));
-    const float bhz = fkey_inv(__reduce_max_sync(0xffffffffu, max(act0 ? fkey(z0) : kmax, act1 ? fkey(z1) : kmax)));
-    // compensated sums (Kahan), updated only for in-support terms
-    float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
-    int nc = 0;
-    auto flush = [&]() {
-      __syncwarp();
-#pragma unroll 2
-      for (int t = 0; t < nc; ++t) {
-        const float4 x = cx4[t], ga = ca4[t], gb = cb4[t], lo = cl4[t];
-        {
-          float u0, u1, u2;
-          amul(ga, gb, (x0 - x.x) - lo.x, (y0 - x.y) - lo.y, (z0 - x.z) - lo.z, u0, u1, u2);
-          const float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
-          const float y = __fsub_rn(gb.z * bspline_s2(s2), c0);
-          const float tt = __fadd_rn(s0, y);
-          const float cn = __fsub_rn(__fsub_rn(tt, s0), y);
-          const bool hit = act0 && s2 < 4.0f;
-          s0 = hit ? tt : s0;
-          c0 = hit ? cn : c0;
-        }
-        if (two) {
-          float u0, u1, u2;
-          amul(ga, gb, (x1 - x.x) - lo.x, (y1 - x.y) - lo.y, (z1 - x.z) - lo.z, u0, u1, u2);
-          const float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
-          const float y = __fsub_rn(gb.z * bspline_s2(s2), c1);
-          const float tt = __fadd_rn(s1, y);
-          const float cn = __fsub_rn(__fsub_rn(tt, s1), y);
-          const bool hit = act1 && s2 < 4.0f;
-          s1 = hit ? tt : s1;
-          c1 = hit ? cn : c1;
-        }
-      }
-      __syncwarp();
-      nc = 0;
-    };
-    for (int dz = -1; dz <= 1; ++dz)
-      for (int dy = -1; dy <= 1; ++dy) {
-        int s, e;
-        if (!nb_row(a.g, cx, cy + dy, cz + dz, &s, &e)) continue;
-        pairs += (long long)(e - s) * ((act0 ? 1 : 0) + (act1 ? 1 : 0));
-        for (int j0 = s; j0 < e; j0 += 32) {
-          const int j = j0 + lane;
-          bool pass = false;
-          float4 x;
-          if (j < e) {
-            x = __ldg(a.P.xm + j);
-            const float ex = fmaxf(fmaxf(blx - x.x, x.x - bhx), 0.f);
-            const float ey = fmaxf(fmaxf(bly - x.y, x.y - bhy), 0.f);
-            const float ez = fmaxf(fmaxf(blz - x.z, x.z - bhz), 0.f);
-            pass = fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < x.w;
-          }
-          const unsigned pm = __ballot_sync(0xffffffffu, pass);
-          if (pass) {
-            const int p = nc + __popc(pm & lt);
-            cx4[p] = x;
-            ca4[p] = __ldg(a.P.ga + j);
-            cb4[p] = __ldg(a.P.gb + j);
-            cl4[p] = __ldg(a.P.xlo + j);
-          }
-          nc += __popc(pm);
-          if (nc > kCandBuf - 32) flush();
-        }
-      }
-    flush();
-    if (act0) qval[q0] = a.iso - s0;
-    if (act1) qval[q1] = a.iso - s1;
+    cell_of(a.g, __shfl_sync(0xffffffffu, x[0], 0), __shfl_sync(0xffffffffu, y[0], 0),
+            __shfl_sync(0xffffffffu, z[0], 0), cx, cy, cz);
+    float sum[2];
+    chunk_field<2>(a.g, a.P, cx, cy, cz, x, y, z, act, slots, st, sum, pairs);
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+      if (act[m]) qval[q[m]] = a.iso - sum[m];
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);

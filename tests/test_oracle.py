@@ -182,3 +182,35 @@ def test_stable_and_std_sort_agree_on_cells():
     il_a, il_b = a.index_list(), b.index_list()
     for s0, e0 in zip(sa, ea):
         assert sorted(il_a[s0:e0]) == sorted(il_b[s0:e0])
+
+
+def test_uniform_grid_lattice_and_values():
+    """UniformGrid (src/marching.cpp:42-93) in the oracle: the resized box,
+    steps and dims follow the reference's float expressions, and each grid
+    value is SingleEval at its lattice point."""
+    fr = synth.small_blob(n=600, seed=21)
+    o = O.OracleFrame(fr.xyz, fr.radius)
+    for s in (1, 2, 3):
+        o.stage(s)
+    box, steps, dims = o.uniform_grid()
+    f32 = np.float32
+    xyz = fr.xyz
+    r = f32(fr.radius)
+    for a in range(3):
+        mn, mx = xyz[:, a].min(), xyz[:, a].max()
+        center = (mn + mx) / f32(2)
+        length = mx - mn
+        rl = f32(np.ceil(length / r)) * r + r * f32(4)
+        assert box[2 * a] == center - rl / f32(2) and box[2 * a + 1] == center + rl / f32(2)
+        assert steps[a] == int(rl / r) and dims[a] == steps[a] + 1
+    vals = o.grid_sample()
+    rng = np.random.default_rng(0)
+    idx = [tuple(int(rng.integers(d)) for d in dims[::-1]) for _ in range(50)]
+
+    def coord(a, i):
+        st = f32(steps[a])
+        return f32(f32(st - f32(i)) / st) * box[2 * a] + f32(f32(i) / st) * box[2 * a + 1]
+
+    pts = np.array([[coord(0, x), coord(1, y), coord(2, z)] for z, y, x in idx], np.float32)
+    ev = o.eval(pts)
+    np.testing.assert_array_equal(np.array([vals[k] for k in idx]), ev)
