@@ -1,7 +1,8 @@
 // pisurf.hpp - C++ facade with the reference's class and method names.
 //
 // Host code written against LCM1999/ParticleIsosurface's in-process API
-// (SurfReconstructor, Evaluator, HashGrid, TNode, Mesh, writeObjFile) calls
+// (SurfReconstructor, Evaluator, HashGrid, TNode, Mesh, writeObjFile,
+// UniformGrid) calls
 // the GPU library through these header-only classes.  They hold no
 // computation of their own: every call goes through the C ABI of pisurf.h,
 // so the library (libpisurf.so) does the work on the GPU and errors come back
@@ -22,6 +23,7 @@
 //   TNode               include/iso_method_ours.h:30-78
 //   Mesh, Vertex, Triangle  include/global.h:13-60, 86-115
 //   writeObjFile        src/main.cpp:54-67
+//   UniformGrid         include/marching.h:18-70 (dense-grid mode)
 #ifndef PISURF_HPP
 #define PISURF_HPP
 
@@ -471,9 +473,59 @@ class SurfReconstructor {
   std::shared_ptr<TNode> root_;
 };
 
+// UniformGrid (include/marching.h:18-70, src/marching.cpp), constant radius:
+// Run samples the field on the lattice of spacing r over the particles' box
+// (resizeRootBoxConstR) into _Scalars (x fastest) and, given a file name,
+// writes <filepath>/<filename>.vti as the reference does through VTK.
+class UniformGrid {
+ public:
+  UniformGrid(const std::vector<Vector3f>& particles, float radius, int device = 0)
+      : _RADIUS(radius), device_(device) {
+    _GlobalParticlesNum = (int)particles.size();
+    xyz_.resize(particles.size() * 3);
+    for (size_t i = 0; i < particles.size(); ++i)
+      for (int c = 0; c < 3; ++c) xyz_[3 * i + c] = particles[i][c];
+  }
+  float _RADIUS = 0.f;
+  float _SMOOTH_FACTOR = 2.0f;
+  int _GlobalParticlesNum = 0;
+  float _BoundingBox[6] = {0, 0, 0, 0, 0, 0};
+  int dims[3] = {0, 0, 0};
+  int steps[3] = {0, 0, 0};
+  std::vector<float> _Scalars;
+
+  // The reference computes its own iso value and ignores iso_value.
+  void Run(float iso_value, const std::string& filename = "", const std::string& filepath = ".") {
+    (void)iso_value;
+    pi_params p;
+    pi_params_default(&p);
+    p.radius = _RADIUS;
+    p.smooth_factor = _SMOOTH_FACTOR;
+    frame_ = std::make_shared<detail::Frame>(detail::Context::get(device_), p);
+    check(pi_frame_upload(frame_->h, xyz_.data(), (int64_t)(xyz_.size() / 3)));
+    check(pi_hashgrid_build(frame_->h));
+    check(pi_aniso_compute(frame_->h));
+    check(pi_normals_compute(frame_->h));
+    int64_t n = 0;
+    check(pi_grid_dims(frame_->h, dims, _BoundingBox, &n));
+    for (int i = 0; i < 3; ++i) steps[i] = dims[i] - 1;
+    _Scalars.assign((size_t)n, 0.f);
+    check(pi_grid_sample(frame_->h, _Scalars.data(), n));
+    if (!filename.empty()) check(pi_grid_write_vti(frame_->h, (filepath + "/" + filename + ".vti").c_str()));
+  }
+  float getIsoValue() const { return frame_ ? frame_->info().iso_value : 0.f; }
+  float getMaxScalar() const { return frame_ ? frame_->info().max_scalar : 0.f; }
+
+ private:
+  std::vector<float> xyz_;
+  int device_ = 0;
+  std::shared_ptr<detail::Frame> frame_;
+};
+
 }  // namespace pisurf
 
 #ifndef PISURF_NO_GLOBAL_NAMES
+using pisurf::UniformGrid;
 using pisurf::Evaluator;
 using pisurf::HashGrid;
 using pisurf::Mesh;

@@ -170,3 +170,46 @@ class SurfReconstructor:
 
     def frame_info(self):
         return self._info()
+
+
+class UniformGrid:
+    """UniformGrid (include/marching.h:18-70, src/marching.cpp), constant
+    radius: Run samples the field on the lattice of spacing r over the
+    particles' box (resizeRootBoxConstR) and writes it as a VTK image
+    <filepath>/<filename>.vti; the values stay in `_Scalars` (x fastest, as
+    the reference stores them) and `dims`, `steps`, `_BoundingBox` describe
+    the lattice."""
+
+    def __init__(self, particles, radius, ctx: N.Context | None = None):
+        self._GlobalParticles = np.ascontiguousarray(np.asarray(particles, np.float32).reshape(-1, 3))
+        self._GlobalParticlesNum = int(self._GlobalParticles.shape[0])
+        self._RADIUS = float(radius)
+        self._ctx = ctx or default_context()
+        self._SMOOTH_FACTOR = 2.0
+        self._frame = None
+        self.dims = np.zeros(3, np.int32)
+        self.steps = np.zeros(3, np.int32)
+        self._BoundingBox = np.zeros(6, np.float32)
+        self._Scalars = np.zeros(0, np.float32)
+
+    def Run(self, iso_value=0.0, filename=None, filepath="."):
+        """The reference computes its own iso value (RecommendIsoValueConstR)
+        and ignores iso_value, as here."""
+        params = N.default_params(self._RADIUS, smooth_factor=self._SMOOTH_FACTOR)
+        self._frame = N.Frame(self._ctx, params).upload(self._GlobalParticles)
+        self._frame.hashgrid().aniso().normals()
+        dims, box, _ = self._frame.grid_dims()
+        self.dims = dims
+        self.steps = dims - 1
+        self._BoundingBox = box
+        self._Scalars = self._frame.grid_sample().ravel()
+        if filename:
+            import os
+            self._frame.write_vti(os.path.join(filepath, filename + ".vti"))
+        return self._Scalars
+
+    def getIsoValue(self):
+        return self._frame.info()["iso_value"]
+
+    def getMaxScalar(self):
+        return self._frame.info()["max_scalar"]

@@ -1,6 +1,7 @@
 // Host program written against the reference's C++ API (the calls of
 // runOurs, src/main.cpp:330-405), compiled against include/pisurf.hpp.
 //   facade_main <xyz float32 file> <n> <radius> <out.obj>
+// (also writes <out.obj's directory>/grid.vti through UniformGrid)
 // Prints one JSON line; exits 3 when no CUDA device is usable (the library
 // has no CPU fallback).
 #include <cstdio>
@@ -79,12 +80,22 @@ int main(int argc, char** argv) {
       for (auto& c : t->children)
         if (c) stack.push_back(c);
     }
+    // the dense-grid mode (UniformGrid::Run writes <dir>/grid.vti)
+    std::string out_obj = argv[4];
+    const size_t slash = out_obj.find_last_of('/');
+    const std::string dir = slash == std::string::npos ? std::string(".") : out_obj.substr(0, slash);
+    UniformGrid ug(particles, radius);
+    ug.Run(0.0f, "grid", dir);
+    double gsum = 0.0;
+    for (float v : ug._Scalars) gsum += v;
     std::printf(
         "{\"vertices\": %u, \"triangles\": %u, \"depth_max\": %d, \"depth_min\": %d, \"iso\": %.9g, "
         "\"max_scalar\": %.9g, \"scalar0\": %.9g, \"neighbors0\": %zu, \"key0\": %lld, \"in_box\": %zu, "
-        "\"grid_sign_change\": %d, \"nodes\": %ld, \"leaves\": %ld}\n",
+        "\"grid_sign_change\": %d, \"nodes\": %ld, \"leaves\": %ld, \"grid_dims\": [%d, %d, %d], "
+        "\"grid_points\": %zu}\n",
         mesh.verticesNum, mesh.trianglesNum, constructor.getDepthMax(), constructor.getDepthMin(), ev->getIsoValue(),
-        ev->getMaxScalar(), s0, nb.size(), key0, inbox.size(), signchange ? 1 : 0, nodes, leaves);
+        ev->getMaxScalar(), s0, nb.size(), key0, inbox.size(), signchange ? 1 : 0, nodes, leaves, ug.dims[0],
+        ug.dims[1], ug.dims[2], ug._Scalars.size());
   } catch (const pisurf::Error& e) {
     std::printf("{\"error\": %d, \"message\": \"%s\"}\n", e.code(), e.what());
     return e.code() == PI_ERR_CUDA ? 3 : 1;

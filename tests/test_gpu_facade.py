@@ -31,8 +31,16 @@ def test_facade_obj_identical_to_library_writer(tmp_path):
     f.write_obj(str(tmp_path / "lib.obj"))
     info = f.info()
     f.close()
-    ctx.close()
     assert (tmp_path / "facade.obj").read_bytes() == (tmp_path / "lib.obj").read_bytes()
+    # UniformGrid through the facade writes the library's VTK image
+    fg = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz)
+    fg.hashgrid().aniso().normals()
+    fg.write_vti(str(tmp_path / "lib_grid.vti"))
+    dims, _, npts = fg.grid_dims()
+    fg.close()
+    ctx.close()
+    assert (tmp_path / "grid.vti").read_bytes() == (tmp_path / "lib_grid.vti").read_bytes()
+    assert out["grid_dims"] == [int(d) for d in dims] and out["grid_points"] == npts
     assert out["vertices"] == info["num_vertices"] and out["triangles"] == info["num_triangles"]
     assert out["depth_max"] == info["depth_max"] and out["nodes"] == info["num_nodes"]
 
