@@ -181,6 +181,26 @@ int pi_grid_sample(pi_frame* f, float* values, int64_t cap);
 int pi_grid_sample_device(pi_frame* f, float* d_values, int64_t cap);
 int pi_grid_write_vti(pi_frame* f, const char* path);
 
+/* Host data formats (no GPU needed).
+ * pi_load_csv: loadParticlesFromCSV (src/main.cpp:215-275).  The header's
+ * quote marks are removed and it is split at ','; the x, y and z columns are
+ * the first titles matching the reference's case-insensitive patterns
+ * ^(.*(:|_|-)( *)(x|0)("*)|x)$ (likewise y|1, z|2), the radius column (read
+ * when radius is not null) the first matching ^((.*)radius|r)$.  Rows follow
+ * until the first empty line, each value parsed as std::stof.  Call with
+ * xyz = radius = null to count rows (*n); cols4 (may be null) receives the
+ * x, y, z, radius column indices (-1 when the radius was not asked for).
+ * PI_ERR_INVALID when a column is missing or a value does not parse (the
+ * reference exits or throws there); PI_ERR_LIMIT when cap < rows.
+ * pi_write_ply / pi_mesh_write_ply: writePlyFile (src/main.cpp:69-114), the
+ * RPly binary file in the host byte order: "float32" x y z per vertex and a
+ * "uchar"-counted "int" list per face with 0-based indices (tris given
+ * 0-based, or 1-based when one_based is set). */
+int pi_load_csv(const char* path, float* xyz, float* radius, int64_t cap, int64_t* n, int32_t* cols4);
+int pi_write_ply(const char* path, const float* verts, int64_t nv, const int32_t* tris, int64_t nt,
+                 int32_t one_based);
+int pi_mesh_write_ply(pi_frame* f, const char* path);
+
 /* One call, host in / host out: upload, Run, download (the e2e path of a
  * frame).  verts/tris must hold max_verts / max_tris entries; the actual
  * counts are returned (PI_ERR_LIMIT if the buffers are too small). */

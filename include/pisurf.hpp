@@ -23,6 +23,7 @@
 //   TNode               include/iso_method_ours.h:30-78
 //   Mesh, Vertex, Triangle  include/global.h:13-60, 86-115
 //   writeObjFile        src/main.cpp:54-67
+//   writePlyFile, loadParticlesFromCSV  src/main.cpp:69-114, 215-275
 //   UniformGrid         include/marching.h:18-70 (dense-grid mode)
 #ifndef PISURF_HPP
 #define PISURF_HPP
@@ -124,6 +125,31 @@ inline void writeObjFile(Mesh& m, const std::string& fn) {
   for (const Vertex& p : m.vertices) std::fprintf(f, "v %f %f %f\n", p[0], p[1], p[2]);
   for (const Triangle& t : m.tris) std::fprintf(f, "f %d %d %d\n", t.v[0], t.v[1], t.v[2]);
   std::fclose(f);
+}
+
+// writePlyFile (src/main.cpp:69-114): binary PLY as RPly writes it.
+inline void writePlyFile(Mesh& m, const std::string& fn) {
+  std::vector<float> v(m.vertices.size() * 3);
+  std::vector<int32_t> t(m.tris.size() * 3);
+  for (size_t i = 0; i < m.vertices.size(); ++i)
+    for (int k = 0; k < 3; ++k) v[3 * i + k] = m.vertices[i][k];
+  for (size_t i = 0; i < m.tris.size(); ++i)
+    for (int k = 0; k < 3; ++k) t[3 * i + k] = m.tris[i].v[k];
+  check(pi_write_ply(fn.c_str(), v.data(), (int64_t)m.vertices.size(), t.data(), (int64_t)m.tris.size(), 1));
+}
+
+// loadParticlesFromCSV (src/main.cpp:215-275); radiuses are read when
+// is_const_radius is false (the reference's IS_CONST_RADIUS).
+inline void loadParticlesFromCSV(const std::string& csvPath, std::vector<Vector3f>& particles,
+                                 std::vector<float>& radiuses, bool is_const_radius = true) {
+  int64_t n = 0;
+  check(pi_load_csv(csvPath.c_str(), nullptr, nullptr, 0, &n, nullptr));
+  std::vector<float> xyz((size_t)n * 3);
+  std::vector<float> rad(is_const_radius ? 0 : (size_t)n);
+  check(pi_load_csv(csvPath.c_str(), xyz.data(), is_const_radius ? nullptr : rad.data(), n, &n, nullptr));
+  particles.resize((size_t)n);
+  for (int64_t i = 0; i < n; ++i) particles[i] = Vector3f(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+  if (!is_const_radius) radiuses = rad;
 }
 
 namespace detail {
@@ -533,7 +559,9 @@ using pisurf::SurfReconstructor;
 using pisurf::TNode;
 using pisurf::Triangle;
 using pisurf::Vertex;
+using pisurf::loadParticlesFromCSV;
 using pisurf::writeObjFile;
+using pisurf::writePlyFile;
 #endif
 
 #endif  // PISURF_HPP

@@ -94,6 +94,9 @@ def _declare(L):
         "pi_mesh_write_obj": (C.c_int, [P, C.c_char_p]),
         "pi_eval_field": (C.c_int, [P, fp, i64, fp, fp]),
         "pi_grid_dims": (C.c_int, [P, C.POINTER(C.c_int32), fp, pi64]),
+        "pi_load_csv": (C.c_int, [C.c_char_p, fp, fp, i64, pi64, C.POINTER(C.c_int32)]),
+        "pi_write_ply": (C.c_int, [C.c_char_p, fp, i64, C.POINTER(C.c_int32), i64, C.c_int32]),
+        "pi_mesh_write_ply": (C.c_int, [P, C.c_char_p]),
         "pi_grid_sample": (C.c_int, [P, fp, i64]),
         "pi_grid_sample_device": (C.c_int, [P, C.c_void_p, i64]),
         "pi_grid_write_vti": (C.c_int, [P, C.c_char_p]),
@@ -147,6 +150,27 @@ def dmc_table():
     c = np.zeros(256, np.int32)
     check(lib().pi_dmc_table(ptr(t, C.c_int32), ptr(f, C.c_int8), ptr(c, C.c_int32)))
     return t, f.astype(bool), c
+
+
+def load_csv(path, radius=False):
+    """loadParticlesFromCSV: (xyz float32 [n, 3], radius float32 [n] or None,
+    column indices x, y, z, radius)."""
+    n = C.c_int64()
+    cols = np.zeros(4, np.int32)
+    check(lib().pi_load_csv(str(path).encode(), None, None, 0, C.byref(n), ptr(cols, C.c_int32)))
+    xyz = np.empty((n.value, 3), np.float32)
+    rad = np.empty(n.value, np.float32) if radius else None
+    check(lib().pi_load_csv(str(path).encode(), ptr(xyz, C.c_float), ptr(rad, C.c_float) if radius else None,
+                            n.value, C.byref(n), ptr(cols, C.c_int32)))
+    return xyz, rad, cols
+
+
+def write_ply(path, verts, tris, one_based=False):
+    """writePlyFile: binary PLY (float32 vertices, uchar/int face lists)."""
+    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(tris, np.int32).reshape(-1, 3)
+    check(lib().pi_write_ply(str(path).encode(), ptr(v, C.c_float), v.shape[0], ptr(t, C.c_int32), t.shape[0],
+                             1 if one_based else 0))
 
 
 class Context:
@@ -310,6 +334,9 @@ class Frame:
 
     def grid_sample_device(self, d_ptr, cap):
         check(lib().pi_grid_sample_device(self.h, C.c_void_p(d_ptr), cap))
+
+    def write_ply(self, path):
+        check(lib().pi_mesh_write_ply(self.h, path.encode()))
 
     def write_vti(self, path):
         check(lib().pi_grid_write_vti(self.h, path.encode()))

@@ -651,6 +651,41 @@ int pi_grid_write_vti(pi_frame* f, const char* path) {
   PI_API_END
 }
 
+int pi_load_csv(const char* path, float* xyz, float* radius, int64_t cap, int64_t* n, int32_t* cols4) {
+  PI_API_BEGIN
+  PI_CHECK(path && n, "bad arguments");
+  int cols[4];
+  const long long rows = load_csv(path, xyz, radius, xyz ? cap : 0, cols);
+  *n = rows;
+  if (cols4)
+    for (int i = 0; i < 4; ++i) cols4[i] = cols[i];
+  if (xyz && rows > cap) throw std::length_error("buffer holds fewer rows than the file");
+  PI_API_END
+}
+
+int pi_write_ply(const char* path, const float* verts, int64_t nv, const int32_t* tris, int64_t nt,
+                 int32_t one_based) {
+  PI_API_BEGIN
+  PI_CHECK(path && nv >= 0 && nt >= 0 && (verts || nv == 0) && (tris || nt == 0), "bad arguments");
+  write_ply(path, verts, nv, tris, nt, one_based);
+  PI_API_END
+}
+
+int pi_mesh_write_ply(pi_frame* f, const char* path) {
+  PI_API_BEGIN
+  PI_CHECK(f && path, "bad arguments");
+  need(f, 6);
+  set_device(f->ctx);
+  cudaStream_t s = f->ctx->stream;
+  std::vector<float> v((size_t)f->nV * 3);
+  std::vector<int32_t> t((size_t)f->nT * 3);
+  if (f->nV) PI_CUDA(cudaMemcpyAsync(v.data(), f->mv.p, sizeof(float) * v.size(), cudaMemcpyDeviceToHost, s));
+  if (f->nT) PI_CUDA(cudaMemcpyAsync(t.data(), f->mt.p, sizeof(int32_t) * t.size(), cudaMemcpyDeviceToHost, s));
+  PI_CUDA(cudaStreamSynchronize(s));
+  write_ply(path, v.data(), f->nV, t.data(), f->nT, 0);
+  PI_API_END
+}
+
 int pi_hashgrid_neighbors(pi_frame* f, const float* pts, int64_t m, int64_t* offsets, int32_t* idx, int64_t cap,
                           int64_t* total) {
   PI_API_BEGIN

@@ -129,6 +129,11 @@ void qef_level(pi_frame* f, long long lb, long long le);
 // x fastest) when cap holds it; returns the number of lattice points.
 void uniform_grid_host(const pi_frame* f, float box[6], int steps[3], int dims[3]);
 long long grid_sample(pi_frame* f, float* d_out, long long cap);
+// Host formats: CSV particles (returns the row count; fills xyz / radius up
+// to cap rows; cols = x, y, z, radius column indices) and binary PLY meshes.
+long long load_csv(const char* path, float* xyz, float* radius, long long cap, int cols[4]);
+void write_ply(const char* path, const float* verts, long long nv, const int32_t* tris, long long nt,
+               int one_based);
 void eval_points(pi_frame* f, const float* d_pts, long long m, float* d_val, float* d_grad);
 long long neighbors(pi_frame* f, const float* h_pts, long long m, long long* h_off, int* h_idx,
                     long long cap);

@@ -59,6 +59,19 @@ def writeObjFile(mesh: Mesh, fn: str):
             f.write("f %d %d %d\n" % (t[0], t[1], t[2]))
 
 
+def writePlyFile(mesh: Mesh, fn: str):
+    """writePlyFile (src/main.cpp:69-114): binary PLY, float32 vertices and
+    0-based int face lists (mesh.tris are 1-based as in the reference)."""
+    N.write_ply(fn, mesh.vertices, mesh.tris, one_based=True)
+
+
+def loadParticlesFromCSV(csv_path, is_const_radius=True):
+    """loadParticlesFromCSV (src/main.cpp:215-275): (particles [n, 3] float32,
+    radiuses [n] float32, empty when is_const_radius)."""
+    xyz, rad, _ = N.load_csv(csv_path, radius=not is_const_radius)
+    return xyz, (rad if rad is not None else np.zeros(0, np.float32))
+
+
 class HashGrid:
     def __init__(self, frame: N.Frame):
         self._f = frame

@@ -1,7 +1,8 @@
 // Host program written against the reference's C++ API (the calls of
 // runOurs, src/main.cpp:330-405), compiled against include/pisurf.hpp.
-//   facade_main <xyz float32 file> <n> <radius> <out.obj>
-// (also writes <out.obj's directory>/grid.vti through UniformGrid)
+//   facade_main <xyz float32 file | particles .csv> <n> <radius> <out.obj>
+// (also writes <out.obj>.ply, and <out.obj's directory>/grid.vti through
+// UniformGrid)
 // Prints one JSON line; exits 3 when no CUDA device is usable (the library
 // has no CPU fallback).
 #include <cstdio>
@@ -18,22 +19,35 @@ int main(int argc, char** argv) {
   }
   const long n = std::atol(argv[2]);
   const float radius = (float)std::atof(argv[3]);
-  std::vector<float> raw((size_t)n * 3);
-  std::ifstream in(argv[1], std::ios::binary);
-  in.read(reinterpret_cast<char*>(raw.data()), (std::streamsize)(raw.size() * sizeof(float)));
-  if (!in) {
-    std::fprintf(stderr, "cannot read %s\n", argv[1]);
-    return 2;
+  std::vector<pisurf::Vector3f> particles;
+  std::vector<float> radiuses;
+  const std::string src = argv[1];
+  if (src.size() > 4 && src.substr(src.size() - 4) == ".csv") {
+    try {
+      loadParticlesFromCSV(src, particles, radiuses, true);
+    } catch (const pisurf::Error& e) {
+      std::printf("{\"error\": %d, \"message\": \"%s\"}\n", e.code(), e.what());
+      return 1;
+    }
+  } else {
+    std::vector<float> raw((size_t)n * 3);
+    std::ifstream in(argv[1], std::ios::binary);
+    in.read(reinterpret_cast<char*>(raw.data()), (std::streamsize)(raw.size() * sizeof(float)));
+    if (!in) {
+      std::fprintf(stderr, "cannot read %s\n", argv[1]);
+      return 2;
+    }
+    particles.resize((size_t)n);
+    for (long i = 0; i < n; ++i) particles[i] = pisurf::Vector3f(raw[3 * i], raw[3 * i + 1], raw[3 * i + 2]);
   }
-  std::vector<pisurf::Vector3f> particles((size_t)n);
-  for (long i = 0; i < n; ++i) particles[i] = pisurf::Vector3f(raw[3 * i], raw[3 * i + 1], raw[3 * i + 2]);
-  std::vector<float> radiuses((size_t)n, radius);
+  radiuses.assign(particles.size(), radius);
 
   Mesh mesh;
   try {
     SurfReconstructor constructor(particles, radiuses, &mesh, radius);
     constructor.Run(1.9f, 2.0f);
     writeObjFile(mesh, argv[4]);
+    writePlyFile(mesh, std::string(argv[4]) + ".ply");
 
     std::shared_ptr<Evaluator> ev = constructor.getEvaluator();
     std::shared_ptr<HashGrid> hg = constructor.getHashGrid();

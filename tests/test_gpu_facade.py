@@ -30,8 +30,17 @@ def test_facade_obj_identical_to_library_writer(tmp_path):
     f = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz).run()
     f.write_obj(str(tmp_path / "lib.obj"))
     info = f.info()
-    f.close()
     assert (tmp_path / "facade.obj").read_bytes() == (tmp_path / "lib.obj").read_bytes()
+    f.write_ply(str(tmp_path / "lib.ply"))
+    assert (tmp_path / "facade.obj.ply").read_bytes() == (tmp_path / "lib.ply").read_bytes()
+    # the same particles through loadParticlesFromCSV give the same mesh
+    csv = tmp_path / "p.csv"
+    csv.write_text('"Points:0","Points:1","Points:2"\n' + "\n".join("%.9g,%.9g,%.9g" % tuple(p) for p in fr.xyz) + "\n")
+    r2 = subprocess.run([exe, str(csv), "0", repr(fr.radius), str(tmp_path / "csv.obj")],
+                        capture_output=True, text=True, timeout=300)
+    assert r2.returncode == 0, r2.stdout + r2.stderr
+    assert (tmp_path / "csv.obj").read_bytes() == (tmp_path / "lib.obj").read_bytes()
+    f.close()
     # UniformGrid through the facade writes the library's VTK image
     fg = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz)
     fg.hashgrid().aniso().normals()
