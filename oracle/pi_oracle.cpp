@@ -585,6 +585,13 @@ struct Evaluator {
       for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) cov(i, j) += (wd[i] * wd[j]) * wj;
     }
+    if (!(wSum > R(0))) {
+      // no candidate within 4r: the reference divides by zero here (its G is
+      // NaN); the identity is used, as for particles with <= 2 candidates
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) G(i, j) = (i == j) ? R(1) : R(0);
+      return;
+    }
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) cov(i, j) /= wSum;
     M3<R> u, v;
@@ -757,7 +764,10 @@ struct Frame : FrameBase {
     float r = radius;
     float maxLen = std::max({(BoundingBox[1] - BoundingBox[0]), (BoundingBox[3] - BoundingBox[2]),
                              (BoundingBox[5] - BoundingBox[4])});
-    DEPTH_MAX = int(std::ceil(std::log2(std::ceil(maxLen / r))));
+    // all particles at one point: log2(0) leaves the reference's depth
+    // undefined; the search then starts at depth 0 (as the library does)
+    const float cells = std::ceil(maxLen / r);
+    DEPTH_MAX = cells >= 1.0f ? int(std::ceil(std::log2(cells))) : 0;
     float resizeLen = (float)(std::pow(2, DEPTH_MAX) * r);
     while (resizeLen - maxLen < (ev._NEIGHBOR_FACTOR * radius * 2)) {
       DEPTH_MAX++;

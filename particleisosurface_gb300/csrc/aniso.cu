@@ -187,19 +187,27 @@ __global__ void k_cov_G(GridView g, const float4* __restrict__ pos, const float4
   float iw = 1.0f / ws.s;
   float a6[6] = {(h2 + c00.s) * iw, c01.s * iw, c02.s * iw, (h2 + c11.s) * iw, c12.s * iw, (h2 + c22.s) * iw};
   float w[3], V[3][3];
-  sym_eig3<float>(a6, w, V);
   float G[9], stretch;
-  float aw0 = fabsf(w[0]), aw1 = fabsf(w[1]), aw2 = fabsf(w[2]);
-  float wmx = fmaxf(aw0, fmaxf(aw1, aw2)), wmn = fminf(aw0, fminf(aw1, aw2));
-  bool degenerate = wmn < 0.25f * wmx;
-  if (degenerate) {
-    double a6d[6], wd[3], Vd[3][3];
-    for (int k = 0; k < 6; ++k) a6d[k] = (double)a6[k];
-    sym_eig3<double>(a6d, wd, Vd);
-    g_from_eig<double>(wd, Vd, G, &stretch);
-    stripe_add(f64count, 0, 1ull);
+  bool degenerate = false;
+  if (!(ws.s > 0.f)) {
+    // no candidate within 4r: the reference divides by zero here (its G is
+    // NaN); the identity is used, as for particles with <= 2 candidates
+    for (int k = 0; k < 9; ++k) G[k] = (k % 4 == 0) ? 1.0f : 0.0f;
+    stretch = 1.0f;
   } else {
-    g_from_eig<float>(w, V, G, &stretch);
+    sym_eig3<float>(a6, w, V);
+    float aw0 = fabsf(w[0]), aw1 = fabsf(w[1]), aw2 = fabsf(w[2]);
+    float wmx = fmaxf(aw0, fmaxf(aw1, aw2)), wmn = fminf(aw0, fminf(aw1, aw2));
+    degenerate = wmn < 0.25f * wmx;
+    if (degenerate) {
+      double a6d[6], wd[3], Vd[3][3];
+      for (int k = 0; k < 6; ++k) a6d[k] = (double)a6[k];
+      sym_eig3<double>(a6d, wd, Vd);
+      g_from_eig<double>(wd, Vd, G, &stretch);
+      stripe_add(f64count, 0, 1ull);
+    } else {
+      g_from_eig<float>(w, V, G, &stretch);
+    }
   }
   // Matrix3f::determinant, cofactors along the first row
   float det = G[0] * (G[4] * G[8] - G[5] * G[7]) - G[1] * (G[3] * G[8] - G[5] * G[6]) +

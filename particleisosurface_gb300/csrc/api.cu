@@ -142,7 +142,10 @@ static void host_root_and_scalars(pi_frame* f) {
   const float r = f->P.radius;
   const float* bb = f->bbox6;
   float maxLen = std::max({(bb[1] - bb[0]), (bb[3] - bb[2]), (bb[5] - bb[4])});
-  int dmax = int(std::ceil(std::log2(std::ceil(maxLen / r))));
+  // all particles at one point: log2(0) would make the reference's depth
+  // undefined; the search then starts at depth 0
+  const float cells = std::ceil(maxLen / r);
+  int dmax = cells >= 1.0f ? int(std::ceil(std::log2(cells))) : 0;
   float resizeLen = (float)(std::pow(2, dmax) * r);
   while (resizeLen - maxLen < (4.0f * r * 2)) {
     dmax++;

@@ -1,0 +1,69 @@
+"""Degenerate inputs on the GPU against the oracle: a single particle, ten
+coincident particles (zero extent: the depth search starts at 0), particles on
+a line and on a one-layer sheet (flat axes: one hash cell across, D_min =
+D_max - 1; the line's last particle lies on the grid's upper bound, gets key
+-1 and has no candidate within 4r, so its G is the identity), and a
+non-finite coordinate (PI_ERR_INVALID)."""
+import numpy as np
+import pytest
+
+import parity as PR
+import pyoracle as O
+from particleisosurface_gb300 import _native as N
+from particleisosurface_gb300 import build as B
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "one": lambda: np.zeros((1, 3), np.float32) + 0.3,
+    "coincident": lambda: np.zeros((10, 3), np.float32) + 0.3,
+    "line": lambda: np.stack([np.linspace(0, 0.2, 11), np.zeros(11), np.zeros(11)], -1).astype(np.float32),
+    "sheet": lambda: np.stack(np.meshgrid(np.arange(12) * 0.02, np.arange(12) * 0.02, [0.1], indexing="ij"),
+                              -1).reshape(-1, 3).astype(np.float32),
+}
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    B.build()
+    O.build()
+    c = N.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_degenerate_frame_matches_oracle(ctx, name):
+    xyz = CASES[name]()
+    r = 0.01
+    o = O.OracleFrame(xyz, r).run()
+    g = N.Frame(ctx, N.default_params(r)).upload(xyz).run()
+    info = g.info()
+    d = o.depths()
+    assert (info["depth_max"], info["depth_min"]) == (d["depth_max"], d["depth_min"])
+    rep = PR.compare_octrees(o.nodes(), g.dump(N.DUMP_NODES), o, o.scalars()["max_scalar"], d["depth_min"])
+    print(name, {k: v for k, v in rep.items() if k not in ("leaf_far_pos", "leaf_far_gpu", "unexplained")},
+          rep["unexplained"][:4])
+    assert not rep["unexplained"] and rep["nodes_oracle"] == rep["nodes_gpu"]
+    vo, to, ko = o.mesh()
+    vg, tg, kg = g.mesh(keys=True)
+    mo = PR.canonical_mesh(vo, to, ko, one_based=True)
+    mg = PR.canonical_mesh(vg, tg, kg, one_based=False)
+    assert set(mo[0]) == set(mg[0]) and mo[1] == mg[1]
+    g.close()
+
+
+def test_non_finite_coordinate_rejected(ctx):
+    xyz = np.zeros((100, 3), np.float32)
+    xyz[:, 0] = np.arange(100) * 0.02
+    xyz[17, 1] = np.nan
+    f = N.Frame(ctx, N.default_params(0.01)).upload(xyz)
+    with pytest.raises(N.PiError) as e:
+        f.run()
+    assert e.value.code == N.PI_ERR_INVALID
+    f.close()
+    # the context still works afterwards
+    xyz[17, 1] = 0.0
+    f = N.Frame(ctx, N.default_params(0.01)).upload(xyz).run()
+    assert f.info()["num_nodes"] > 0
+    f.close()
