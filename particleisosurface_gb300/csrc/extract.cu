@@ -125,16 +125,31 @@ __device__ __forceinline__ uint32_t compact3(uint32_t v) {
 __global__ void k_corner_mark(const int* __restrict__ leaves, long long nl, const int4* __restrict__ nd_org,
                               int full, unsigned* __restrict__ bits) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nl * 8) return;
-  const int4 o = nd_org[leaves[t >> 3]];
-  const int k = (int)(t & 7);
-  const int x = o.x + ((k & 1) ? o.w : 0), y = o.y + ((k & 2) ? o.w : 0), z = o.z + ((k & 4) ? o.w : 0);
-  if (x <= 0 || x >= full || y <= 0 || y >= full || z <= 0 || z >= full) return;
-  const uint32_t idx = spread3((uint32_t)(x - 1)) | (spread3((uint32_t)(y - 1)) << 1) |
-                       (spread3((uint32_t)(z - 1)) << 2);
-  const unsigned bit = 1u << (idx & 31);
-  unsigned* w = bits + (idx >> 5);
-  if (!(__ldg(w) & bit)) atomicOr(w, bit);
+  const int lane = threadIdx.x & 31;
+  // one lane per corner; corners of sibling leaves fall in a few bitmap words,
+  // so the warp ORs its bits per word and issues one atomic per word
+  long long word = -1;
+  unsigned bit = 0u;
+  if (t < nl * 8) {
+    const int4 o = nd_org[leaves[t >> 3]];
+    const int k = (int)(t & 7);
+    const int x = o.x + ((k & 1) ? o.w : 0), y = o.y + ((k & 2) ? o.w : 0), z = o.z + ((k & 4) ? o.w : 0);
+    if (x > 0 && x < full && y > 0 && y < full && z > 0 && z < full) {
+      const uint32_t idx = spread3((uint32_t)(x - 1)) | (spread3((uint32_t)(y - 1)) << 1) |
+                           (spread3((uint32_t)(z - 1)) << 2);
+      word = idx >> 5;
+      bit = 1u << (idx & 31);
+    }
+  }
+  unsigned todo = __ballot_sync(0xffffffffu, word >= 0);
+  while (todo) {
+    const int leader = __ffs(todo) - 1;
+    const long long lw = __shfl_sync(0xffffffffu, word, leader);
+    const bool mine = word == lw;
+    const unsigned m = __reduce_or_sync(0xffffffffu, mine ? bit : 0u);
+    if (lane == leader && (__ldg(bits + lw) & m) != m) atomicOr(bits + lw, m);
+    todo &= ~__ballot_sync(0xffffffffu, mine);
+  }
 }
 
 __global__ void k_bitmap_count(const unsigned* __restrict__ bits, long long nw, int* __restrict__ cnt) {
@@ -278,10 +293,10 @@ __global__ void k_unique_write(const uint64_t* __restrict__ keys, const int* __r
   if (k != invalid && (i == 0 || keys[i - 1] != k)) out[scan[i]] = k;
 }
 
-// Leaf containing octant `oct` (bit set = + side) of lattice point (x, y, z).
+// Leaf containing octant `oct` (bit set = + side) of lattice point (x, y, z),
+// descending from `node` (which contains the octant's point).
 __device__ __forceinline__ int locate(int x, int y, int z, int oct, const int* __restrict__ nd_child,
-                                      const int4* __restrict__ nd_org) {
-  int node = 0;
+                                      const int4* __restrict__ nd_org, int node) {
   for (int guard = 0; guard < 64; ++guard) {
     int ch = nd_child[node];
     if (ch < 0) return node;
@@ -307,10 +322,21 @@ __global__ void k_dual(const uint64_t* __restrict__ verts, long long nu, int B, 
   const uint64_t key = verts[u];
   const uint64_t m = (1ull << B) - 1ull;
   const int x = (int)((key >> (2 * B)) & m), y = (int)((key >> B) & m), z = (int)(key & m);
+  // the eight octant points share the descent until the node one of whose
+  // mid-planes holds the corner; each octant continues from there
+  int start = 0;
+  for (int guard = 0; guard < 64; ++guard) {
+    const int ch = nd_child[start];
+    if (ch < 0) break;
+    const int4 o = nd_org[start];
+    const int mid = o.w >> 1;
+    if (x == o.x + mid || y == o.y + mid || z == o.z + mid) break;
+    start = ch + ((x > o.x + mid) ? 1 : 0) + ((y > o.y + mid) ? 2 : 0) + ((z > o.z + mid) ? 4 : 0);
+  }
   int n8[8];
   int index = 0;
   for (int c = 0; c < 8; ++c) {
-    n8[c] = locate(x, y, z, c, nd_child, nd_org);
+    n8[c] = locate(x, y, z, c, nd_child, nd_org, start);
     if (nd_v[n8[c]].w > 0.f) index |= 1 << c;
   }
   const int code = c_code[index];
