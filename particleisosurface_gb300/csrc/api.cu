@@ -5,11 +5,15 @@
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
+#include <cstdlib>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <string>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "internal.h"
 
@@ -181,10 +185,20 @@ static void need(const pi_frame* f, int stage) {
   if (f->stage < stage) throw StateError("stage called before the stages it depends on");
 }
 
+// An NVTX range per stage (names as the reference's printf stage titles), so
+// a timeline tool shows the stages; free when no tool is attached.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+
 static void run_stage(pi_frame* f, int target) {
   // target: 2 hash, 3 aniso, 4 normals, 5 octree, 6 mesh
   if (f->stage >= target) return;
   need(f, target - 1);
+  static const char* const names[7] = {"", "", "pisurf hash grid", "pisurf anisotropy", "pisurf normals",
+                                        "pisurf octree", "pisurf extraction"};
+  NvtxRange range(names[target]);
   ev_record(f, 0);
   switch (target) {
     case 2:
@@ -459,12 +473,35 @@ int pi_extract_mesh(pi_frame* f) {
   run_stage(f, 6);
   PI_API_END
 }
+// One JSON line per completed frame, appended to the file named by the
+// PISURF_METRICS environment variable (unset: nothing is written).  The
+// reference prints its stage times and frontier sizes instead
+// (src/surface_reconstructor.cpp:322-470).
+static void metrics_record(const pi_frame* f) {
+  static const char* path = std::getenv("PISURF_METRICS");
+  if (!path || !*path) return;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
+  FILE* fp = std::fopen(path, "a");
+  if (!fp) return;
+  std::fprintf(fp,
+               "{\"particles\": %lld, \"depth_max\": %d, \"nodes\": %lld, \"leaves\": %lld, "
+               "\"dual_cells\": %lld, \"vertices\": %lld, \"triangles\": %lld, \"field_evals\": %lld, "
+               "\"candidate_pairs\": %lld, \"qef_accepted\": %lld, \"stage_ms\": {\"hash\": %.4f, "
+               "\"aniso\": %.4f, \"normals\": %.4f, \"octree\": %.4f, \"extract\": %.4f}}\n",
+               f->N, f->dmax, f->nNodes, f->nLeaves, f->nDual, f->nV, f->nT, f->fieldEvals, f->pairs,
+               f->qefAccepted, f->stage_ms[1], f->stage_ms[2], f->stage_ms[3], f->stage_ms[4], f->stage_ms[6]);
+  std::fclose(fp);
+}
+
 int pi_run(pi_frame* f) {
   PI_API_BEGIN
   PI_CHECK(f, "frame is null");
   set_device(f->ctx);
   need(f, 1);
+  const bool fresh = f->stage < 6;
   for (int t = 2; t <= 6; ++t) run_stage(f, t);
+  if (fresh) metrics_record(f);
   PI_API_END
 }
 

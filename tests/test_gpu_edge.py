@@ -67,3 +67,56 @@ def test_non_finite_coordinate_rejected(ctx):
     f = N.Frame(ctx, N.default_params(0.01)).upload(xyz).run()
     assert f.info()["num_nodes"] > 0
     f.close()
+
+
+def test_zero_particles_rejected(ctx):
+    f = N.Frame(ctx, N.default_params(0.01))
+    with pytest.raises(N.PiError) as e:
+        f.upload(np.zeros((0, 3), np.float32))
+    assert e.value.code == N.PI_ERR_INVALID
+    f.close()
+
+
+def test_budget_exhausted_then_recovers():
+    """A context whose byte budget is too small reports PI_ERR_NOMEM from the
+    stage that overruns it, holds no bytes once the frame is gone, and the
+    same input runs under a sufficient budget."""
+    from particleisosurface_gb300 import synth
+    fr = synth.small_blob(n=3000, seed=5)
+    small = N.Context(0, budget_bytes=256 << 10)
+    f = N.Frame(small, N.default_params(fr.radius)).upload(fr.xyz)
+    with pytest.raises(N.PiError) as e:
+        f.run()
+    assert e.value.code == N.PI_ERR_NOMEM
+    f.close()
+    assert small.stats()["bytes"] == 0
+    small.close()
+    big = N.Context(0, budget_bytes=1 << 30)
+    f = N.Frame(big, N.default_params(fr.radius)).upload(fr.xyz).run()
+    assert f.info()["num_vertices"] > 0
+    f.close()
+    big.close()
+
+
+def test_metrics_record_per_frame(tmp_path):
+    """PISURF_METRICS names a file that receives one JSON line per frame."""
+    import json
+    import os
+    import subprocess
+    import sys
+    out = tmp_path / "metrics.jsonl"
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import sys; sys.path.insert(0, %r)\n"
+            "from particleisosurface_gb300 import _native as N, synth\n"
+            "fr = synth.small_blob(n=2000, seed=3)\n"
+            "c = N.Context(0)\n"
+            "f = N.Frame(c, N.default_params(fr.radius)).upload(fr.xyz).run()\n"
+            "f.reset().run()\n"
+            "print(f.info()['num_triangles'])\n" % root)
+    r = subprocess.run([sys.executable, "-c", code], env=dict(os.environ, PISURF_METRICS=str(out)),
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = [json.loads(l) for l in out.read_text().splitlines()]
+    assert len(lines) == 2
+    assert lines[0]["triangles"] == int(r.stdout.strip().splitlines()[-1]) == lines[1]["triangles"]
+    assert lines[0]["particles"] == 2000 and lines[0]["stage_ms"]["octree"] > 0
