@@ -628,7 +628,8 @@ def ours(a):
             "config": {"workload": WORKLOAD, "frames_per_step_per_gpu": 1, "parallelism": "replicas",
                        "l2": "512 MiB buffer written between steps", "depth_max": info["depth_max"],
                        "nodes": info["num_nodes"], "vertices": info["num_vertices"],
-                       "triangles": info["num_triangles"]},
+                       "triangles": info["num_triangles"],
+                       "samples_per_lane": dict(zip(["leaf_level", "level_above"], ctx.tuning()))},
             "field_evals_per_s": world * evals / (ms / 1000.0),
             "field_evals_per_frame": evals,
             "candidate_pairs_per_frame": info["candidate_pairs"],

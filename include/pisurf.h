@@ -117,6 +117,15 @@ int pi_ctx_stats(const pi_ctx* ctx, uint64_t* launches, uint64_t* bytes);
 int pi_ctx_profile(pi_ctx* ctx, int enable);
 int pi_ctx_kernel_time(pi_ctx* ctx, double* total_ms, int64_t* launches, int64_t* pairs,
                        int64_t* evals);
+/* Samples per lane of the chunked field evaluation at the two finest
+ * octree levels (a warp evaluates chunks of 32 x that many samples sharing a
+ * candidate list).  By default each context times 1, 2 and 4 on its first
+ * frame's levels and keeps the fastest per level kind; pi_ctx_tune(ctx, k)
+ * with k = 1, 2 or 4 fixes it, k = 0 returns to timing.  The choice changes
+ * no result.  pi_ctx_tuning reports it (0 = not chosen yet): out2[0] for the
+ * leaf level, out2[1] for the level above. */
+int pi_ctx_tune(pi_ctx* ctx, int32_t samples_per_lane);
+int pi_ctx_tuning(const pi_ctx* ctx, int32_t* out2);
 /* The context stream as a cudaStream_t cast to void*. */
 void* pi_ctx_stream(pi_ctx* ctx);
 

@@ -77,6 +77,8 @@ def _declare(L):
         "pi_ctx_profile": (C.c_int, [P, C.c_int]),
         "pi_ctx_kernel_time": (C.c_int, [P, C.POINTER(C.c_double), pi64, pi64, pi64]),
         "pi_ctx_stream": (P, [P]),
+        "pi_ctx_tune": (C.c_int, [P, C.c_int32]),
+        "pi_ctx_tuning": (C.c_int, [P, C.POINTER(C.c_int32)]),
         "pi_frame_create": (C.c_int, [P, C.POINTER(Params), PP]),
         "pi_frame_destroy": (C.c_int, [P]),
         "pi_frame_upload": (C.c_int, [P, fp, i64]),
@@ -197,6 +199,16 @@ class Context:
         b = C.c_uint64()
         check(lib().pi_ctx_stats(self.h, C.byref(a), C.byref(b)))
         return dict(launches=a.value, bytes=b.value)
+
+    def tune(self, samples_per_lane=0):
+        """Fix the chunked evaluation's samples per lane (1, 2 or 4); 0 = time them."""
+        check(lib().pi_ctx_tune(self.h, samples_per_lane))
+
+    def tuning(self):
+        """[leaf level, level above]: samples per lane in use, 0 = not chosen yet."""
+        out = (C.c_int32 * 2)()
+        check(lib().pi_ctx_tuning(self.h, out))
+        return [out[0], out[1]]
 
     def profile(self, enable=True):
         check(lib().pi_ctx_profile(self.h, 1 if enable else 0))

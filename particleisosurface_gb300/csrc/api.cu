@@ -378,6 +378,24 @@ int pi_ctx_kernel_time(pi_ctx* c, double* total_ms, int64_t* launches, int64_t* 
 
 void* pi_ctx_stream(pi_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
+int pi_ctx_tune(pi_ctx* c, int32_t samples_per_lane) {
+  PI_API_BEGIN
+  PI_CHECK(c, "ctx is null");
+  PI_CHECK(samples_per_lane == 0 || samples_per_lane == 1 || samples_per_lane == 2 || samples_per_lane == 4,
+           "samples per lane must be 0, 1, 2 or 4");
+  c->eval_forced = samples_per_lane;
+  c->eval_lanes[0] = c->eval_lanes[1] = 0;
+  PI_API_END
+}
+
+int pi_ctx_tuning(const pi_ctx* c, int32_t* out2) {
+  PI_API_BEGIN
+  PI_CHECK(c && out2, "null argument");
+  out2[0] = c->eval_forced ? c->eval_forced : c->eval_lanes[0];
+  out2[1] = c->eval_forced ? c->eval_forced : c->eval_lanes[1];
+  PI_API_END
+}
+
 int pi_frame_create(pi_ctx* c, const pi_params* p, pi_frame** out) {
   PI_API_BEGIN
   PI_CHECK(c && p && out, "null argument");

@@ -58,6 +58,11 @@ struct pi_ctx {
   // one reference for the owner plus one per live frame; the context is
   // released when the last reference goes
   std::atomic<int> refs{1};
+  // samples per lane of the chunked field evaluation, per dense-level kind
+  // (0: leaf level, cell-octant buckets; 1: the level above, cell buckets);
+  // 0 = not chosen yet (timed on the first such level), forced by pi_ctx_tune
+  int eval_lanes[2] = {0, 0};
+  int eval_forced = 0;
 };
 
 struct pi_frame {

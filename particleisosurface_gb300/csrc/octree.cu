@@ -42,7 +42,6 @@ enum : int8_t { T_EMPTY = 0, T_INTERNAL = 1, T_LEAF = 2, T_UNCERTAIN = 3 };
 
 constexpr int kQ = 28;  // 27 samples + the centre per node
 constexpr int kEvalWarps = 8;  // warps per block of k_q_eval
-constexpr int kChunk = 64;     // samples per chunk of k_q_eval: two per lane
 
 struct LevelArgs {
   GridView g;
@@ -219,9 +218,9 @@ __device__ __forceinline__ uint32_t hash3(float x, float y, float z) {
 // once.  Equal points share a bucket; bucket k owns hash slots
 // [2 qoff[k], 2 qoff[k+1]) and a point's first inserter becomes its
 // representative.  On a dense level representatives get consecutive places
-// in the bucket's range of `order` and every kChunk-th place starts a chunk
-// (bucket, place); on a sparse level they are listed compactly in `order`
-// and *nchunks counts them.
+// in the bucket's range of `order` (k_q_chunks then cuts them into chunks);
+// on a sparse level they are listed compactly in `order` and *nchunks counts
+// them.
 __global__ void k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c, const float4* __restrict__ nd_v,
                            const int* __restrict__ qkey, const int* __restrict__ qoff, unsigned* __restrict__ hslot,
                            int* __restrict__ ucnt, int* __restrict__ rep, int* __restrict__ order,
@@ -229,7 +228,7 @@ __global__ void k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const int k = i < n ? qkey[i] : -1;
-  bool head = false, uniq = false;
+  bool uniq = false;
   int place = 0;
   if (k >= 0) {
     float qx, qy, qz;
@@ -280,27 +279,40 @@ __global__ void k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c
     b0 = __shfl_sync(peers, b0, leader);
     place = b0 + __popc(peers & ((1u << lane) - 1u));
     order[qoff[k] + place] = (int)i;
-    head = place % kChunk == 0;
   }
-  const unsigned hm = __ballot_sync(0xffffffffu, head);
-  if (hm == 0u) return;
-  const int hl = __ffs(hm) - 1;
-  int cb = 0;
-  if (lane == hl) cb = atomicAdd(nchunks, __popc(hm));
-  cb = __shfl_sync(0xffffffffu, cb, hl);
-  if (head) chunks[cb + __popc(hm & ((1u << lane) - 1u))] = make_int2(k, place);
+}
+
+// Chunks of a dense level: each bucket's distinct samples cut into runs of
+// `chunk` places (bucket, first place); list order is arbitrary.
+__global__ void k_q_chunks(long long nb, const int* __restrict__ ucnt, int chunk, int2* __restrict__ chunks,
+                           int* __restrict__ nchunks) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int u = k < nb ? ucnt[k] : 0;
+  const int c = (u + chunk - 1) / chunk;
+  int incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  if (total == 0) return;
+  int base = 0;
+  if (lane == 31) base = atomicAdd(nchunks, total);
+  base = __shfl_sync(0xffffffffu, base, 31) + incl - c;
+  for (int j = 0; j < c; ++j) chunks[base + j] = make_int2((int)k, j * chunk);
 }
 
 // Field at the samples of one chunk per warp (persistent, grid-stride over
-// the chunks); lane l holds samples l and l + 32 of the chunk.  All samples
-// of a chunk share a hash cell, hence the 27-cell candidate list of
-// Evaluator::SingleEval.  The warp tests 32 candidates at a time against the
-// chunk's bounding box: a candidate whose support radius R (|G d| < 2h needs
-// |d| < R, stored as R^2 * 1.002) does not reach the box contributes to no
-// sample.  Survivors' records are staged in shared memory in candidate order
-// and every lane walks them, so each sample's compensated sum sees the
-// in-support terms in candidate order.
-__global__ void __launch_bounds__(32 * kEvalWarps, 3) k_q_eval(QArgs a, const int* __restrict__ order,
+// the chunks); a chunk holds up to 32 K samples and lane l holds samples
+// l, l + 32, ..., K per lane (K is autotuned per context, see
+// eval_lanes_for).  All samples of a chunk share a hash cell, hence the
+// 27-cell candidate list of Evaluator::SingleEval; chunk_field filters the
+// candidates against the chunk's bounding box, stages the survivors in
+// shared memory and sums in candidate order.
+template <int K>
+__global__ void __launch_bounds__(32 * kEvalWarps, (K > 2 ? 2 : 3)) k_q_eval(QArgs a, const int* __restrict__ order,
                                                             const int* __restrict__ qoff,
                                                             const int* __restrict__ ucnt,
                                                             const int2* __restrict__ chunks,
@@ -319,13 +331,15 @@ __global__ void __launch_bounds__(32 * kEvalWarps, 3) k_q_eval(QArgs a, const in
   long long pairs = 0;
   for (int ci = blockIdx.x * kEvalWarps + wib; ci < nchunks; ci += nwarps) {
     const int2 ch = chunks[ci];
-    const int len = min(kChunk, __ldg(ucnt + ch.x) - ch.y);
+    const int len = min(32 * K, __ldg(ucnt + ch.x) - ch.y);
     const int* ord = order + __ldg(qoff + ch.x) + ch.y;
-    int q[2] = {0, 0};
-    float x[2] = {0.f, 0.f}, y[2] = {0.f, 0.f}, z[2] = {0.f, 0.f};
-    bool act[2], slots[2];
+    int q[K];
+    float x[K], y[K], z[K];
+    bool act[K], slots[K];
 #pragma unroll
-    for (int m = 0; m < 2; ++m) {
+    for (int m = 0; m < K; ++m) {
+      q[m] = 0;
+      x[m] = y[m] = z[m] = 0.f;
       act[m] = lane + 32 * m < len;
       slots[m] = len > 32 * m;  // warp-uniform
       if (act[m]) {
@@ -337,10 +351,10 @@ __global__ void __launch_bounds__(32 * kEvalWarps, 3) k_q_eval(QArgs a, const in
     int cx, cy, cz;
     cell_of(a.g, __shfl_sync(0xffffffffu, x[0], 0), __shfl_sync(0xffffffffu, y[0], 0),
             __shfl_sync(0xffffffffu, z[0], 0), cx, cy, cz);
-    float sum[2];
-    chunk_field<2>(a.g, a.P, cx, cy, cz, x, y, z, act, slots, st, sum, pairs);
+    float sum[K];
+    chunk_field<K>(a.g, a.P, cx, cy, cz, x, y, z, act, slots, st, sum, pairs);
 #pragma unroll
-    for (int m = 0; m < 2; ++m)
+    for (int m = 0; m < K; ++m)
       if (act[m]) qval[q[m]] = a.iso - sum[m];
   }
 #pragma unroll
@@ -655,6 +669,75 @@ __global__ void k_root(float cx, float cy, float cz, float h, int size, float4* 
   nd_org[0] = make_int4(0, 0, 0, size);
 }
 
+template <int K>
+static void launch_eval(pi_frame* f, const QArgs& qa, long long qn, const int* order, const int* qoff,
+                        const int* ucnt, const int2* chunks, const int* nchunks, float* qval,
+                        unsigned long long* counters) {
+  pi_ctx* ctx = f->ctx;
+  static thread_local int occ[64][3] = {};
+  const int dev = ctx->device & 63, slot = K == 1 ? 0 : K == 2 ? 1 : 2;
+  if (occ[dev][slot] == 0) {
+    int nb = 0;
+    PI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_q_eval<K>, 32 * kEvalWarps, 0));
+    occ[dev][slot] = nb > 0 ? nb : 1;
+  }
+  const int blocks = (int)std::min<long long>((long long)ctx->smCount * occ[dev][slot],
+                                              div_up(qn, 32 * kEvalWarps));
+  PI_LAUNCH(k_q_eval<K>, blocks, 32 * kEvalWarps, 0, ctx->stream, qa, order, qoff, ucnt, chunks, nchunks, f->nd_c.p,
+            f->nd_v.p, qval, counters);
+}
+
+// Chunk list for K samples per lane, then the chunked evaluation.
+static void dense_eval(pi_frame* f, int K, const QArgs& qa, long long qn, long long nbuckets, const int* order,
+                       const int* qoff, const int* ucnt, int2* chunks, int* nchunks, float* qval,
+                       unsigned long long* counters) {
+  cudaStream_t s = f->ctx->stream;
+  PI_CUDA(cudaMemsetAsync(nchunks, 0, sizeof(int), s));
+  PI_LAUNCH(k_q_chunks, div_up(nbuckets, 256), 256, 0, s, nbuckets, ucnt, 32 * K, chunks, nchunks);
+  if (K == 1)
+    launch_eval<1>(f, qa, qn, order, qoff, ucnt, chunks, nchunks, qval, counters);
+  else if (K == 2)
+    launch_eval<2>(f, qa, qn, order, qoff, ucnt, chunks, nchunks, qval, counters);
+  else
+    launch_eval<4>(f, qa, qn, order, qoff, ucnt, chunks, nchunks, qval, counters);
+}
+
+// Samples per lane for a dense level of the given kind: the context's choice,
+// or, the first time, the fastest of K = 1, 2, 4 timed on this level (the
+// evaluation is pure, so the runs give identical values).
+static int eval_lanes_for(pi_frame* f, int kind, const QArgs& qa, long long qn, long long nbuckets,
+                          const int* order, const int* qoff, const int* ucnt, int2* chunks, int* nchunks,
+                          float* qval) {
+  pi_ctx* ctx = f->ctx;
+  if (ctx->eval_forced) return ctx->eval_forced;
+  if (ctx->eval_lanes[kind]) return ctx->eval_lanes[kind];
+  cudaStream_t s = ctx->stream;
+  cudaEvent_t e0, e1;
+  PI_CUDA(cudaEventCreate(&e0));
+  PI_CUDA(cudaEventCreate(&e1));
+  static const int cand[3] = {1, 2, 4};
+  float best = 1e30f;
+  int bestk = 2;
+  DBuf<unsigned long long> scratch;  // the trial runs' event counters are not the frame's
+  scratch.alloc(ctx, s, kCounterWords);
+  for (int c = 0; c < 3; ++c) {
+    PI_CUDA(cudaEventRecord(e0, s));
+    dense_eval(f, cand[c], qa, qn, nbuckets, order, qoff, ucnt, chunks, nchunks, qval, scratch.p);
+    PI_CUDA(cudaEventRecord(e1, s));
+    PI_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    PI_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best) {
+      best = ms;
+      bestk = cand[c];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->eval_lanes[kind] = bestk;
+  return bestk;
+}
+
 static void ensure_nodes(pi_frame* f, long long need) {
   if ((long long)f->nd_c.n >= need) return;
   long long cap = std::max<long long>(need, (long long)(f->nd_c.n * 3 / 2) + 1024);
@@ -697,14 +780,6 @@ void stage_octree(pi_frame* f) {
   DBuf<float> qval;
   qcnt.alloc(ctx, s, ek + 2);  // bucket counts, total, chunk count
   ucnt.alloc(ctx, s, ek);      // distinct points per bucket
-  static thread_local int eval_occ[64] = {0};
-  const int dev = ctx->device & 63;
-  if (eval_occ[dev] == 0) {
-    int nb = 0;
-    PI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_q_eval, 32 * kEvalWarps, 0));
-    eval_occ[dev] = nb > 0 ? nb : 1;
-  }
-  const int eval_blocks = ctx->smCount * eval_occ[dev];
   long long lb = 0, le = 1;
   bool known = false;  // emptiness and curvature of this level settled by the parents' scan
   for (int depth = 0;; ++depth) {
@@ -742,11 +817,13 @@ void stage_octree(pi_frame* f) {
       exclusive_scan_i32(qcnt.p, qcnt.p, ek + 1, nullptr, f->tmp.p, s);
       PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
                 ucnt.p, rep.p, order.p, chunks.p, qcnt.p + ek + 1, dense);
+      int lanes = 0;
+      if (dense)
+        lanes = eval_lanes_for(f, depth == f->dmax ? 0 : 1, qa, qn, ek, order.p, qcnt.p, ucnt.p, chunks.p,
+                               qcnt.p + ek + 1, qval.p);
       prof_begin(ctx, s);
       if (dense)
-        PI_LAUNCH(k_q_eval, (int)std::min<long long>(eval_blocks, div_up(qn, 32 * kEvalWarps)), 32 * kEvalWarps, 0,
-                  s, qa, order.p, qcnt.p, ucnt.p, chunks.p, qcnt.p + ek + 1, f->nd_c.p, f->nd_v.p, qval.p,
-                  f->dcount.p);
+        dense_eval(f, lanes, qa, qn, ek, order.p, qcnt.p, ucnt.p, chunks.p, qcnt.p + ek + 1, qval.p, f->dcount.p);
       else
         PI_LAUNCH(k_q_eval_thread, (int)std::min<long long>((long long)ctx->smCount * 8, div_up(qn, 256)), 256, 0,
                   s, qa, order.p, qcnt.p + ek + 1, f->nd_c.p, f->nd_v.p, qval.p, f->dcount.p);

@@ -1,0 +1,56 @@
+"""Samples per lane of the chunked field evaluation (pi_ctx_tune): K = 1, 2
+and 4 chunk the same distinct samples differently, and each sample's sum runs
+over the same candidates in the same order, so every node value, the octree
+and the mesh are bit-identical whatever K, with and without the QEF leaves.
+The timed choice (K = 0) settles on one of 1, 2, 4 per level kind."""
+import numpy as np
+import pytest
+
+from particleisosurface_gb300 import _native as N
+from particleisosurface_gb300 import build as B
+from particleisosurface_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    B.build()
+    c = N.Context(0)
+    yield c
+    c.close()
+
+
+def run_frame(ctx, fr, qef, k):
+    ctx.tune(k)
+    g = N.Frame(ctx, N.default_params(fr.radius, qef=qef)).upload(fr.xyz).run()
+    nodes = g.dump(N.DUMP_NODES)
+    v, t = g.mesh()
+    tuning = ctx.tuning()
+    g.close()
+    return nodes, v, t, tuning
+
+
+@pytest.mark.parametrize("qef", [False, True])
+def test_samples_per_lane_change_no_result(ctx, qef):
+    fr = synth.slab_and_sphere(n=20000, seed=1)
+    ref = run_frame(ctx, fr, qef, 1)
+    assert ref[3] == [1, 1]
+    for k in (2, 4, 0):
+        nodes, v, t, tuning = run_frame(ctx, fr, qef, k)
+        assert nodes.tobytes() == ref[0].tobytes(), k
+        assert np.array_equal(v, ref[1]) and np.array_equal(t, ref[2]), k
+        if k:
+            assert tuning == [k, k]
+        else:
+            # without QEF the leaf level evaluates node centres only (no
+            # chunked evaluation there), so only the level above is timed
+            assert tuning[0] in ((1, 2, 4) if qef else (0,)) and tuning[1] in (1, 2, 4)
+    ctx.tune(0)
+
+
+def test_tune_rejects_other_values(ctx):
+    for k in (3, 8, -1):
+        with pytest.raises(N.PiError):
+            ctx.tune(k)
+    ctx.tune(0)
