@@ -64,6 +64,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-evals", type=int, default=200_000)
     p.add_argument("--qef", action="store_true", help="with --single: per-leaf QEF vertices on")
+    p.add_argument("--samples-per-lane", type=int, default=0, choices=[0, 1, 2, 4],
+                   help="with --single: fix the chunked evaluation's samples per lane (0 = timed choice)")
     p.add_argument("--single", action="store_true",
                    help="reconstruct one frame once and print its counters (for profiler captures)")
     p.add_argument("--workload", choices=["dam_break_1m", "batch64", "serving", "stress", "grid"], default="dam_break_1m",
@@ -354,6 +356,7 @@ def single(a):
     B.build()
     fr = make_frame(a.n)
     ctx = N.Context(0)
+    ctx.tune(a.samples_per_lane)
     p = N.default_params(fr.radius)
     p.qef = 1 if a.qef else 0
     f = N.Frame(ctx, p).upload(fr.xyz).run()

@@ -41,7 +41,8 @@ namespace pisurf {
 enum : int8_t { T_EMPTY = 0, T_INTERNAL = 1, T_LEAF = 2, T_UNCERTAIN = 3 };
 
 constexpr int kQ = 28;  // 27 samples + the centre per node
-constexpr int kEvalWarps = 8;  // warps per block of k_q_eval
+constexpr int kEvalWarps = 8;   // warps per block of k_q_eval
+constexpr int kSpawnWarps = 8;  // warps per block of k_spawn_scan
 
 struct LevelArgs {
   GridView g;
@@ -523,15 +524,17 @@ __global__ void k_spawn(long long lb, long long le, long long cbase, const int* 
 // would compute them (checkEmptyAndCalcCurv, src/surface_reconstructor.cpp:
 // 152-222).  One warp per parent; lane k writes child k.
 template <bool CURV>
-__global__ void __launch_bounds__(256) k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict__ rank,
+__global__ void __launch_bounds__(32 * kSpawnWarps) k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict__ rank,
                                                     int child_depth, float4* __restrict__ nd_c,
                                                     float4* __restrict__ nd_v, uint64_t* __restrict__ nd_id,
                                                     int* __restrict__ nd_parent, int* __restrict__ nd_child,
                                                     int8_t* nd_type, int8_t* __restrict__ nd_depth,
                                                     int8_t* __restrict__ nd_sc, float* __restrict__ nd_curv,
                                                     int4* __restrict__ nd_org) {
-  const long long i = a.lb + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  __shared__ int s_row[kSpawnWarps][32];  // row starting at each element position of a batch
+  const long long i = a.lb + (long long)blockIdx.x * kSpawnWarps + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
+  int* const srow = s_row[threadIdx.x >> 5];
   if (i >= a.le) return;
   if (nd_type[i] != T_INTERNAL) {
     if (lane == 0) nd_child[i] = -1;
@@ -586,14 +589,21 @@ __global__ void __launch_bounds__(256) k_spawn_scan(LevelArgs a, long long cbase
       }
       const int excl = incl - rl;
       const int total = __shfl_sync(0xffffffffu, incl, 31);
-      const int nr = min(32, rows - r0);
+      int carry = 0;  // row of the batch's element before its first
       for (int t0 = 0; t0 < total; t0 += 32) {
         if (!CURV && t0 > 0 && __reduce_or_sync(0xffffffffu, found) == 0xffu) break;
         const int t = t0 + lane;
-        // row of element t: the last row whose start is <= t
-        int rr = 0;
-        for (int k = 1; k < nr; ++k)
-          if (__shfl_sync(0xffffffffu, excl, k) <= t) rr = k;
+        // row of element t: the non-empty row starting at the last position
+        // <= t of this batch, else the row carried over from the batch before
+        // (non-empty rows start at distinct positions)
+        const bool starts = rl > 0 && excl >= t0 && excl < t0 + 32;
+        __syncwarp();
+        if (starts) srow[excl - t0] = lane;
+        const unsigned smask = __reduce_or_sync(0xffffffffu, starts ? 1u << (excl - t0) : 0u);
+        __syncwarp();
+        const unsigned below = smask & (0xffffffffu >> (31 - lane));
+        const int rr = below ? srow[31 - __clz(below)] : carry;
+        carry = __shfl_sync(0xffffffffu, rr, 31);
         const int j = __shfl_sync(0xffffffffu, rs, rr) + (t - __shfl_sync(0xffffffffu, excl, rr));
         if (t >= total) continue;
         const float4 p = __ldg(a.pos + j);
@@ -849,11 +859,11 @@ void stage_octree(pi_frame* f) {
       const float cell_child = 2.0f * std::ldexp(f->rootH, -(depth + 1));
       const int child_curv = (double)(cell_child - f->P.radius) < 1e-8 ? 0 : 1;
       if (child_curv)
-        PI_LAUNCH(k_spawn_scan<true>, div_up(nl, wpb), 32 * wpb, 0, s, la, le, flag.p, depth + 1, f->nd_c.p,
+        PI_LAUNCH(k_spawn_scan<true>, div_up(nl, kSpawnWarps), 32 * kSpawnWarps, 0, s, la, le, flag.p, depth + 1, f->nd_c.p,
                   f->nd_v.p, f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p,
                   f->nd_curv.p, f->nd_org.p);
       else
-        PI_LAUNCH(k_spawn_scan<false>, div_up(nl, wpb), 32 * wpb, 0, s, la, le, flag.p, depth + 1, f->nd_c.p,
+        PI_LAUNCH(k_spawn_scan<false>, div_up(nl, kSpawnWarps), 32 * kSpawnWarps, 0, s, la, le, flag.p, depth + 1, f->nd_c.p,
                   f->nd_v.p, f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p,
                   f->nd_curv.p, f->nd_org.p);
     } else {
