@@ -218,14 +218,12 @@ __device__ __forceinline__ uint32_t hash3(float x, float y, float z) {
 // candidates, same summation order), so each distinct point is evaluated
 // once.  Equal points share a bucket; bucket k owns hash slots
 // [2 qoff[k], 2 qoff[k+1]) and a point's first inserter becomes its
-// representative.  On a dense level representatives get consecutive places
-// in the bucket's range of `order` (k_q_chunks then cuts them into chunks);
-// on a sparse level they are listed compactly in `order` and *nchunks counts
-// them.
+// representative.  Representatives get consecutive places in the bucket's
+// range of `order` (on a dense level k_q_chunks then cuts them into chunks, on
+// a sparse level k_q_compact lists them in bucket order).
 __global__ void k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c, const float4* __restrict__ nd_v,
                            const int* __restrict__ qkey, const int* __restrict__ qoff, unsigned* __restrict__ hslot,
-                           int* __restrict__ ucnt, int* __restrict__ rep, int* __restrict__ order,
-                           int2* __restrict__ chunks, int* __restrict__ nchunks, int dense) {
+                           int* __restrict__ ucnt, int* __restrict__ rep, int* __restrict__ order) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   const int k = i < n ? qkey[i] : -1;
@@ -259,18 +257,7 @@ __global__ void k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c
     rep[i] = r;
     uniq = r == (int)i;
   }
-  if (!dense) {
-    // sparse level: representatives go to a compact list, one thread each
-    const unsigned um = __ballot_sync(0xffffffffu, uniq);
-    if (um == 0u) return;
-    const int ul = __ffs(um) - 1;
-    int ub = 0;
-    if (lane == ul) ub = atomicAdd(nchunks, __popc(um));
-    ub = __shfl_sync(0xffffffffu, ub, ul);
-    if (uniq) order[ub + __popc(um & ((1u << lane) - 1u))] = (int)i;
-    return;
-  }
-  // dense level: places for the representatives, one atomic per bucket and warp
+  // places for the representatives, one atomic per bucket and warp
   const unsigned um = __ballot_sync(0xffffffffu, uniq);
   const unsigned peers = __match_any_sync(0xffffffffu, uniq ? k : -1) & um;
   if (uniq) {
@@ -365,7 +352,8 @@ __global__ void __launch_bounds__(32 * kEvalWarps, (K > 2 ? 2 : 3)) k_q_eval(QAr
 
 // Sparse levels (a few distinct samples per bucket): one thread per distinct
 // sample, each walking its own 27-cell candidate list (field_sum, the same
-// tests and summation order as k_q_eval).
+// tests and summation order as k_q_eval).  The list is in bucket order, so a
+// warp's threads mostly share their cells and walk the same rows.
 __global__ void __launch_bounds__(256, 4) k_q_eval_thread(QArgs a, const int* __restrict__ list,
                                                        const int* __restrict__ count_ptr,
                                                        const float4* __restrict__ nd_c,
@@ -383,6 +371,20 @@ __global__ void __launch_bounds__(256, 4) k_q_eval_thread(QArgs a, const int* __
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
   if ((threadIdx.x & 31) == 0 && pairs) stripe_add(counters, 1, (unsigned long long)pairs);
+}
+
+// Sparse levels: the distinct samples, placed per bucket by k_q_dedupe, made
+// into one list in bucket order (ucum = exclusive scan of the bucket counts),
+// so that neighbouring threads of k_q_eval_thread walk the same cells.
+__global__ void k_q_compact(long long nb, const int* __restrict__ qoff, const int* __restrict__ ucnt,
+                            const int* __restrict__ ucum, const int* __restrict__ order, int* __restrict__ list) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nb) return;
+  const int u = ucnt[k];
+  if (u == 0) return;
+  const int* src = order + qoff[k];
+  int* dst = list + ucum[k];
+  for (int t = 0; t < u; ++t) dst[t] = src[t];
 }
 
 // Leaves by size without QEF: afterSampleEval (src/surface_reconstructor.cpp:
@@ -784,12 +786,13 @@ void stage_octree(pi_frame* f) {
   const int ekx = gh.nx + 4, eky = gh.ny + 4;
   const long long ek = (long long)ekx * eky * (gh.nz + 4) * 8;  // buckets: cell x octant
   counters_reset(f);
-  DBuf<int> flag, qcnt, qkey, rep, order, ucnt;
+  DBuf<int> flag, qcnt, qkey, rep, order, ucnt, ucum;
   DBuf<unsigned> hslot;
   DBuf<int2> chunks;
   DBuf<float> qval;
   qcnt.alloc(ctx, s, ek + 2);  // bucket counts, total, chunk count
-  ucnt.alloc(ctx, s, ek);      // distinct points per bucket
+  ucnt.alloc(ctx, s, ek + 1);  // distinct points per bucket (+ 1 for the scan's total)
+  ucum.alloc(ctx, s, ek + 1);  // exclusive scan of ucnt (sparse levels)
   long long lb = 0, le = 1;
   bool known = false;  // emptiness and curvature of this level settled by the parents' scan
   for (int depth = 0;; ++depth) {
@@ -816,7 +819,7 @@ void stage_octree(pi_frame* f) {
       order.alloc(ctx, s, qn);
       chunks.alloc(ctx, s, qn);
       PI_CUDA(cudaMemsetAsync(qcnt.p, 0, sizeof(int) * (ek + 2), s));
-      PI_CUDA(cudaMemsetAsync(ucnt.p, 0, sizeof(int) * ek, s));
+      PI_CUDA(cudaMemsetAsync(ucnt.p, 0, sizeof(int) * (ek + 1), s));
       PI_CUDA(cudaMemsetAsync(hslot.p, 0, sizeof(unsigned) * 2 * qn, s));
       // the leaf level (node size r, samples r/2 apart) holds about 50
       // distinct samples per cell octant, the level above about 50 per cell;
@@ -826,7 +829,12 @@ void stage_octree(pi_frame* f) {
       PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
       exclusive_scan_i32(qcnt.p, qcnt.p, ek + 1, nullptr, f->tmp.p, s);
       PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
-                ucnt.p, rep.p, order.p, chunks.p, qcnt.p + ek + 1, dense);
+                ucnt.p, rep.p, order.p);
+      int* list = reinterpret_cast<int*>(hslot.p);  // the hash slots are free once the samples are placed
+      if (!dense) {
+        exclusive_scan_i32(ucnt.p, ucum.p, ek + 1, nullptr, f->tmp.p, s);
+        PI_LAUNCH(k_q_compact, div_up(ek, 256), 256, 0, s, ek, qcnt.p, ucnt.p, ucum.p, order.p, list);
+      }
       int lanes = 0;
       if (dense)
         lanes = eval_lanes_for(f, depth == f->dmax ? 0 : 1, qa, qn, ek, order.p, qcnt.p, ucnt.p, chunks.p,
@@ -836,7 +844,7 @@ void stage_octree(pi_frame* f) {
         dense_eval(f, lanes, qa, qn, ek, order.p, qcnt.p, ucnt.p, chunks.p, qcnt.p + ek + 1, qval.p, f->dcount.p);
       else
         PI_LAUNCH(k_q_eval_thread, (int)std::min<long long>((long long)ctx->smCount * 8, div_up(qn, 256)), 256, 0,
-                  s, qa, order.p, qcnt.p + ek + 1, f->nd_c.p, f->nd_v.p, qval.p, f->dcount.p);
+                  s, qa, list, ucum.p + ek, f->nd_c.p, f->nd_v.p, qval.p, f->dcount.p);
       prof_end(ctx, s, -1, -1);
       PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p, f->nd_type.p,
                 f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p);
