@@ -389,12 +389,57 @@ struct BisectArgs {
   float rr;  // r / 2
 };
 
-__global__ void k_bisect(BisectArgs a, long long nv, const int* __restrict__ rep, const int* __restrict__ slotA,
+// Vertices listed by the hash cell of their first bisection midpoint (count
+// per cell, scan, place), so that neighbouring threads of k_bisect walk the
+// same cells.  Order within a cell is arbitrary: each vertex's result
+// depends on its own edge only.
+__device__ __forceinline__ int vertex_cell(const BisectArgs& a, const float4& p, const float4& q, int ekx,
+                                           int eky) {
+  const float mx = __fmul_rn(__fadd_rn(p.x, q.x), 0.5f);
+  const float my = __fmul_rn(__fadd_rn(p.y, q.y), 0.5f);
+  const float mz = __fmul_rn(__fadd_rn(p.z, q.z), 0.5f);
+  int cx, cy, cz;
+  cell_of(a.g, mx, my, mz, cx, cy, cz);
+  return ((cz + 2) * eky + (cy + 2)) * ekx + (cx + 2);
+}
+
+__global__ void k_vcell_count(BisectArgs a, long long nv, const int* __restrict__ rep, const int* __restrict__ slotA,
+                              const int* __restrict__ slotB, const float4* __restrict__ nd_v, int ekx, int eky,
+                              int* __restrict__ cnt, int* __restrict__ key) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  int k = -1;
+  if (v < nv) {
+    const int s = rep[v];
+    k = vertex_cell(a, nd_v[slotA[s]], nd_v[slotB[s]], ekx, eky);
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, k);
+  if (k >= 0 && lane == __ffs(peers) - 1) atomicAdd(cnt + k, __popc(peers));
+  if (v < nv) key[v] = k;
+}
+
+__global__ void k_vcell_place(long long nv, const int* __restrict__ key, const int* __restrict__ off,
+                              int* __restrict__ fill, int* __restrict__ list) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int k = v < nv ? key[v] : -1;
+  const unsigned peers = __match_any_sync(0xffffffffu, k);
+  if (k < 0) return;
+  const int leader = __ffs(peers) - 1;
+  int b = 0;
+  if (lane == leader) b = atomicAdd(fill + k, __popc(peers));
+  b = __shfl_sync(peers, b, leader);
+  list[off[k] + b + __popc(peers & ((1u << lane) - 1u))] = (int)v;
+}
+
+__global__ void k_bisect(BisectArgs a, long long nv, const int* __restrict__ order, const int* __restrict__ rep,
+                         const int* __restrict__ slotA,
                          const int* __restrict__ slotB, const float4* __restrict__ nd_v,
                          const uint64_t* __restrict__ nd_id, float* __restrict__ out,
                          uint64_t* __restrict__ vkeys, unsigned long long* __restrict__ counters) {
-  long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= nv) return;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nv) return;
+  const long long v = order[t];
   const int s = rep[v];
   const int A = slotA[s], B = slotB[s];
   float4 p = nd_v[A], q = nd_v[B];
@@ -576,8 +621,24 @@ void stage_extract(pi_frame* f) {
   const GridHost& gh = f->g;
   BisectArgs ba{GridView{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p},
                 PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p}, f->iso, f->P.radius / 2};
-  PI_LAUNCH(k_bisect, div_up(nv, 128), 128, 0, s, ba, nv, rep.p, slotA.p, slotB.p, f->nd_v.p, f->nd_id.p, f->mv.p,
-            f->mk.p, f->dcount.p);
+  {
+    const int ekx = gh.nx + 4, eky = gh.ny + 4;
+    const long long nc = (long long)ekx * eky * (gh.nz + 4);
+    DBuf<int> vcnt, vfill, vkey, vorder;
+    vcnt.alloc(c, s, nc + 1);
+    vfill.alloc(c, s, nc);
+    vkey.alloc(c, s, nv > 0 ? nv : 1);
+    vorder.alloc(c, s, nv > 0 ? nv : 1);
+    if (tmp.n < scan_tmp_ints(nc + 1)) tmp.alloc(c, s, scan_tmp_ints(nc + 1));
+    PI_CUDA(cudaMemsetAsync(vcnt.p, 0, sizeof(int) * (nc + 1), s));
+    PI_CUDA(cudaMemsetAsync(vfill.p, 0, sizeof(int) * nc, s));
+    PI_LAUNCH(k_vcell_count, div_up(nv, 256), 256, 0, s, ba, nv, rep.p, slotA.p, slotB.p, f->nd_v.p, ekx, eky,
+              vcnt.p, vkey.p);
+    exclusive_scan_i32(vcnt.p, vcnt.p, nc + 1, nullptr, tmp.p, s);
+    PI_LAUNCH(k_vcell_place, div_up(nv, 256), 256, 0, s, nv, vkey.p, vcnt.p, vfill.p, vorder.p);
+    PI_LAUNCH(k_bisect, div_up(nv, 128), 128, 0, s, ba, nv, vorder.p, rep.p, slotA.p, slotB.p, f->nd_v.p,
+              f->nd_id.p, f->mv.p, f->mk.p, f->dcount.p);
+  }
   // 7. triangles: first of each sorted vertex triple, in generation order
   DBuf<int> otri, trank;
   DBuf<unsigned> ttab;

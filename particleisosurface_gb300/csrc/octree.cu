@@ -175,9 +175,10 @@ __device__ __forceinline__ int ext_key(const QArgs& a, int cx, int cy, int cz) {
   return ((cz + 2) * a.eky + (cy + 2)) * a.ekx + (cx + 2);
 }
 
-// Bucket of a sample: its hash cell (extended key) times 8 plus the octant of
-// the cell it lies in, so that a warp's points are close together.  Counts
-// come from one warp-aggregated atomic per bucket and warp.
+// Bucket of a sample: its hash cell (extended key), times 8 plus the octant
+// of the cell it lies in when a.octants is set, so that a chunk's points are
+// close together.  Counts come from one warp-aggregated atomic per bucket and
+// warp.
 __global__ void k_q_count(QArgs a, const float4* __restrict__ nd_c, const float4* __restrict__ nd_v,
                           const int8_t* __restrict__ nd_type, int* __restrict__ qcnt, int* __restrict__ qkey) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -191,11 +192,13 @@ __global__ void k_q_count(QArgs a, const float4* __restrict__ nd_c, const float4
     sample_point(nd_c[node], nd_v[node], (int)(i % kQ), qx, qy, qz);
     int cx, cy, cz;
     cell_of(a.g, qx, qy, qz, cx, cy, cz);
-    const float fx = __fdiv_rn(__fsub_rn(qx, a.g.b0), a.g.cell) - (float)cx;
-    const float fy = __fdiv_rn(__fsub_rn(qy, a.g.b2), a.g.cell) - (float)cy;
-    const float fz = __fdiv_rn(__fsub_rn(qz, a.g.b4), a.g.cell) - (float)cz;
-    const int oct = a.octants ? ((fx >= 0.5f ? 1 : 0) | (fy >= 0.5f ? 2 : 0) | (fz >= 0.5f ? 4 : 0)) : 0;
-    k = ext_key(a, cx, cy, cz) * 8 + oct;
+    k = ext_key(a, cx, cy, cz);
+    if (a.octants) {
+      const float fx = __fdiv_rn(__fsub_rn(qx, a.g.b0), a.g.cell) - (float)cx;
+      const float fy = __fdiv_rn(__fsub_rn(qy, a.g.b2), a.g.cell) - (float)cy;
+      const float fz = __fdiv_rn(__fsub_rn(qz, a.g.b4), a.g.cell) - (float)cz;
+      k = k * 8 + ((fx >= 0.5f ? 1 : 0) | (fy >= 0.5f ? 2 : 0) | (fz >= 0.5f ? 4 : 0));
+    }
   }
   const unsigned peers = __match_any_sync(0xffffffffu, k);
   const int leader = __ffs(peers) - 1;
@@ -811,40 +814,43 @@ void stage_octree(pi_frame* f) {
                 f->nd_c.p, f->nd_v.p, f->nd_type.p, f->dcount.p);
     } else if (depth >= f->dmin) {
       const long long qn = nl * kQ;
-      if (f->tmp.n < scan_tmp_ints(ek + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(ek + 1));
+      // buckets: cell octants on the leaf level, whole cells above it
+      const int octants = depth == f->dmax ? 1 : 0;
+      const long long nb = octants ? ek : ek / 8;
+      if (f->tmp.n < scan_tmp_ints(nb + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(nb + 1));
       qkey.alloc(ctx, s, qn);
       rep.alloc(ctx, s, qn);
       hslot.alloc(ctx, s, 2 * qn);
       qval.alloc(ctx, s, qn);
       order.alloc(ctx, s, qn);
       chunks.alloc(ctx, s, qn);
-      PI_CUDA(cudaMemsetAsync(qcnt.p, 0, sizeof(int) * (ek + 2), s));
-      PI_CUDA(cudaMemsetAsync(ucnt.p, 0, sizeof(int) * (ek + 1), s));
+      PI_CUDA(cudaMemsetAsync(qcnt.p, 0, sizeof(int) * (nb + 2), s));
+      PI_CUDA(cudaMemsetAsync(ucnt.p, 0, sizeof(int) * (nb + 1), s));
       PI_CUDA(cudaMemsetAsync(hslot.p, 0, sizeof(unsigned) * 2 * qn, s));
       // the leaf level (node size r, samples r/2 apart) holds about 50
       // distinct samples per cell octant, the level above about 50 per cell;
       // coarser levels hold a few per cell
       const int dense = depth >= f->dmax - 1 ? 1 : 0;
-      QArgs qa{g, P, f->iso, lb, le, ekx, eky, depth == f->dmax ? 1 : 0};
+      QArgs qa{g, P, f->iso, lb, le, ekx, eky, octants};
       PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
-      exclusive_scan_i32(qcnt.p, qcnt.p, ek + 1, nullptr, f->tmp.p, s);
+      exclusive_scan_i32(qcnt.p, qcnt.p, nb + 1, nullptr, f->tmp.p, s);
       PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
                 ucnt.p, rep.p, order.p);
       int* list = reinterpret_cast<int*>(hslot.p);  // the hash slots are free once the samples are placed
       if (!dense) {
-        exclusive_scan_i32(ucnt.p, ucum.p, ek + 1, nullptr, f->tmp.p, s);
-        PI_LAUNCH(k_q_compact, div_up(ek, 256), 256, 0, s, ek, qcnt.p, ucnt.p, ucum.p, order.p, list);
+        exclusive_scan_i32(ucnt.p, ucum.p, nb + 1, nullptr, f->tmp.p, s);
+        PI_LAUNCH(k_q_compact, div_up(nb, 256), 256, 0, s, nb, qcnt.p, ucnt.p, ucum.p, order.p, list);
       }
       int lanes = 0;
       if (dense)
-        lanes = eval_lanes_for(f, depth == f->dmax ? 0 : 1, qa, qn, ek, order.p, qcnt.p, ucnt.p, chunks.p,
-                               qcnt.p + ek + 1, qval.p);
+        lanes = eval_lanes_for(f, depth == f->dmax ? 0 : 1, qa, qn, nb, order.p, qcnt.p, ucnt.p, chunks.p,
+                               qcnt.p + nb + 1, qval.p);
       prof_begin(ctx, s);
       if (dense)
-        dense_eval(f, lanes, qa, qn, ek, order.p, qcnt.p, ucnt.p, chunks.p, qcnt.p + ek + 1, qval.p, f->dcount.p);
+        dense_eval(f, lanes, qa, qn, nb, order.p, qcnt.p, ucnt.p, chunks.p, qcnt.p + nb + 1, qval.p, f->dcount.p);
       else
         PI_LAUNCH(k_q_eval_thread, (int)std::min<long long>((long long)ctx->smCount * 8, div_up(qn, 256)), 256, 0,
-                  s, qa, list, ucum.p + ek, f->nd_c.p, f->nd_v.p, qval.p, f->dcount.p);
+                  s, qa, list, ucum.p + nb, f->nd_c.p, f->nd_v.p, qval.p, f->dcount.p);
       prof_end(ctx, s, -1, -1);
       PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p, f->nd_type.p,
                 f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p);
