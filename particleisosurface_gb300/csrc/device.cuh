@@ -89,7 +89,9 @@ __device__ __forceinline__ bool nb_row(const GridView& g, int cx, int y, int z, 
 // Cubic B-spline of ratio q = sqrt(s2) in [0, 2) without the Sigma factor
 // (Bspline_kernel, src/evaluator.cpp:383-396).
 __device__ __forceinline__ float bspline_s2(float s2) {
-  float q = s2 > 0.f ? s2 * rsqrtf(s2) : 0.f;
+  // sqrt(s2) as s2 / sqrt(s2); the floor only changes q for s2 < 1e-30,
+  // where b1 rounds to 1 either way
+  float q = s2 * rsqrtf(fmaxf(s2, 1e-30f));
   float b1 = fmaf(s2, fmaf(0.75f, q, -1.5f), 1.0f);
   float t = 2.0f - q;
   float b2 = 0.25f * t * t * t;
