@@ -31,8 +31,9 @@ struct ChunkStage {
 };
 
 // Sums over the chunk's candidates for the K points of this lane.  act[m]
-// marks the lane's valid points; slots[m] (warp-uniform) whether any lane
-// holds a point m.  Returns the compensated sums in sum[]; adds the
+// marks the lane's valid points, and an invalid point's coordinates must be
+// NaN (its s2 is then NaN and no term passes s2 < 4); slots[m]
+// (warp-uniform) tells whether any lane holds a point m.  Returns the compensated sums in sum[]; adds the
 // algorithmic candidate pairs of the lane's points to pairs.
 template <int K>
 __device__ __forceinline__ void chunk_field(const GridView& g, const PartView& P, int cx, int cy, int cz,
@@ -81,7 +82,7 @@ __device__ __forceinline__ void chunk_field(const GridView& g, const PartView& P
         const float y = __fsub_rn(gb.z * bspline_s2(s2), c[m]);
         const float tt = __fadd_rn(s[m], y);
         const float cn = __fsub_rn(__fsub_rn(tt, s[m]), y);
-        const bool hit = act[m] && s2 < 4.0f;
+        const bool hit = s2 < 4.0f;
         s[m] = hit ? tt : s[m];
         c[m] = hit ? cn : c[m];
       }

@@ -330,7 +330,7 @@ __global__ void __launch_bounds__(32 * kEvalWarps, (K > 2 ? 2 : 3)) k_q_eval(QAr
 #pragma unroll
     for (int m = 0; m < K; ++m) {
       q[m] = 0;
-      x[m] = y[m] = z[m] = 0.f;
+      x[m] = y[m] = z[m] = __int_as_float(0x7fc00000);  // NaN: no term for an invalid point
       act[m] = lane + 32 * m < len;
       slots[m] = len > 32 * m;  // warp-uniform
       if (act[m]) {

@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(32 * kGridWarps, 2) k_grid_eval(GridView g, Pa
       const int p = lane + 32 * m;
       act[m] = p < npts;
       slots[m] = npts > 32 * m;  // warp-uniform
-      x[m] = y[m] = z[m] = 0.f;
+      x[m] = y[m] = z[m] = __int_as_float(0x7fc00000);  // NaN: no term for an invalid point
       idx[m] = 0;
       if (act[m]) {
         const int ix = x0 + p % kx, iy = y0 + (p / kx) % ky, iz = z0 + p / (kx * ky);
