@@ -129,7 +129,7 @@ void stage_aniso(pi_frame* f);
 void stage_normals(pi_frame* f);
 void stage_octree(pi_frame* f);
 void stage_extract(pi_frame* f);
-void qef_level(pi_frame* f, long long lb, long long le);
+void qef_level(pi_frame* f, long long lb, long long le, int depth);
 // UniformGrid: lattice of the loadRootBox box; sampling into d_out (device,
 // x fastest) when cap holds it; returns the number of lattice points.
 void uniform_grid_host(const pi_frame* f, float box[6], int steps[3], int dims[3]);

@@ -15,6 +15,8 @@
 // is singular the reference's Matrix4f::inverse yields non-finite values and
 // the vertex is rejected; so is it here, and the number of singular leaves is
 // counted.
+#include <cmath>
+
 #include "device.cuh"
 #include "internal.h"
 
@@ -67,7 +69,12 @@ struct QefArgs {
   float iso;
   float radius;
   long long lb, le;
+  // the level's finite-difference step (every node of a level has the same
+  // half size) as 1 / step and 1 / (2 step), in FP64
+  double i1, i2;
 };
+
+constexpr int kQefThreads = 64;
 
 // LDL^T factorisation of the symmetric 4x4 A (no pivoting) and, when every
 // pivot is at least `floor`, the inverse A^-1 = L^-T diag(1/d) L^-1.
@@ -105,10 +112,15 @@ __device__ int ldlt_inverse4(const double A[4][4], double floor, double Ai[4][4]
 }
 
 // counters: 5 QEF vertices accepted, 6 singular systems, 7 field evaluations
-__global__ void k_qef(QefArgs a, float4* __restrict__ nd_v, const float4* __restrict__ nd_c,
-                      const int8_t* __restrict__ nd_type, const float* __restrict__ nd_samp,
-                      float* __restrict__ qef_err, unsigned long long* __restrict__ counters) {
-  const long long node = a.lb + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, float4* __restrict__ nd_v,
+                                                     const float4* __restrict__ nd_c,
+                                                     const int8_t* __restrict__ nd_type,
+                                                     const float* __restrict__ nd_samp, float* __restrict__ qef_err,
+                                                     unsigned long long* __restrict__ counters) {
+  // the 27 sample values in FP64, converted once per leaf (conversions run on
+  // the FP64 pipe, which bounds this kernel)
+  __shared__ double s_sv[27][kQefThreads];
+  const long long node = a.lb + (long long)blockIdx.x * kQefThreads + threadIdx.x;
   if (node >= a.le || nd_type[node] != Q_LEAF) return;
   const float4 c = nd_c[node];
   const float h = c.w;
@@ -117,27 +129,35 @@ __global__ void k_qef(QefArgs a, float4* __restrict__ nd_v, const float4* __rest
   const float mn[3] = {__fsub_rn(c.x, h), __fsub_rn(c.y, h), __fsub_rn(c.z, h)};
   const float mx[3] = {__fadd_rn(c.x, h), __fadd_rn(c.y, h), __fadd_rn(c.z, h)};
   const float* sv = nd_samp + node * 27;
+  double* const sd = &s_sv[0][threadIdx.x];  // sd[i * kQefThreads] = sample i
+#pragma unroll
+  for (int i = 0; i < 27; ++i) sd[i * kQefThreads] = (double)sv[i];
+  // sample positions (GenerateSampling): three per axis
+  auto lattice = [&](int ax, int k) {
+    return (double)__fadd_rn(__fmul_rn(1.0f - k * 0.5f, mn[ax]), __fmul_rn(k * 0.5f, mx[ax]));
+  };
+  const double px0 = lattice(0, 0), px1 = lattice(0, 1), px2 = lattice(0, 2);
+  const double py0 = lattice(1, 0), py1 = lattice(1, 1), py2 = lattice(1, 2);
+  const double pz0 = lattice(2, 0), pz1 = lattice(2, 1), pz2 = lattice(2, 2);
   // GridEval's finite differences (src/evaluator.cpp:185-240), in FP64 by
   // multiplication with the reciprocal steps
-  const double i1 = 1.0 / (double)step, i2 = 1.0 / (2.0 * (double)step);
+  const double i1 = a.i1, i2 = a.i2;
   double q[15];
 #pragma unroll
   for (int k = 0; k < 15; ++k) q[k] = 0.0;
   for (int i = 0; i < 27; ++i) {
     const int x = i % 3, y = (i / 3) % 3, z = i / 9;
-    // sample position (GenerateSampling)
-    const float t[3] = {x * 0.5f, y * 0.5f, z * 0.5f};
-    const double px = __fadd_rn(__fmul_rn(1.0f - t[0], mn[0]), __fmul_rn(t[0], mx[0]));
-    const double py = __fadd_rn(__fmul_rn(1.0f - t[1], mn[1]), __fmul_rn(t[1], mx[1]));
-    const double pz = __fadd_rn(__fmul_rn(1.0f - t[2], mn[2]), __fmul_rn(t[2], mx[2]));
+    const double px = x == 0 ? px0 : x == 1 ? px1 : px2;
+    const double py = y == 0 ? py0 : y == 1 ? py1 : py2;
+    const double pz = z == 0 ? pz0 : z == 1 ? pz1 : pz2;
     auto fd = [&](int d, int stride) {
-      if (d == 0) return ((double)sv[i] - (double)sv[i + stride]) * i1;
-      if (d == 2) return ((double)sv[i - stride] - (double)sv[i]) * i1;
-      return ((double)sv[i - stride] - (double)sv[i + stride]) * i2;
+      if (d == 0) return (sd[i * kQefThreads] - sd[(i + stride) * kQefThreads]) * i1;
+      if (d == 2) return (sd[(i - stride) * kQefThreads] - sd[i * kQefThreads]) * i1;
+      return (sd[(i - stride) * kQefThreads] - sd[(i + stride) * kQefThreads]) * i2;
     };
     const double gx = fd(x, 1), gy = fd(y, 3), gz = fd(z, 9);
     // plane [g, -1, f - p.g] (NodeCalcNode) accumulated as QEFNormal::combineSelf
-    const double pl[5] = {gx, gy, gz, -1.0, -(px * gx + py * gy + pz * gz) + (double)sv[i]};
+    const double pl[5] = {gx, gy, gz, -1.0, -(px * gx + py * gy + pz * gz) + sd[i * kQefThreads]};
     int idx = 0;
 #pragma unroll
     for (int r = 0; r < 5; ++r)
@@ -258,13 +278,22 @@ __global__ void k_qef(QefArgs a, float4* __restrict__ nd_v, const float4* __rest
   if (qef_err) qef_err[node] = err;
 }
 
-void qef_level(pi_frame* f, long long lb, long long le) {
+void qef_level(pi_frame* f, long long lb, long long le, int depth) {
   cudaStream_t s = f->ctx->stream;
   const GridHost& gh = f->g;
+  // half size of the level's nodes (the root's halved exactly per level);
+  // the step of GridEval is cellsize / 2 = that half size
+  const float step = std::ldexp(f->rootH, -depth);
   QefArgs qa{GridView{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p},
-             PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p}, f->iso, f->P.radius, lb, le};
-  PI_LAUNCH(k_qef, div_up(le - lb, 64), 64, 0, s, qa, f->nd_v.p, f->nd_c.p, f->nd_type.p, f->nd_samp.p, nullptr,
-            f->dcount.p);
+             PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p},
+             f->iso,
+             f->P.radius,
+             lb,
+             le,
+             1.0 / (double)step,
+             1.0 / (2.0 * (double)step)};
+  PI_LAUNCH(k_qef, div_up(le - lb, kQefThreads), kQefThreads, 0, s, qa, f->nd_v.p, f->nd_c.p, f->nd_type.p,
+            f->nd_samp.p, nullptr, f->dcount.p);
 }
 
 }  // namespace pisurf
