@@ -420,12 +420,21 @@ class Clocks:
         self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
 
     def start(self):
+        """Starts the sampler and returns once its first sample is written, so
+        that nvidia-smi's own start-up (process, NVML) lies before the timed
+        region rather than inside its first steps."""
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.tmp, stderr=subprocess.DEVNULL)
+                 "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.tmp, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+            return
+        t0 = time.time()
+        while time.time() - t0 < 1.5 and self.proc.poll() is None:
+            if os.path.getsize(self.tmp.name) > 0:
+                break
+            time.sleep(0.01)
 
     def stop(self):
         if self.proc is None:

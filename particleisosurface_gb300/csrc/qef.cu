@@ -162,8 +162,10 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, float4* __restri
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
-      for (int s2 = r; s2 < 5; ++s2) q[idx++] += pl[r] * pl[s2];
+      for (int s2 = r; s2 < 5; ++s2, ++idx)
+        if (idx != 12) q[idx] += pl[r] * pl[s2];
   }
+  q[12] = 27.0;  // the (-1) x (-1) entry: 27 ones
   double A[4][4], B[4];
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
