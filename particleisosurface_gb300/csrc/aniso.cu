@@ -249,9 +249,7 @@ void stage_aniso(pi_frame* f) {
   PI_LAUNCH(k_xmean, div_up(n, 128), 128, 0, s, g, f->pos.p, n, nI, nI2, inv_h3, c_mean, f->nrm.p, f->xlo.p);
   PI_LAUNCH(k_cov_G, div_up(n, 128), 128, 0, s, g, f->pos.p, f->nrm.p, f->xlo.p, f->xm.p, n, nI, nI2, inv_h3, f->influ2,
             1.0f / h, f->sigma, f->ga.p, f->gb.p, f->gfull.p, f->det.p, f->f64flag.p, f->dcount.p);
-  unsigned long long c[8];
-  counters_read(f, c);
-  f->fp64Count = (long long)c[0];
+  counters_snapshot(f, kPinAniso);
 }
 
 }  // namespace pisurf

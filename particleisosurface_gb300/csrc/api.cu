@@ -124,6 +124,60 @@ void counters_read(pi_frame* f, unsigned long long out[8]) {
   }
 }
 
+void counters_snapshot(pi_frame* f, int slot) {
+  PI_CUDA(cudaMemcpyAsync(f->ctx->hpin + (size_t)slot * kCounterWords, f->dcount.p,
+                          sizeof(unsigned long long) * kCounterWords, cudaMemcpyDeviceToHost, f->ctx->stream));
+  f->pin_pending |= 1 << slot;
+}
+
+static void fold_counters(const unsigned long long* h, unsigned long long out[8]) {
+  for (int w = 0; w < 8; ++w) {
+    out[w] = 0;
+    for (int k = 0; k < kStripes; ++k) out[w] += h[((size_t)w * kStripes + k) * 4];
+  }
+}
+
+void resolve_pending(pi_frame* f) {
+  if (!f->ev_pending && !f->pin_pending) return;
+  PI_CUDA(cudaStreamSynchronize(f->ctx->stream));
+  for (int k = 0; k < 8; ++k)
+    if (f->ev_pending & (1 << k)) {
+      float ms = 0;
+      PI_CUDA(cudaEventElapsedTime(&ms, f->ev[2 * k], f->ev[2 * k + 1]));
+      f->stage_ms[k] += ms;
+    }
+  f->ev_pending = 0;
+  const unsigned long long* h = f->ctx->hpin;
+  unsigned long long c[8];
+  if (f->pin_pending & (1 << kPinAniso)) {
+    fold_counters(h + (size_t)kPinAniso * kCounterWords, c);
+    f->fp64Count = (long long)c[0];
+  }
+  if (f->pin_pending & (1 << kPinOctree)) {
+    fold_counters(h + (size_t)kPinOctree * kCounterWords, c);
+    f->fieldEvals = (long long)c[0] + (long long)c[7];
+    f->pairs = (long long)c[1];
+    f->qefAccepted = (long long)c[5];
+    f->qefSingular = (long long)c[6];
+    if (f->ctx->profile) {
+      f->ctx->kernel_pairs += f->pairs;
+      f->ctx->kernel_evals += f->fieldEvals;
+    }
+  }
+  if (f->pin_pending & (1 << kPinExtract)) {
+    fold_counters(h + (size_t)kPinExtract * kCounterWords, c);
+    f->nDual = (long long)c[2];
+    f->bisectEvals = (long long)c[3];
+    f->fieldEvals += (long long)c[3];
+    f->pairs += (long long)c[4];
+  }
+  if (f->pin_pending & (1 << kPinValid)) {
+    const int valid = *reinterpret_cast<const int*>(h + (size_t)kPinSlots * kCounterWords);
+    f->g.nInvalid = (int)(f->N - valid);
+  }
+  f->pin_pending = 0;
+}
+
 void prof_begin(pi_ctx* c, cudaStream_t s) {
   if (!c->profile) return;
   cudaEvent_t e;
@@ -174,12 +228,9 @@ static void ev_record(pi_frame* f, int i) {
   if (!f->ev[i]) PI_CUDA(cudaEventCreate(&f->ev[i]));
   PI_CUDA(cudaEventRecord(f->ev[i], f->ctx->stream));
 }
-static void ev_close(pi_frame* f, int stage_slot, int a, int b) {
-  PI_CUDA(cudaEventSynchronize(f->ev[b]));
-  float ms = 0;
-  PI_CUDA(cudaEventElapsedTime(&ms, f->ev[a], f->ev[b]));
-  f->stage_ms[stage_slot] += ms;
-}
+// Stage slot k's time is read by resolve_pending, at the end of the API call
+// (or, for an upload, at the next one that synchronises).
+static void ev_close(pi_frame* f, int stage_slot) { f->ev_pending |= 1 << stage_slot; }
 
 static void need(const pi_frame* f, int stage) {
   if (f->stage < stage) throw StateError("stage called before the stages it depends on");
@@ -199,7 +250,8 @@ static void run_stage(pi_frame* f, int target) {
   static const char* const names[7] = {"", "", "pisurf hash grid", "pisurf anisotropy", "pisurf normals",
                                         "pisurf octree", "pisurf extraction"};
   NvtxRange range(names[target]);
-  ev_record(f, 0);
+  const int slot = target == 2 ? 1 : target == 3 ? 2 : target == 4 ? 3 : target == 5 ? 4 : 6;
+  ev_record(f, 2 * slot);
   switch (target) {
     case 2:
       stage_hashgrid(f);
@@ -216,18 +268,13 @@ static void run_stage(pi_frame* f, int target) {
       break;
     case 5:
       stage_octree(f);
-      if (f->ctx->profile) {
-        f->ctx->kernel_pairs += f->pairs;
-        f->ctx->kernel_evals += f->fieldEvals;
-      }
       break;
     case 6:
       stage_extract(f);
       break;
   }
-  ev_record(f, 1);
-  const int slot = target == 2 ? 1 : target == 3 ? 2 : target == 4 ? 3 : target == 5 ? 4 : 6;
-  ev_close(f, slot, 0, 1);
+  ev_record(f, 2 * slot + 1);
+  ev_close(f, slot);
   f->stage = target;
 }
 
@@ -312,6 +359,7 @@ int pi_ctx_create(int device, size_t budget_bytes, pi_ctx** out) {
   PI_CUDA(cudaSetDevice(device));
   PI_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   PI_CUDA(cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, device));
+  PI_CUDA(cudaMallocHost(&c->hpin, sizeof(unsigned long long) * ((size_t)kPinSlots * kCounterWords + 8)));
   cudaMemPool_t pool;
   PI_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
   uint64_t thr = UINT64_MAX;
@@ -325,6 +373,7 @@ static void ctx_release(pi_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   for (auto e : c->prof_events) cudaEventDestroy(e);
+  if (c->hpin) cudaFreeHost(c->hpin);
   cudaStreamDestroy(c->stream);
   (void)cudaGetLastError();
   delete c;
@@ -430,7 +479,7 @@ int pi_frame_upload(pi_frame* f, const float* xyz, int64_t n) {
   ev_record(f, 0);
   stage_upload_host(f, xyz, n);
   ev_record(f, 1);
-  ev_close(f, 0, 0, 1);
+  ev_close(f, 0);
   f->stage = 1;
   PI_API_END
 }
@@ -452,6 +501,7 @@ int pi_frame_reset(pi_frame* f) {
   f->stage = 1;
   f->nNodes = f->nV = f->nT = f->nDual = 0;
   f->fieldEvals = f->pairs = f->bisectEvals = f->fp64Count = f->nLeaves = f->nEmpty = 0;
+  f->ev_pending = f->pin_pending = 0;
   for (int k = 0; k < 8; ++k) f->stage_ms[k] = 0;
   PI_API_END
 }
@@ -461,6 +511,7 @@ int pi_hashgrid_build(pi_frame* f) {
   PI_CHECK(f, "frame is null");
   set_device(f->ctx);
   run_stage(f, 2);
+  resolve_pending(f);
   PI_API_END
 }
 int pi_aniso_compute(pi_frame* f) {
@@ -468,6 +519,7 @@ int pi_aniso_compute(pi_frame* f) {
   PI_CHECK(f, "frame is null");
   set_device(f->ctx);
   run_stage(f, 3);
+  resolve_pending(f);
   PI_API_END
 }
 int pi_normals_compute(pi_frame* f) {
@@ -475,6 +527,7 @@ int pi_normals_compute(pi_frame* f) {
   PI_CHECK(f, "frame is null");
   set_device(f->ctx);
   run_stage(f, 4);
+  resolve_pending(f);
   PI_API_END
 }
 int pi_octree_build(pi_frame* f) {
@@ -482,6 +535,7 @@ int pi_octree_build(pi_frame* f) {
   PI_CHECK(f, "frame is null");
   set_device(f->ctx);
   run_stage(f, 5);
+  resolve_pending(f);
   PI_API_END
 }
 int pi_extract_mesh(pi_frame* f) {
@@ -489,6 +543,7 @@ int pi_extract_mesh(pi_frame* f) {
   PI_CHECK(f, "frame is null");
   set_device(f->ctx);
   run_stage(f, 6);
+  resolve_pending(f);
   PI_API_END
 }
 // One JSON line per completed frame, appended to the file named by the
@@ -519,6 +574,7 @@ int pi_run(pi_frame* f) {
   need(f, 1);
   const bool fresh = f->stage < 6;
   for (int t = 2; t <= 6; ++t) run_stage(f, t);
+  resolve_pending(f);
   if (fresh) metrics_record(f);
   PI_API_END
 }
@@ -526,6 +582,7 @@ int pi_run(pi_frame* f) {
 int pi_frame_info_get(const pi_frame* f, pi_frame_info* o) {
   PI_API_BEGIN
   PI_CHECK(f && o, "null argument");
+  resolve_pending(const_cast<pi_frame*>(f));
   std::memset(o, 0, sizeof(*o));
   o->num_particles = f->N;
   o->num_invalid_keys = f->g.nInvalid;

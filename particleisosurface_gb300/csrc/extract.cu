@@ -657,12 +657,7 @@ void stage_extract(pi_frame* f) {
   f->nT = nt;
   f->mt.alloc(c, s, nt * 3 > 0 ? nt * 3 : 3);
   PI_LAUNCH(k_tri_write, div_up(nt0, 256), 256, 0, s, nt0, trank.p, otri.p, f->mt.p);
-  unsigned long long bc[8];
-  counters_read(f, bc);
-  f->nDual = (long long)bc[2];
-  f->bisectEvals = (long long)bc[3];
-  f->fieldEvals += (long long)bc[3];
-  f->pairs += (long long)bc[4];
+  counters_snapshot(f, kPinExtract);
 }
 
 }  // namespace pisurf

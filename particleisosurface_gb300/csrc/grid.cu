@@ -175,10 +175,11 @@ void stage_hashgrid(pi_frame* f) {
   exclusive_scan_i32(f->off.p, f->off.p, g.cellNum + 1, nullptr, f->tmp.p, s);
   f->pos.alloc(f->ctx, s, n);
   PI_LAUNCH(k_gather_pos, div_up(n, 256), 256, 0, s, f->xyz.p, f->sidx.p, n, f->pos.p);
-  int valid = 0;
-  PI_CUDA(cudaMemcpyAsync(&valid, f->off.p + g.cellNum, sizeof(int), cudaMemcpyDeviceToHost, s));
-  PI_CUDA(cudaStreamSynchronize(s));
-  g.nInvalid = (int)(n - valid);
+  // the valid-key count (offset table total) reaches g.nInvalid in
+  // resolve_pending; nothing before the end of the call reads it
+  PI_CUDA(cudaMemcpyAsync(reinterpret_cast<int*>(f->ctx->hpin + (size_t)kPinSlots * kCounterWords),
+                          f->off.p + g.cellNum, sizeof(int), cudaMemcpyDeviceToHost, s));
+  f->pin_pending |= 1 << kPinValid;
   // loadRootBox result kept for the octree root (resizeRootBoxConstR)
   for (int k2 = 0; k2 < 6; ++k2) f->bbox6[k2] = bb[k2];
 }

@@ -63,6 +63,11 @@ struct pi_ctx {
   // 0 = not chosen yet (timed on the first such level), forced by pi_ctx_tune
   int eval_lanes[2] = {0, 0};
   int eval_forced = 0;
+  // pinned host area for reads that need no synchronisation of their own:
+  // per-stage counter snapshots (kPinSlots x kCounterWords words) and one
+  // word for the hash grid's valid-key count; folded into the frame at the
+  // end of the API call that produced them
+  unsigned long long* hpin = nullptr;
 };
 
 struct pi_frame {
@@ -116,11 +121,25 @@ struct pi_frame {
   long long qefAccepted = 0, qefSingular = 0;
   long long gridPairs = 0;  // candidate pairs of the last uniform-grid sampling
   pisurf::DBuf<unsigned long long> dcount;  // device counters
-  cudaEvent_t ev[9] = {};
+  // stage timing: ev[2k], ev[2k+1] bracket stage slot k; the times are read
+  // when the frame's next synchronisation point has passed
+  cudaEvent_t ev[16] = {};
+  int ev_pending = 0;   // bit k: slot k's events recorded, time not read yet
+  int pin_pending = 0;  // bit k: pinned slot k written by this call, not folded yet
   float stage_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 namespace pisurf {
+
+// pinned snapshot slots
+constexpr int kPinAniso = 0, kPinOctree = 1, kPinExtract = 2, kPinSlots = 3;
+constexpr int kPinValid = kPinSlots;  // bit of pin_pending for the valid-key count
+// Copies the frame's device counters into pinned slot `slot` (stream-ordered,
+// no synchronisation); the values reach the frame in resolve_pending.
+void counters_snapshot(pi_frame* f, int slot);
+// Waits for the context stream once and folds every pending stage time and
+// counter snapshot into the frame.
+void resolve_pending(pi_frame* f);
 
 void stage_upload_host(pi_frame* f, const float* xyz, long long n);
 void stage_upload_device(pi_frame* f, const float* d_xyz, long long n);

@@ -891,13 +891,7 @@ void stage_octree(pi_frame* f) {
     lb = le;
     le = le + newn;
   }
-  unsigned long long cnt[8];
-  counters_read(f, cnt);
-  f->fieldEvals = (long long)cnt[0];
-  f->pairs = (long long)cnt[1];
-  f->qefAccepted = (long long)cnt[5];
-  f->qefSingular = (long long)cnt[6];
-  f->fieldEvals += (long long)cnt[7];
+  counters_snapshot(f, kPinOctree);
 }
 
 }  // namespace pisurf

@@ -79,16 +79,24 @@ __global__ void k_scan_top(int* __restrict__ sums, int nb, int* __restrict__ d_t
   if (threadIdx.x == 0 && d_total) *d_total = carry;
 }
 
+// Tile index with one padding word per 32, so that a thread's run of
+// kItems consecutive elements and a warp's coalesced row both fall in
+// distinct banks.
+__device__ __forceinline__ int tpad(int i) { return i + (i >> 5); }
+
+// Down-sweep of one tile: the block's exclusive scan plus the tile's offset
+// (sums[blockIdx.x]; 0 when sums is null, the single-tile case, which also
+// writes the total to *d_total when given).
 __global__ void k_scan_down(const int* __restrict__ in, int* __restrict__ out, long long n,
-                            const int* __restrict__ sums) {
-  __shared__ int s_tile[kTile];
+                            const int* __restrict__ sums, int* __restrict__ d_total) {
+  __shared__ int s_tile[kTile + kTile / 32];
   __shared__ int s_warp[32];
   __shared__ int s_total;
   long long base = (long long)blockIdx.x * kTile;
 #pragma unroll
   for (int i = 0; i < kItems; ++i) {
     long long idx = base + (long long)i * kThreads + threadIdx.x;
-    s_tile[i * kThreads + threadIdx.x] = idx < n ? in[idx] : 0;
+    s_tile[tpad(i * kThreads + threadIdx.x)] = idx < n ? in[idx] : 0;
   }
   __syncthreads();
   int loc[kItems];
@@ -96,16 +104,17 @@ __global__ void k_scan_down(const int* __restrict__ in, int* __restrict__ out, l
 #pragma unroll
   for (int i = 0; i < kItems; ++i) {
     loc[i] = acc;
-    acc += s_tile[threadIdx.x * kItems + i];
+    acc += s_tile[tpad(threadIdx.x * kItems + i)];
   }
-  int ex = block_excl_scan<kThreads>(acc, s_warp, &s_total) + sums[blockIdx.x];
+  int ex = block_excl_scan<kThreads>(acc, s_warp, &s_total) + (sums ? sums[blockIdx.x] : 0);
+  if (!sums && d_total && threadIdx.x == 0) *d_total = s_total;
 #pragma unroll
-  for (int i = 0; i < kItems; ++i) s_tile[threadIdx.x * kItems + i] = ex + loc[i];
+  for (int i = 0; i < kItems; ++i) s_tile[tpad(threadIdx.x * kItems + i)] = ex + loc[i];
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < kItems; ++i) {
     long long idx = base + (long long)i * kThreads + threadIdx.x;
-    if (idx < n) out[idx] = s_tile[i * kThreads + threadIdx.x];
+    if (idx < n) out[idx] = s_tile[tpad(i * kThreads + threadIdx.x)];
   }
 }
 
@@ -118,9 +127,13 @@ void exclusive_scan_i32(const int* in, int* out, long long n, int* d_total, int*
     return;
   }
   unsigned nb = div_up(n, kTile);
+  if (nb == 1) {  // one tile: one launch
+    PI_LAUNCH(k_scan_down, 1, kThreads, 0, s, in, out, n, nullptr, d_total);
+    return;
+  }
   PI_LAUNCH(k_scan_reduce, nb, kThreads, 0, s, in, n, tmp);
   PI_LAUNCH(k_scan_top, 1, 1024, 0, s, tmp, (int)nb, d_total);
-  PI_LAUNCH(k_scan_down, nb, kThreads, 0, s, in, out, n, tmp);
+  PI_LAUNCH(k_scan_down, nb, kThreads, 0, s, in, out, n, tmp, nullptr);
 }
 
 // ---------------------------------------------------------------------------
