@@ -359,7 +359,7 @@ int pi_ctx_create(int device, size_t budget_bytes, pi_ctx** out) {
   PI_CUDA(cudaSetDevice(device));
   PI_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   PI_CUDA(cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, device));
-  PI_CUDA(cudaMallocHost(&c->hpin, sizeof(unsigned long long) * ((size_t)kPinSlots * kCounterWords + 8)));
+  PI_CUDA(cudaMallocHost(&c->hpin, sizeof(unsigned long long) * (size_t)kPinWords));
   cudaMemPool_t pool;
   PI_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
   uint64_t thr = UINT64_MAX;

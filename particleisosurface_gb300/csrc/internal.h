@@ -123,7 +123,7 @@ struct pi_frame {
   pisurf::DBuf<unsigned long long> dcount;  // device counters
   // stage timing: ev[2k], ev[2k+1] bracket stage slot k; the times are read
   // when the frame's next synchronisation point has passed
-  cudaEvent_t ev[16] = {};
+  cudaEvent_t ev[17] = {};
   int ev_pending = 0;   // bit k: slot k's events recorded, time not read yet
   int pin_pending = 0;  // bit k: pinned slot k written by this call, not folded yet
   float stage_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -134,6 +134,11 @@ namespace pisurf {
 // pinned snapshot slots
 constexpr int kPinAniso = 0, kPinOctree = 1, kPinExtract = 2, kPinSlots = 3;
 constexpr int kPinValid = kPinSlots;  // bit of pin_pending for the valid-key count
+// after the slots: word 0 the valid-key count, word 1 the octree level's
+// INTERNAL count
+constexpr int kPinWords = kPinSlots * kCounterWords + 8;
+// event that marks the INTERNAL count's copy in the octree level loop
+constexpr int kLevelEvent = 16;
 // Copies the frame's device counters into pinned slot `slot` (stream-ordered,
 // no synchronisation); the values reach the frame in resolve_pending.
 void counters_snapshot(pi_frame* f, int slot);

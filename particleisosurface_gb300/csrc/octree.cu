@@ -779,6 +779,7 @@ void stage_octree(pi_frame* f) {
   f->nNodes = 0;
   f->levelBegin.clear();
   ensure_nodes(f, 1 << 16);
+  if (!f->ev[kLevelEvent]) PI_CUDA(cudaEventCreateWithFlags(&f->ev[kLevelEvent], cudaEventDisableTiming));
   PI_LAUNCH(k_root, 1, 1, 0, s, f->rootC[0], f->rootC[1], f->rootC[2], f->rootH, 1 << f->dmax, f->nd_c.p,
             f->nd_v.p, f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p,
             f->nd_curv.p, f->nd_org.p);
@@ -861,12 +862,15 @@ void stage_octree(pi_frame* f) {
     PI_LAUNCH(k_internal_flag, div_up(nl, 256), 256, 0, s, f->nd_type.p, lb, le, flag.p);
     PI_CUDA(cudaMemsetAsync(flag.p + nl, 0, sizeof(int), s));
     exclusive_scan_i32(flag.p, flag.p, nl + 1, nullptr, f->tmp.p, s);
-    int nint = 0;
-    PI_CUDA(cudaMemcpyAsync(&nint, flag.p + nl, sizeof(int), cudaMemcpyDeviceToHost, s));
-    PI_CUDA(cudaStreamSynchronize(s));
-    const long long newn = 8LL * nint;
-    ensure_nodes(f, le + newn);
-    known = nint > 0 && depth + 1 >= f->dmin && depth < f->dmax;
+    // the number of INTERNAL nodes goes to pinned host memory and is read
+    // while the spawn kernel runs, so that the device is still busy when the
+    // host sizes the next level
+    int* const nint_h = reinterpret_cast<int*>(ctx->hpin + kPinSlots * kCounterWords + 1);
+    PI_CUDA(cudaMemcpyAsync(nint_h, flag.p + nl, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PI_CUDA(cudaEventRecord(f->ev[kLevelEvent], s));
+    f->nNodes = le;
+    ensure_nodes(f, le + 8 * nl);  // room for the children: at most 8 per node of the level
+    known = depth + 1 >= f->dmin && depth < f->dmax;
     if (known) {
       // leaves by size never read their curvature (afterSampleEval returns
       // before the curvature test), so their parents only settle emptiness
@@ -885,6 +889,9 @@ void stage_octree(pi_frame* f) {
                 f->nd_v.p, f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p,
                 f->nd_curv.p, f->nd_org.p);
     }
+    PI_CUDA(cudaEventSynchronize(f->ev[kLevelEvent]));
+    const int nint = *nint_h;
+    const long long newn = 8LL * nint;
     f->nNodes = le + newn;
     // depth D_max nodes are leaves by size, so nothing spawns past it
     if (nint == 0 || depth >= f->dmax) break;
