@@ -212,7 +212,10 @@ int pi_mesh_write_ply(pi_frame* f, const char* path);
 
 /* One call, host in / host out: upload, Run, download (the e2e path of a
  * frame).  verts/tris must hold max_verts / max_tris entries; the actual
- * counts are returned (PI_ERR_LIMIT if the buffers are too small). */
+ * counts are returned (PI_ERR_LIMIT if the buffers are too small).  A
+ * context created without a budget keeps the frame of this call for the
+ * next one (its device buffers stay allocated until pi_ctx_destroy); with a
+ * budget the frame's memory is returned before the call ends. */
 int pi_reconstruct(pi_ctx* ctx, const pi_params* params, const float* xyz, int64_t n, float* verts,
                    int64_t max_verts, int32_t* tris, int64_t max_tris, int64_t* nverts,
                    int64_t* ntris);

@@ -68,6 +68,7 @@ void DBuf<T>::grow(pi_ctx* c, cudaStream_t st, size_t count, size_t keep) {
   n = 0;
   alloc(c, st, count);
   if (old) {
+    keep = keep < oldn ? keep : oldn;  // never past the old allocation
     if (keep) PI_CUDA(cudaMemcpyAsync(p, old, keep * sizeof(T), cudaMemcpyDeviceToDevice, st));
     cudaFreeAsync(old, os);
     ctx_account(oc, -(long long)(oldn * sizeof(T)));
@@ -382,6 +383,11 @@ static void ctx_release(pi_ctx* c) {
 int pi_ctx_destroy(pi_ctx* c) {
   PI_API_BEGIN
   if (!c) return PI_OK;
+  if (c->recon) {
+    pi_frame* r = c->recon;
+    c->recon = nullptr;
+    pi_frame_destroy(r);
+  }
   // frames still alive keep the context (and its stream) until they are destroyed
   ctx_release(c);
   PI_API_END
@@ -445,11 +451,26 @@ int pi_ctx_tuning(const pi_ctx* c, int32_t* out2) {
   PI_API_END
 }
 
+static void check_params(const pi_params* p) {
+  PI_CHECK(std::isfinite(p->radius) && p->radius > 0, "radius must be positive");
+  PI_CHECK(std::isfinite(p->smooth_factor) && p->smooth_factor > 0, "smooth_factor must be positive");
+}
+
+// Back to `stage` (0: nothing uploaded, 1: particles uploaded) with every
+// result and counter cleared; device buffers are kept for reuse.
+static void frame_clear(pi_frame* f, int stage) {
+  f->stage = stage;
+  f->nNodes = f->nV = f->nT = f->nDual = 0;
+  f->fieldEvals = f->pairs = f->bisectEvals = f->fp64Count = f->nLeaves = f->nEmpty = 0;
+  f->qefAccepted = f->qefSingular = 0;
+  f->ev_pending = f->pin_pending = 0;
+  for (int k = 0; k < 8; ++k) f->stage_ms[k] = 0;
+}
+
 int pi_frame_create(pi_ctx* c, const pi_params* p, pi_frame** out) {
   PI_API_BEGIN
   PI_CHECK(c && p && out, "null argument");
-  PI_CHECK(std::isfinite(p->radius) && p->radius > 0, "radius must be positive");
-  PI_CHECK(std::isfinite(p->smooth_factor) && p->smooth_factor > 0, "smooth_factor must be positive");
+  check_params(p);
   *out = nullptr;
   pi_frame* f = new pi_frame();
   f->ctx = c;
@@ -498,11 +519,7 @@ int pi_frame_reset(pi_frame* f) {
   PI_API_BEGIN
   PI_CHECK(f, "frame is null");
   need(f, 1);
-  f->stage = 1;
-  f->nNodes = f->nV = f->nT = f->nDual = 0;
-  f->fieldEvals = f->pairs = f->bisectEvals = f->fp64Count = f->nLeaves = f->nEmpty = 0;
-  f->ev_pending = f->pin_pending = 0;
-  for (int k = 0; k < 8; ++k) f->stage_ms[k] = 0;
+  frame_clear(f, 1);
   PI_API_END
 }
 
@@ -962,13 +979,29 @@ int pi_reconstruct(pi_ctx* c, const pi_params* p, const float* xyz, int64_t n, f
                    int32_t* tris, int64_t max_tris, int64_t* nverts, int64_t* ntris) {
   PI_API_BEGIN
   PI_CHECK(c && p && xyz && nverts && ntris, "null argument");
+  check_params(p);
+  // without a budget the context keeps this call's frame for the next one,
+  // so that its device buffers and events carry over; with a budget the
+  // frame's memory is returned at the end of the call
+  const bool keep = c->budget == 0;
   pi_frame* f = nullptr;
-  int rc = pi_frame_create(c, p, &f);
-  if (rc) return rc;
+  if (keep && c->recon) {
+    f = c->recon;
+    f->P = *p;
+    frame_clear(f, 0);
+  } else {
+    int rc = pi_frame_create(c, p, &f);
+    if (rc) return rc;
+    if (keep) c->recon = f;
+  }
   struct Guard {
     pi_frame* f;
-    ~Guard() { pi_frame_destroy(f); }
-  } guard{f};
+    bool keep;
+    ~Guard() {
+      if (!keep) pi_frame_destroy(f);
+    }
+  } guard{f, keep};
+  int rc = 0;
   rc = pi_frame_upload(f, xyz, n);
   if (rc) return rc;
   rc = pi_run(f);

@@ -68,6 +68,10 @@ struct pi_ctx {
   // word for the hash grid's valid-key count; folded into the frame at the
   // end of the API call that produced them
   unsigned long long* hpin = nullptr;
+  // the frame pi_reconstruct reuses from call to call when the context has
+  // no budget (its device buffers and events carry over); freed with the
+  // context
+  pi_frame* recon = nullptr;
 };
 
 struct pi_frame {

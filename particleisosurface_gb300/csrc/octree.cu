@@ -754,7 +754,11 @@ static int eval_lanes_for(pi_frame* f, int kind, const QArgs& qa, long long qn, 
 }
 
 static void ensure_nodes(pi_frame* f, long long need) {
-  if ((long long)f->nd_c.n >= need) return;
+  // the QEF samples exist only in QEF mode, so a frame that switches it on
+  // (pi_reconstruct reuses its frame across parameters) may hold node arrays
+  // large enough and no samples yet
+  const bool samp_ok = !f->P.qef || (long long)f->nd_samp.n >= need * 27;
+  if ((long long)f->nd_c.n >= need && samp_ok) return;
   long long cap = std::max<long long>(need, (long long)(f->nd_c.n * 3 / 2) + 1024);
   pi_ctx* c = f->ctx;
   cudaStream_t s = c->stream;

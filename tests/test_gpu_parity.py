@@ -200,6 +200,36 @@ def test_reconstruct_host_roundtrip(ctx):
     np.testing.assert_array_equal(t, t2)
 
 
+def test_reconstruct_reuses_its_frame(ctx):
+    """pi_reconstruct keeps one frame per context (no budget): calls on
+    different inputs and parameters in a row, a failed call among them, each
+    give what a fresh frame gives."""
+    a = synth.small_blob(n=1500, seed=9)
+    b = synth.slab_and_sphere(n=6000, seed=7)
+
+    def fresh(fr, qef=False):
+        g = N.Frame(ctx, N.default_params(fr.radius, qef=qef)).upload(fr.xyz).run()
+        m = g.mesh()
+        g.close()
+        return m
+
+    want_a, want_b, want_bq = fresh(a), fresh(b), fresh(b, qef=True)
+    bad = np.zeros((10, 3), np.float32)
+    bad[3, 1] = np.nan
+    for fr, params, want in ((a, N.default_params(a.radius), want_a),
+                             (b, N.default_params(b.radius), want_b),
+                             (bad, N.default_params(0.01), None),
+                             (b, N.default_params(b.radius, qef=True), want_bq),
+                             (a, N.default_params(a.radius), want_a)):
+        if want is None:
+            with pytest.raises(N.PiError):
+                ctx.reconstruct(fr, params)
+            continue
+        v, t = ctx.reconstruct(fr.xyz, params)
+        np.testing.assert_array_equal(v, want[0])
+        np.testing.assert_array_equal(t, want[1])
+
+
 def test_invalid_input_reported(ctx):
     xyz = np.zeros((10, 3), np.float32)
     xyz[3, 1] = np.nan
