@@ -361,6 +361,9 @@ int pi_ctx_create(int device, size_t budget_bytes, pi_ctx** out) {
   PI_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   PI_CUDA(cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, device));
   PI_CUDA(cudaMallocHost(&c->hpin, sizeof(unsigned long long) * (size_t)kPinWords));
+  PI_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  PI_CUDA(cudaEventCreateWithFlags(&c->ev_tris_ready, cudaEventDisableTiming));
+  PI_CUDA(cudaEventCreateWithFlags(&c->ev_tris_copied, cudaEventDisableTiming));
   cudaMemPool_t pool;
   PI_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
   uint64_t thr = UINT64_MAX;
@@ -375,6 +378,12 @@ static void ctx_release(pi_ctx* c) {
   cudaStreamSynchronize(c->stream);
   for (auto e : c->prof_events) cudaEventDestroy(e);
   if (c->hpin) cudaFreeHost(c->hpin);
+  if (c->copy_stream) {
+    cudaStreamSynchronize(c->copy_stream);
+    cudaStreamDestroy(c->copy_stream);
+  }
+  if (c->ev_tris_ready) cudaEventDestroy(c->ev_tris_ready);
+  if (c->ev_tris_copied) cudaEventDestroy(c->ev_tris_copied);
   cudaStreamDestroy(c->stream);
   (void)cudaGetLastError();
   delete c;
@@ -998,9 +1007,18 @@ int pi_reconstruct(pi_ctx* c, const pi_params* p, const float* xyz, int64_t n, f
     pi_frame* f;
     bool keep;
     ~Guard() {
+      // the triangle copy reads the frame and writes the caller's buffer:
+      // it ends before the call does, on every path
+      if (f->tris_sent) cudaEventSynchronize(f->ctx->ev_tris_copied);
+      f->host_tris = nullptr;
+      f->host_tcap = 0;
+      f->tris_sent = false;
       if (!keep) pi_frame_destroy(f);
     }
   } guard{f, keep};
+  f->host_tris = tris;
+  f->host_tcap = tris ? max_tris : 0;
+  f->tris_sent = false;
   int rc = 0;
   rc = pi_frame_upload(f, xyz, n);
   if (rc) return rc;
@@ -1009,7 +1027,7 @@ int pi_reconstruct(pi_ctx* c, const pi_params* p, const float* xyz, int64_t n, f
   *nverts = f->nV;
   *ntris = f->nT;
   if (f->nV > max_verts || f->nT > max_tris) throw std::length_error("mesh buffers too small");
-  rc = pi_mesh_get(f, verts, tris, nullptr);
+  rc = pi_mesh_get(f, verts, f->tris_sent ? nullptr : tris, nullptr);
   if (rc) return rc;
   PI_API_END
 }

@@ -614,7 +614,34 @@ void stage_extract(pi_frame* f) {
   vrank.release();
   khi.release();
   klo.release();
-  // 6. vertex positions by bisection
+  // 6. triangles: first of each sorted vertex triple, in generation order
+  // (they need the vertex numbering, not the positions, so they come before
+  // the bisection and, for a host destination, their copy overlaps it)
+  DBuf<int> otri, trank;
+  DBuf<unsigned> ttab;
+  DBuf<uint32_t> twhere;
+  otri.alloc(c, s, nt0 * 3 > 0 ? nt0 * 3 : 3);
+  PI_LAUNCH(k_tri_orient, div_up(nt0, 256), 256, 0, s, nt0, slot_vertex.p, tflip.p, otri.p);
+  const uint32_t tmask = table_mask(nt0);
+  ttab.alloc(c, s, (size_t)tmask + 1);
+  twhere.alloc(c, s, nt0 > 0 ? nt0 : 1);
+  trank.alloc(c, s, nt0 + 1);
+  PI_CUDA(cudaMemsetAsync(ttab.p, 0, sizeof(unsigned) * ((size_t)tmask + 1), s));
+  PI_LAUNCH(k_tri_insert, div_up(nt0, 256), 256, 0, s, nt0, otri.p, tmask, ttab.p, twhere.p);
+  PI_LAUNCH(k_first_flag, div_up(nt0 + 1, 256), 256, 0, s, nt0, ttab.p, twhere.p, trank.p);
+  exclusive_scan_i32(trank.p, trank.p, nt0 + 1, nullptr, tmp.p, s);
+  const long long nt = read_int(f, trank.p + nt0);
+  f->nT = nt;
+  f->mt.alloc(c, s, nt * 3 > 0 ? nt * 3 : 3);
+  PI_LAUNCH(k_tri_write, div_up(nt0, 256), 256, 0, s, nt0, trank.p, otri.p, f->mt.p);
+  if (f->host_tris && nt > 0 && nt <= f->host_tcap) {
+    PI_CUDA(cudaEventRecord(c->ev_tris_ready, s));
+    PI_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_tris_ready, 0));
+    PI_CUDA(cudaMemcpyAsync(f->host_tris, f->mt.p, sizeof(int) * 3 * nt, cudaMemcpyDeviceToHost, c->copy_stream));
+    PI_CUDA(cudaEventRecord(c->ev_tris_copied, c->copy_stream));
+    f->tris_sent = true;
+  }
+  // 7. vertex positions by bisection
   f->nV = nv;
   f->mv.alloc(c, s, nv * 3 > 0 ? nv * 3 : 3);
   f->mk.alloc(c, s, nv * 2 > 0 ? nv * 2 : 2);
@@ -639,24 +666,6 @@ void stage_extract(pi_frame* f) {
     PI_LAUNCH(k_bisect, div_up(nv, 128), 128, 0, s, ba, nv, vorder.p, rep.p, slotA.p, slotB.p, f->nd_v.p,
               f->nd_id.p, f->mv.p, f->mk.p, f->dcount.p);
   }
-  // 7. triangles: first of each sorted vertex triple, in generation order
-  DBuf<int> otri, trank;
-  DBuf<unsigned> ttab;
-  DBuf<uint32_t> twhere;
-  otri.alloc(c, s, nt0 * 3 > 0 ? nt0 * 3 : 3);
-  PI_LAUNCH(k_tri_orient, div_up(nt0, 256), 256, 0, s, nt0, slot_vertex.p, tflip.p, otri.p);
-  const uint32_t tmask = table_mask(nt0);
-  ttab.alloc(c, s, (size_t)tmask + 1);
-  twhere.alloc(c, s, nt0 > 0 ? nt0 : 1);
-  trank.alloc(c, s, nt0 + 1);
-  PI_CUDA(cudaMemsetAsync(ttab.p, 0, sizeof(unsigned) * ((size_t)tmask + 1), s));
-  PI_LAUNCH(k_tri_insert, div_up(nt0, 256), 256, 0, s, nt0, otri.p, tmask, ttab.p, twhere.p);
-  PI_LAUNCH(k_first_flag, div_up(nt0 + 1, 256), 256, 0, s, nt0, ttab.p, twhere.p, trank.p);
-  exclusive_scan_i32(trank.p, trank.p, nt0 + 1, nullptr, tmp.p, s);
-  const long long nt = read_int(f, trank.p + nt0);
-  f->nT = nt;
-  f->mt.alloc(c, s, nt * 3 > 0 ? nt * 3 : 3);
-  PI_LAUNCH(k_tri_write, div_up(nt0, 256), 256, 0, s, nt0, trank.p, otri.p, f->mt.p);
   counters_snapshot(f, kPinExtract);
 }
 

@@ -72,6 +72,10 @@ struct pi_ctx {
   // no budget (its device buffers and events carry over); freed with the
   // context
   pi_frame* recon = nullptr;
+  // a second stream for device-to-host copies that overlap the compute
+  // stream (pi_reconstruct's triangle download), and its two events
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_tris_ready = nullptr, ev_tris_copied = nullptr;
 };
 
 struct pi_frame {
@@ -128,6 +132,12 @@ struct pi_frame {
   // stage timing: ev[2k], ev[2k+1] bracket stage slot k; the times are read
   // when the frame's next synchronisation point has passed
   cudaEvent_t ev[17] = {};
+  // pi_reconstruct's host triangle buffer: when set and large enough, the
+  // extraction copies the triangles there on the context's copy stream while
+  // the bisection runs (tris_sent then holds until the call ends)
+  int32_t* host_tris = nullptr;
+  long long host_tcap = 0;
+  bool tris_sent = false;
   int ev_pending = 0;   // bit k: slot k's events recorded, time not read yet
   int pin_pending = 0;  // bit k: pinned slot k written by this call, not folded yet
   float stage_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
