@@ -253,7 +253,10 @@ int pi_hashgrid_build_noalloc(const float* d_xyz, int64_t n, float radius, int32
  * in arrival order while their estimated device footprint fits in
  * budget_bytes (0 = no cap; one request is always admitted), runs admitted
  * frames concurrently and keeps results in host memory until fetched.  A
- * result equals pi_run's on the same input. */
+ * result equals pi_run's on the same input.  Without a budget each worker
+ * keeps its frame's device buffers from one request to the next (held until
+ * pi_server_destroy); with a budget a request's memory is returned when it
+ * completes. */
 typedef struct pi_server pi_server;
 int pi_server_create(int device, int slots, size_t budget_bytes, pi_server** out);
 /* copies xyz[n*3]; returns a ticket */

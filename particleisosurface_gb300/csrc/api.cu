@@ -279,6 +279,23 @@ static void run_stage(pi_frame* f, int target) {
   f->stage = target;
 }
 
+void check_params(const pi_params* p) {
+  if (!(std::isfinite(p->radius) && p->radius > 0)) throw std::invalid_argument("radius must be positive");
+  if (!(std::isfinite(p->smooth_factor) && p->smooth_factor > 0))
+    throw std::invalid_argument("smooth_factor must be positive");
+}
+
+// Back to `stage` (0: nothing uploaded, 1: particles uploaded) with every
+// result and counter cleared; device buffers are kept for reuse.
+void frame_clear(pi_frame* f, int stage) {
+  f->stage = stage;
+  f->nNodes = f->nV = f->nT = f->nDual = 0;
+  f->fieldEvals = f->pairs = f->bisectEvals = f->fp64Count = f->nLeaves = f->nEmpty = 0;
+  f->qefAccepted = f->qefSingular = 0;
+  f->ev_pending = f->pin_pending = 0;
+  for (int k = 0; k < 8; ++k) f->stage_ms[k] = 0;
+}
+
 }  // namespace pisurf
 
 using namespace pisurf;
@@ -458,22 +475,6 @@ int pi_ctx_tuning(const pi_ctx* c, int32_t* out2) {
   out2[0] = c->eval_forced ? c->eval_forced : c->eval_lanes[0];
   out2[1] = c->eval_forced ? c->eval_forced : c->eval_lanes[1];
   PI_API_END
-}
-
-static void check_params(const pi_params* p) {
-  PI_CHECK(std::isfinite(p->radius) && p->radius > 0, "radius must be positive");
-  PI_CHECK(std::isfinite(p->smooth_factor) && p->smooth_factor > 0, "smooth_factor must be positive");
-}
-
-// Back to `stage` (0: nothing uploaded, 1: particles uploaded) with every
-// result and counter cleared; device buffers are kept for reuse.
-static void frame_clear(pi_frame* f, int stage) {
-  f->stage = stage;
-  f->nNodes = f->nV = f->nT = f->nDual = 0;
-  f->fieldEvals = f->pairs = f->bisectEvals = f->fp64Count = f->nLeaves = f->nEmpty = 0;
-  f->qefAccepted = f->qefSingular = 0;
-  f->ev_pending = f->pin_pending = 0;
-  for (int k = 0; k < 8; ++k) f->stage_ms[k] = 0;
 }
 
 int pi_frame_create(pi_ctx* c, const pi_params* p, pi_frame** out) {

@@ -156,6 +156,11 @@ constexpr int kLevelEvent = 16;
 // Copies the frame's device counters into pinned slot `slot` (stream-ordered,
 // no synchronisation); the values reach the frame in resolve_pending.
 void counters_snapshot(pi_frame* f, int slot);
+// Parameter checks of pi_frame_create (throws std::invalid_argument).
+void check_params(const pi_params* p);
+// Back to `stage` (0: nothing uploaded, 1: particles uploaded) with every
+// result and counter cleared; device buffers are kept for reuse.
+void frame_clear(pi_frame* f, int stage);
 // Waits for the context stream once and folds every pending stage time and
 // counter snapshot into the frame.
 void resolve_pending(pi_frame* f);

@@ -73,6 +73,11 @@ namespace pisurf {
 static void worker_main(pi_server* s, int slot) {
   pi_ctx* ctx = nullptr;
   int rc0 = pi_ctx_create(s->device, 0, &ctx);
+  // without a server budget a worker keeps one frame for all its requests
+  // (device buffers and events carry over); with a budget each request's
+  // memory is returned when it completes, as admission assumes
+  pi_frame* kept = nullptr;
+  const bool reuse = s->budget == 0;
   for (;;) {
     std::shared_ptr<Request> r;
     {
@@ -96,7 +101,20 @@ static void worker_main(pi_server* s, int slot) {
     std::string err = rc0 ? std::string(pi_last_error()) : std::string();
     if (!rc) {
       pi_frame* f = nullptr;
-      rc = pi_frame_create(ctx, &r->P, &f);
+      if (reuse && kept) {
+        try {
+          check_params(&r->P);
+          kept->P = r->P;
+          frame_clear(kept, 0);
+          f = kept;
+        } catch (const std::exception& e) {
+          rc = PI_ERR_INVALID;
+          g_last_error = e.what();
+        }
+      } else {
+        rc = pi_frame_create(ctx, &r->P, &f);
+        if (!rc && reuse) kept = f;
+      }
       if (!rc) rc = pi_frame_upload(f, r->xyz.data(), r->n);
       if (!rc) rc = pi_run(f);
       int64_t nv = 0, nt = 0;
@@ -107,7 +125,7 @@ static void worker_main(pi_server* s, int slot) {
         rc = pi_mesh_get(f, r->verts.data(), r->tris.data(), nullptr);
       }
       if (rc) err = pi_last_error();
-      if (f) pi_frame_destroy(f);
+      if (f && f != kept) pi_frame_destroy(f);
     }
     r->xyz.clear();
     r->xyz.shrink_to_fit();
@@ -124,6 +142,7 @@ static void worker_main(pi_server* s, int slot) {
     s->cv_done.notify_all();
     s->cv_work.notify_all();
   }
+  if (kept) pi_frame_destroy(kept);
   if (ctx) pi_ctx_destroy(ctx);
   (void)slot;
 }
