@@ -57,17 +57,27 @@ __global__ void k_xmean(GridView g, const float4* __restrict__ pos, long long n,
       int s, e;
       if (!nb_row(g, cx, cy + dy, cz + dz, &s, &e)) continue;
       cand += e - s;
-      for (int j = s; j < e; ++j) {
-        if (j == t) continue;
-        float4 q = __ldg(pos + j);
-        const float dx = __fsub_rn(q.x, p.x), dy2 = __fsub_rn(q.y, p.y), dz2 = __fsub_rn(q.z, p.z);
-        float d2 = d2_exact(dx, dy2, dz2);
-        if (d2 >= nI2) continue;
-        float w = wij_f(__fsqrt_rn(d2), nI, inv_h3);
-        ws.add(w);
-        sx.add(dx * w);
-        sy.add(dy2 * w);
-        sz.add(dz2 * w);
+      // 32 candidates at a time: the distance test into a bit mask, then
+      // the weights of the set bits in candidate order
+      for (int j0 = s; j0 < e; j0 += 32) {
+        const int cnt = min(32, e - j0);
+        unsigned m = 0u;
+        for (int k = 0; k < cnt; ++k) {
+          const float4 q = __ldg(pos + j0 + k);
+          const float dx = __fsub_rn(q.x, p.x), dy2 = __fsub_rn(q.y, p.y), dz2 = __fsub_rn(q.z, p.z);
+          m |= (d2_exact(dx, dy2, dz2) < nI2 && j0 + k != t ? 1u : 0u) << k;
+        }
+        while (m) {
+          const int j = j0 + __ffs(m) - 1;
+          m &= m - 1u;
+          const float4 q = __ldg(pos + j);
+          const float dx = __fsub_rn(q.x, p.x), dy2 = __fsub_rn(q.y, p.y), dz2 = __fsub_rn(q.z, p.z);
+          const float w = wij_f(__fsqrt_rn(d2_exact(dx, dy2, dz2)), nI, inv_h3);
+          ws.add(w);
+          sx.add(dx * w);
+          sy.add(dy2 * w);
+          sz.add(dz2 * w);
+        }
       }
     }
   float4 hi = make_float4(p.x, p.y, p.z, 0.f), lo = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -165,23 +175,37 @@ __global__ void k_cov_G(GridView g, const float4* __restrict__ pos, const float4
     for (int dy = -1; dy <= 1; ++dy) {
       int s, e;
       if (!nb_row(g, cx, cy + dy, cz + dz, &s, &e)) continue;
-      for (int j = s; j < e; ++j) {
-        float4 q = __ldg(xm0 + j);
-        const float4 lq = __ldg(xlo + j);
-        // centre difference from the hi parts (exact for nearby centres) plus the lo parts
-        float dx = __fadd_rn(__fsub_rn(q.x, xp.x), __fsub_rn(lq.x, lp.x));
-        float dy2 = __fadd_rn(__fsub_rn(q.y, xp.y), __fsub_rn(lq.y, lp.y));
-        float dz2 = __fadd_rn(__fsub_rn(q.z, xp.z), __fsub_rn(lq.z, lp.z));
-        float d2 = d2_exact(dx, dy2, dz2);
-        if (d2 >= nI2) continue;
-        float w = wij_f(__fsqrt_rn(d2), nI, inv_h3);
-        ws.add(w);
-        c00.add(dx * dx * w);
-        c01.add(dx * dy2 * w);
-        c02.add(dx * dz2 * w);
-        c11.add(dy2 * dy2 * w);
-        c12.add(dy2 * dz2 * w);
-        c22.add(dz2 * dz2 * w);
+      // 32 candidates at a time: the distance test into a bit mask, then
+      // the weighted products of the set bits in candidate order
+      for (int j0 = s; j0 < e; j0 += 32) {
+        const int cnt = min(32, e - j0);
+        unsigned m = 0u;
+        for (int k = 0; k < cnt; ++k) {
+          const float4 q = __ldg(xm0 + j0 + k);
+          const float4 lq = __ldg(xlo + j0 + k);
+          // centre difference from the hi parts (exact for nearby centres) plus the lo parts
+          const float dx = __fadd_rn(__fsub_rn(q.x, xp.x), __fsub_rn(lq.x, lp.x));
+          const float dy2 = __fadd_rn(__fsub_rn(q.y, xp.y), __fsub_rn(lq.y, lp.y));
+          const float dz2 = __fadd_rn(__fsub_rn(q.z, xp.z), __fsub_rn(lq.z, lp.z));
+          m |= (d2_exact(dx, dy2, dz2) < nI2 ? 1u : 0u) << k;
+        }
+        while (m) {
+          const int j = j0 + __ffs(m) - 1;
+          m &= m - 1u;
+          const float4 q = __ldg(xm0 + j);
+          const float4 lq = __ldg(xlo + j);
+          const float dx = __fadd_rn(__fsub_rn(q.x, xp.x), __fsub_rn(lq.x, lp.x));
+          const float dy2 = __fadd_rn(__fsub_rn(q.y, xp.y), __fsub_rn(lq.y, lp.y));
+          const float dz2 = __fadd_rn(__fsub_rn(q.z, xp.z), __fsub_rn(lq.z, lp.z));
+          const float w = wij_f(__fsqrt_rn(d2_exact(dx, dy2, dz2)), nI, inv_h3);
+          ws.add(w);
+          c00.add(dx * dx * w);
+          c01.add(dx * dy2 * w);
+          c02.add(dx * dz2 * w);
+          c11.add(dy2 * dy2 * w);
+          c12.add(dy2 * dz2 * w);
+          c22.add(dz2 * dz2 * w);
+        }
       }
     }
   float iw = 1.0f / ws.s;

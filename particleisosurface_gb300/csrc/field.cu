@@ -23,20 +23,31 @@ __device__ __forceinline__ void grad_sum(const GridView& g, const PartView& P, f
     for (int dy = -1; dy <= 1; ++dy) {
       int s, e;
       if (!nb_row(g, cx, cy + dy, cz + dz, &s, &e)) continue;
-      for (int j = s; j < e; ++j) {
-        float4 x = __ldg(P.xm + j);
-        float dx = qx - x.x, dyy = qy - x.y, dzz = qz - x.z;
-        float e2 = fmaf(dx, dx, fmaf(dyy, dyy, dzz * dzz));
-        if (e2 < 0.25f * x.w) {  // |A d| < 1 needs |d| < R / 2
-          float4 a = __ldg(P.ga + j);
-          float4 b = __ldg(P.gb + j);
+      // 32 candidates at a time: the |d| < R / 2 test (|A d| < 1 needs it)
+      // into a bit mask, then the terms of the set bits in candidate order
+      for (int j0 = s; j0 < e; j0 += 32) {
+        const int cnt = min(32, e - j0);
+        unsigned m = 0u;
+        for (int k = 0; k < cnt; ++k) {
+          const float4 x = __ldg(P.xm + j0 + k);
+          const float dx = qx - x.x, dyy = qy - x.y, dzz = qz - x.z;
+          const float e2 = fmaf(dx, dx, fmaf(dyy, dyy, dzz * dzz));
+          m |= (e2 < 0.25f * x.w ? 1u : 0u) << k;
+        }
+        while (m) {
+          const int j = j0 + __ffs(m) - 1;
+          m &= m - 1u;
+          const float4 x = __ldg(P.xm + j);
+          const float dx = qx - x.x, dyy = qy - x.y, dzz = qz - x.z;
+          const float4 a = __ldg(P.ga + j);
+          const float4 b = __ldg(P.gb + j);
           const float4 lo = __ldg(P.xlo + j);
           float u0, u1, u2;
           amul(a, b, dx - lo.x, dyy - lo.y, dzz - lo.z, u0, u1, u2);
-          float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
+          const float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
           if (s2 < 1.0f) {
-            float om = 1.0f - s2;
-            float f = b.z * om * om;
+            const float om = 1.0f - s2;
+            const float f = b.z * om * om;
             ax.add(u0 * f);
             ay.add(u1 * f);
             az.add(u2 * f);
