@@ -13,7 +13,7 @@
 
 namespace pisurf {
 
-constexpr int kCandBuf = 64;  // staged candidate records per warp
+constexpr int kCandBuf = 96;  // staged candidate records per warp
 
 // Order-preserving map of a float onto a signed int (for warp min / max).
 __device__ __forceinline__ int fkey(float v) {
