@@ -293,23 +293,9 @@ __global__ void k_unique_write(const uint64_t* __restrict__ keys, const int* __r
   if (k != invalid && (i == 0 || keys[i - 1] != k)) out[scan[i]] = k;
 }
 
-// Leaf containing octant `oct` (bit set = + side) of lattice point (x, y, z),
-// descending from `node` (which contains the octant's point).
-__device__ __forceinline__ int locate(int x, int y, int z, int oct, const int* __restrict__ nd_child,
-                                      const int4* __restrict__ nd_org, int node) {
-  for (int guard = 0; guard < 64; ++guard) {
-    int ch = nd_child[node];
-    if (ch < 0) return node;
-    int4 o = nd_org[node];
-    int mid = o.w >> 1;
-    int bx = (x > o.x + mid || (x == o.x + mid && (oct & 1))) ? 1 : 0;
-    int by = (y > o.y + mid || (y == o.y + mid && (oct & 2))) ? 1 : 0;
-    int bz = (z > o.z + mid || (z == o.z + mid && (oct & 4))) ? 1 : 0;
-    node = ch + (bx | (by << 1) | (bz << 2));
-  }
-  return node;
-}
-
+// One thread per dual vertex (a unique interior leaf corner): the eight leaves
+// around it by descent from the root, the octant of each point deciding the
+// side of a mid-plane that holds it, then the DMC case.
 __global__ void k_dual(const uint64_t* __restrict__ verts, long long nu, int B, const int* __restrict__ nd_child,
                        const int4* __restrict__ nd_org, const float4* __restrict__ nd_v, int* __restrict__ cells,
                        int* __restrict__ procs, int* __restrict__ tcount, unsigned long long* __restrict__ ndual) {
@@ -333,12 +319,33 @@ __global__ void k_dual(const uint64_t* __restrict__ verts, long long nu, int B, 
     if (x == o.x + mid || y == o.y + mid || z == o.z + mid) break;
     start = ch + ((x > o.x + mid) ? 1 : 0) + ((y > o.y + mid) ? 2 : 0) + ((z > o.z + mid) ? 4 : 0);
   }
+  // the eight descents below `start` advance in lockstep, so that their
+  // loads are in flight together rather than one chain after another
   int n8[8];
-  int index = 0;
-  for (int c = 0; c < 8; ++c) {
-    n8[c] = locate(x, y, z, c, nd_child, nd_org, start);
-    if (nd_v[n8[c]].w > 0.f) index |= 1 << c;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) n8[c] = start;
+  for (int guard = 0; guard < 64; ++guard) {
+    int ch[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) ch[c] = nd_child[n8[c]];
+    bool more = false;
+#pragma unroll
+    for (int c = 0; c < 8; ++c)
+      if (ch[c] >= 0) {
+        const int4 o = nd_org[n8[c]];
+        const int mid = o.w >> 1;
+        const int bx = (x > o.x + mid || (x == o.x + mid && (c & 1))) ? 1 : 0;
+        const int by = (y > o.y + mid || (y == o.y + mid && (c & 2))) ? 1 : 0;
+        const int bz = (z > o.z + mid || (z == o.z + mid && (c & 4))) ? 1 : 0;
+        n8[c] = ch[c] + (bx | (by << 1) | (bz << 2));
+        more = true;
+      }
+    if (!more) break;
   }
+  int index = 0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c)
+    if (nd_v[n8[c]].w > 0.f) index |= 1 << c;
   const int code = c_code[index];
   int nt = 0;
   if (code != 0 && code != 255) {
