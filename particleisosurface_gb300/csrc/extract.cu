@@ -99,47 +99,76 @@ __global__ void k_corner_keys(const int* __restrict__ leaves, long long nl, cons
   vals[t] = (uint32_t)t;
 }
 
-// Morton code of three coordinates of up to 10 bits each.
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {
-  v &= 0x3ffu;
-  v = (v | (v << 16)) & 0x030000ffu;
-  v = (v | (v << 8)) & 0x0300f00fu;
-  v = (v | (v << 4)) & 0x030c30c3u;
-  v = (v | (v << 2)) & 0x09249249u;
+// Morton code of three coordinates of up to 21 bits each (bit interleaving
+// by the usual shift-and-mask steps), and its inverse.
+__device__ __forceinline__ uint64_t spread3(uint64_t v) {
+  v &= 0x1fffffull;
+  v = (v | (v << 32)) & 0x1f00000000ffffull;
+  v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+  v = (v | (v << 8)) & 0x100f00f00f00f00full;
+  v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+  v = (v | (v << 2)) & 0x1249249249249249ull;
   return v;
 }
-__device__ __forceinline__ uint32_t compact3(uint32_t v) {
-  v &= 0x09249249u;
-  v = (v | (v >> 2)) & 0x030c30c3u;
-  v = (v | (v >> 4)) & 0x0300f00fu;
-  v = (v | (v >> 8)) & 0x030000ffu;
-  v = (v | (v >> 16)) & 0x3ffu;
+__device__ __forceinline__ uint64_t compact3(uint64_t v) {
+  v &= 0x1249249249249249ull;
+  v = (v ^ (v >> 2)) & 0x10c30c30c30c30c3ull;
+  v = (v ^ (v >> 4)) & 0x100f00f00f00f00full;
+  v = (v ^ (v >> 8)) & 0x1f0000ff0000ffull;
+  v = (v ^ (v >> 16)) & 0x1f00000000ffffull;
+  v = (v ^ (v >> 32)) & 0x1fffffull;
   return v;
 }
 
 // Interior leaf corners (coordinates 1 .. 2^D_max - 1) as bits of a lattice
-// bitmap indexed by the Morton code of (x - 1, y - 1, z - 1): 2^(3 D_max)
-// bits, 16 MB at D_max = 9.  The set bits in index order are the unique
-// corners in Z order, which keeps the later per-vertex work spatially
-// coherent (as the reference's recursive traversal is).
+// bitmap indexed by the Morton code of (x - 1, y - 1, z - 1).  The Morton
+// range is cut into blocks of 2^bb codes (a 2^(bb/3)-cube of lattice
+// points).  Up to D_max = 10 (2^30 bits) every block is stored (slot = block,
+// slot and blist null); above it only the blocks that hold a corner, with
+// consecutive slots in block order, so that work and memory follow the
+// surface rather than the volume of the lattice.  Either way the set bits in
+// slot order are the unique corners in Z order, which keeps the later
+// per-vertex work spatially coherent (as the reference's recursive
+// traversal is).
+__device__ __forceinline__ bool corner_code(const int* __restrict__ leaves, const int4* __restrict__ nd_org,
+                                            int full, long long t, uint64_t* idx) {
+  const int4 o = nd_org[leaves[t >> 3]];
+  const int k = (int)(t & 7);
+  const int x = o.x + ((k & 1) ? o.w : 0), y = o.y + ((k & 2) ? o.w : 0), z = o.z + ((k & 4) ? o.w : 0);
+  if (!(x > 0 && x < full && y > 0 && y < full && z > 0 && z < full)) return false;
+  *idx = spread3((uint64_t)(x - 1)) | (spread3((uint64_t)(y - 1)) << 1) | (spread3((uint64_t)(z - 1)) << 2);
+  return true;
+}
+
+// used[block] = 1 for every block that holds a corner.
+__global__ void k_block_mark(const int* __restrict__ leaves, long long nl, const int4* __restrict__ nd_org, int full,
+                             int bb, int* __restrict__ used) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  uint64_t idx;
+  if (t < nl * 8 && corner_code(leaves, nd_org, full, t, &idx)) used[idx >> bb] = 1;
+}
+
+// slot -> block (the inverse of the scan of used)
+__global__ void k_block_list(long long nb, const int* __restrict__ used, const int* __restrict__ slot,
+                             long long* __restrict__ blist) {
+  const long long b = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < nb && used[b]) blist[slot[b]] = b;
+}
+
 __global__ void k_corner_mark(const int* __restrict__ leaves, long long nl, const int4* __restrict__ nd_org,
-                              int full, unsigned* __restrict__ bits) {
-  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+                              int full, int bb, const int* __restrict__ slot, unsigned* __restrict__ bits) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   // one lane per corner; corners of sibling leaves fall in a few bitmap words,
   // so the warp ORs its bits per word and issues one atomic per word
   long long word = -1;
   unsigned bit = 0u;
-  if (t < nl * 8) {
-    const int4 o = nd_org[leaves[t >> 3]];
-    const int k = (int)(t & 7);
-    const int x = o.x + ((k & 1) ? o.w : 0), y = o.y + ((k & 2) ? o.w : 0), z = o.z + ((k & 4) ? o.w : 0);
-    if (x > 0 && x < full && y > 0 && y < full && z > 0 && z < full) {
-      const uint32_t idx = spread3((uint32_t)(x - 1)) | (spread3((uint32_t)(y - 1)) << 1) |
-                           (spread3((uint32_t)(z - 1)) << 2);
-      word = idx >> 5;
-      bit = 1u << (idx & 31);
-    }
+  uint64_t idx;
+  if (t < nl * 8 && corner_code(leaves, nd_org, full, t, &idx)) {
+    const uint64_t in_block = idx & ((1ull << bb) - 1ull);
+    const long long blk = slot ? (long long)slot[idx >> bb] : (long long)(idx >> bb);
+    word = (blk << (bb - 5)) + (long long)(in_block >> 5);
+    bit = 1u << (unsigned)(in_block & 31ull);
   }
   unsigned todo = __ballot_sync(0xffffffffu, word >= 0);
   while (todo) {
@@ -158,16 +187,18 @@ __global__ void k_bitmap_count(const unsigned* __restrict__ bits, long long nw, 
   if (w == nw) cnt[w] = 0;
 }
 
-__global__ void k_bitmap_keys(const unsigned* __restrict__ bits, long long nw, const int* __restrict__ off, int B,
-                              uint64_t* __restrict__ out) {
+__global__ void k_bitmap_keys(const unsigned* __restrict__ bits, long long nw, const int* __restrict__ off, int bb,
+                              const long long* __restrict__ blist, int B, uint64_t* __restrict__ out) {
   long long w = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= nw) return;
   unsigned b = bits[w];
   int o = off[w];
+  const long long sl = w >> (bb - 5);
+  const uint64_t base = ((uint64_t)(blist ? blist[sl] : sl) << bb) | ((uint64_t)(w & ((1LL << (bb - 5)) - 1)) << 5);
   while (b) {
     const int i = __ffs(b) - 1;
     b &= b - 1;
-    const uint32_t idx = ((uint32_t)w << 5) | (uint32_t)i;
+    const uint64_t idx = base | (uint64_t)i;
     const uint64_t x = compact3(idx) + 1, y = compact3(idx >> 1) + 1, z = compact3(idx >> 2) + 1;
     out[o++] = (x << (2 * B)) | (y << B) | z;
   }
@@ -499,6 +530,7 @@ __global__ void k_tri_orient(long long nt, const int* __restrict__ slot_vertex, 
   otri[3 * t + 2] = tflip[t] ? c : a;
 }
 
+// Mask of the smallest power-of-two table with more than n entries.
 static uint32_t table_mask(long long n) {
   uint32_t m = 1;
   while ((long long)m < n + 1) m <<= 1;
@@ -533,20 +565,44 @@ void stage_extract(pi_frame* f) {
   const long long nk = nl * 8;
   DBuf<uint64_t> uverts;
   long long nu = 0;
-  if (f->dmax <= 10) {
-    const long long nw = div_up(1LL << (3 * f->dmax), 32);
+  // block size: 2^bb Morton codes, bb a multiple of 3 and at least 15 (32^3
+  // points, 1024 words), so that at most 2^24 blocks cover the lattice; past
+  // 2^18 codes a block (D_max > 14) the blocks grow too large and the corners
+  // are sorted instead (below)
+  const int bb = std::max(15, ((3 * f->dmax - 24 + 2) / 3) * 3);
+  if (bb <= 18) {
+    const long long nb = 1LL << std::max(0, 3 * f->dmax - bb);
+    // the whole bitmap costs less than finding the used blocks up to 2^30 bits
+    const bool dense = f->dmax <= 10;
+    long long nused = nb;
+    DBuf<int> used, slot;
+    DBuf<long long> blist;
+    if (!dense) {
+      used.alloc(c, s, nb + 1);
+      if (tmp.n < scan_tmp_ints(nb + 1)) tmp.alloc(c, s, scan_tmp_ints(nb + 1));
+      PI_CUDA(cudaMemsetAsync(used.p, 0, sizeof(int) * (nb + 1), s));
+      PI_LAUNCH(k_block_mark, div_up(nk, 256), 256, 0, s, leaves.p, nl, f->nd_org.p, full, bb, used.p);
+      slot.alloc(c, s, nb + 1);
+      exclusive_scan_i32(used.p, slot.p, nb + 1, nullptr, tmp.p, s);
+      nused = read_int(f, slot.p + nb);
+      blist.alloc(c, s, nused > 0 ? nused : 1);
+      PI_LAUNCH(k_block_list, div_up(nb, 256), 256, 0, s, nb, used.p, slot.p, blist.p);
+    }
+    const long long nw = nused << (bb - 5);
     DBuf<unsigned> bits;
     DBuf<int> cnt;
-    bits.alloc(c, s, nw);
+    bits.alloc(c, s, nw > 0 ? nw : 1);
     cnt.alloc(c, s, nw + 1);
     if (tmp.n < scan_tmp_ints(nw + 1)) tmp.alloc(c, s, scan_tmp_ints(nw + 1));
-    PI_CUDA(cudaMemsetAsync(bits.p, 0, sizeof(unsigned) * nw, s));
-    PI_LAUNCH(k_corner_mark, div_up(nk, 256), 256, 0, s, leaves.p, nl, f->nd_org.p, full, bits.p);
+    PI_CUDA(cudaMemsetAsync(bits.p, 0, sizeof(unsigned) * (nw > 0 ? nw : 1), s));
+    PI_LAUNCH(k_corner_mark, div_up(nk, 256), 256, 0, s, leaves.p, nl, f->nd_org.p, full, bb,
+              dense ? nullptr : slot.p, bits.p);
     PI_LAUNCH(k_bitmap_count, div_up(nw + 1, 256), 256, 0, s, bits.p, nw, cnt.p);
     exclusive_scan_i32(cnt.p, cnt.p, nw + 1, nullptr, tmp.p, s);
     nu = read_int(f, cnt.p + nw);
     uverts.alloc(c, s, nu > 0 ? nu : 1);
-    PI_LAUNCH(k_bitmap_keys, div_up(nw, 256), 256, 0, s, bits.p, nw, cnt.p, B, uverts.p);
+    PI_LAUNCH(k_bitmap_keys, div_up(nw, 256), 256, 0, s, bits.p, nw, cnt.p, bb, dense ? nullptr : blist.p, B,
+              uverts.p);
   } else {
     const uint64_t invalid = (1ull << (3 * B)) - 1ull;
     DBuf<uint64_t> keys, keys2;
@@ -629,7 +685,10 @@ void stage_extract(pi_frame* f) {
   DBuf<uint32_t> twhere;
   otri.alloc(c, s, nt0 * 3 > 0 ? nt0 * 3 : 3);
   PI_LAUNCH(k_tri_orient, div_up(nt0, 256), 256, 0, s, nt0, slot_vertex.p, tflip.p, otri.p);
-  const uint32_t tmask = table_mask(nt0);
+  // nearly every triangle is distinct, so the table gets twice as many
+  // entries as triangles (load at most 1/2; linear probing degrades fast
+  // above that)
+  const uint32_t tmask = table_mask(2 * nt0);
   ttab.alloc(c, s, (size_t)tmask + 1);
   twhere.alloc(c, s, nt0 > 0 ? nt0 : 1);
   trank.alloc(c, s, nt0 + 1);

@@ -14,12 +14,25 @@ from particleisosurface_gb300 import build as B
 
 pytestmark = pytest.mark.gpu
 
+def _two_balls(gap):
+    """Two jittered lattice balls (radius 0.1, spacing 0.02) `gap` apart: a
+    root box of about gap / r leaf cells per axis, hence a deep octree."""
+    rng = np.random.default_rng(5)
+    g = np.arange(-0.1, 0.1001, 0.02)
+    p = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    p = p[(p ** 2).sum(1) <= 0.1 ** 2]
+    p = p + rng.uniform(-0.004, 0.004, p.shape)
+    return np.concatenate([p, p + np.array([gap, 0.3 * gap, 0.1])]).astype(np.float32)
+
+
 CASES = {
     "one": lambda: np.zeros((1, 3), np.float32) + 0.3,
     "coincident": lambda: np.zeros((10, 3), np.float32) + 0.3,
     "line": lambda: np.stack([np.linspace(0, 0.2, 11), np.zeros(11), np.zeros(11)], -1).astype(np.float32),
     "sheet": lambda: np.stack(np.meshgrid(np.arange(12) * 0.02, np.arange(12) * 0.02, [0.1], indexing="ij"),
                               -1).reshape(-1, 3).astype(np.float32),
+    # D_max 11: the dual-vertex lattice is stored by occupied blocks
+    "far_d11": lambda: _two_balls(15.0),
 }
 
 
@@ -41,6 +54,8 @@ def test_degenerate_frame_matches_oracle(ctx, name):
     info = g.info()
     d = o.depths()
     assert (info["depth_max"], info["depth_min"]) == (d["depth_max"], d["depth_min"])
+    if name.startswith("far_d"):
+        assert info["depth_max"] == int(name[len("far_d"):]), info["depth_max"]
     rep = PR.compare_octrees(o.nodes(), g.dump(N.DUMP_NODES), o, o.scalars()["max_scalar"], d["depth_min"])
     print(name, {k: v for k, v in rep.items() if k not in ("leaf_far_pos", "leaf_far_gpu", "unexplained")},
           rep["unexplained"][:4])
@@ -50,6 +65,30 @@ def test_degenerate_frame_matches_oracle(ctx, name):
     mo = PR.canonical_mesh(vo, to, ko, one_based=True)
     mg = PR.canonical_mesh(vg, tg, kg, one_based=False)
     assert set(mo[0]) == set(mg[0]) and mo[1] == mg[1]
+    g.close()
+
+
+def test_depth_15_frame_close_to_oracle(ctx):
+    """D_max 15: past D_max 14 the dual vertices come from sorted corner keys.
+    The balls sit some 10^4 r from the origin, where a float coordinate
+    resolves only about 1e-3 r, so the library (compensated sums, hi/lo
+    centres) and the float oracle may disagree on samples near the
+    isovalue: the octree sizes and meshes must agree to a small fraction,
+    not node for node."""
+    xyz = _two_balls(250.0)
+    r = 0.01
+    o = O.OracleFrame(xyz, r).run()
+    g = N.Frame(ctx, N.default_params(r)).upload(xyz).run()
+    info = g.info()
+    assert info["depth_max"] == o.depths()["depth_max"] == 15
+    n_o, n_g = len(o.nodes()["id"]), info["num_nodes"]
+    assert abs(n_o - n_g) <= max(16, n_o // 50), (n_o, n_g)
+    rep = PR.compare_meshes(o.mesh(), g.mesh(keys=True), r)
+    print(rep)
+    n_v = rep["verts_oracle"]
+    assert n_v > 1000
+    assert rep["verts_only_oracle"] + rep["verts_only_gpu"] <= n_v // 20
+    assert rep["tris_only_oracle"] + rep["tris_only_gpu"] <= rep["tris_oracle"] // 20
     g.close()
 
 
