@@ -379,6 +379,7 @@ int pi_ctx_create(int device, size_t budget_bytes, pi_ctx** out) {
   PI_CUDA(cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, device));
   PI_CUDA(cudaMallocHost(&c->hpin, sizeof(unsigned long long) * (size_t)kPinWords));
   PI_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  c->coop_blocks = top_levels_grid(device, c->smCount);
   PI_CUDA(cudaEventCreateWithFlags(&c->ev_tris_ready, cudaEventDisableTiming));
   PI_CUDA(cudaEventCreateWithFlags(&c->ev_tris_copied, cudaEventDisableTiming));
   cudaMemPool_t pool;

@@ -72,6 +72,9 @@ struct pi_ctx {
   // no budget (its device buffers and events carry over); freed with the
   // context
   pi_frame* recon = nullptr;
+  // grid of the cooperative coarse-level octree kernel (0: no cooperative
+  // launch on this device)
+  int coop_blocks = 0;
   // a second stream for device-to-host copies that overlap the compute
   // stream (pi_reconstruct's triangle download), and its two events
   cudaStream_t copy_stream = nullptr;
@@ -149,8 +152,10 @@ namespace pisurf {
 constexpr int kPinAniso = 0, kPinOctree = 1, kPinExtract = 2, kPinSlots = 3;
 constexpr int kPinValid = kPinSlots;  // bit of pin_pending for the valid-key count
 // after the slots: word 0 the valid-key count, word 1 the octree level's
-// INTERNAL count
-constexpr int kPinWords = kPinSlots * kCounterWords + 8;
+// INTERNAL count; then the coarse-level kernel's level starts and depth
+constexpr int kPinTopOffset = kPinSlots * kCounterWords + 8;
+constexpr int kPinTopWords = 32;
+constexpr int kPinWords = kPinTopOffset + kPinTopWords;
 // event that marks the INTERNAL count's copy in the octree level loop
 constexpr int kLevelEvent = 16;
 // Copies the frame's device counters into pinned slot `slot` (stream-ordered,
@@ -172,6 +177,9 @@ void stage_aniso(pi_frame* f);
 void stage_normals(pi_frame* f);
 void stage_octree(pi_frame* f);
 void stage_extract(pi_frame* f);
+// Grid (blocks) of the cooperative coarse-level octree kernel on `device`,
+// 0 where cooperative launches are not available.
+int top_levels_grid(int device, int sm_count);
 void qef_level(pi_frame* f, long long lb, long long le, int depth);
 // UniformGrid: lattice of the loadRootBox box; sampling into d_out (device,
 // x fastest) when cap holds it; returns the number of lattice points.

@@ -32,6 +32,8 @@
 #include <algorithm>
 #include <cmath>
 
+#include <cooperative_groups.h>
+
 #include "chunk.cuh"
 #include "device.cuh"
 #include "internal.h"
@@ -669,6 +671,173 @@ __global__ void __launch_bounds__(32 * kSpawnWarps) k_spawn_scan(LevelArgs a, lo
   }
 }
 
+// The coarse levels (depth < D_min - 1) in one cooperative launch: their
+// nodes are INTERNAL exactly when their grown box holds a particle, so a
+// level is an emptiness test per node, a scan of the INTERNAL flags and the
+// spawn of 8 children per INTERNAL node, the same steps (and results) as
+// k_empty, k_internal_flag, the scan and k_spawn, with grid-wide barriers
+// in place of launches and of the host's read of each level's size.  The
+// levels are small (at most kTopLevelNodes nodes; the loop stops before a
+// larger one), so block 0 scans the flags alone.  Node data written in the
+// launch is read through the L2 (ld.global.cg), never the read-only path.
+constexpr int kTopLevelNodes = 4096;
+constexpr int kTopThreads = 256;
+
+struct TopArgs {
+  LevelArgs la;  // grid, particles, expand, iso (lb / le / big set per level)
+  int dstop;     // levels 0 .. dstop - 1 at most
+  long long* lv;     // level starts: level d is [lv[d], lv[d + 1])
+  int* flag;         // kTopLevelNodes + 1
+  int* depth_out;    // levels done
+  float4* nd_c;
+  float4* nd_v;
+  uint64_t* nd_id;
+  int* nd_parent;
+  int* nd_child;
+  int8_t* nd_type;
+  int8_t* nd_depth;
+  int8_t* nd_sc;
+  float* nd_curv;
+  int4* nd_org;
+};
+
+__global__ void __launch_bounds__(kTopThreads) k_top_levels(TopArgs t) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  __shared__ int s_warp[kTopThreads / 32];
+  __shared__ int s_carry;
+  const int lane = threadIdx.x & 31;
+  const long long gwarp = ((long long)blockIdx.x * kTopThreads + threadIdx.x) >> 5;
+  const long long nwarps = (long long)gridDim.x * kTopThreads / 32;
+  const long long gthread = (long long)blockIdx.x * kTopThreads + threadIdx.x;
+  const long long nthreads = (long long)gridDim.x * kTopThreads;
+  int depth = 0;
+  for (;;) {
+    const long long lb = __ldcg(t.lv + depth), le = __ldcg(t.lv + depth + 1);
+    const long long n = le - lb;
+    LevelArgs a = t.la;
+    // emptiness: one warp per node (k_empty's test), INTERNAL if non-empty
+    for (long long w = gwarp; w < n; w += nwarps) {
+      const long long node = lb + w;
+      const GrownBox b = grown_box(a.g, __ldcg(t.nd_c + node), a.expand);
+      bool found = false;
+      if (b.x0 <= b.x1 && b.y0 <= b.y1 && b.z0 <= b.z1) {
+        const int nyb = b.y1 - b.y0 + 1;
+        const int rows = (b.z1 - b.z0 + 1) * nyb;
+        for (int r0 = 0; r0 < rows && !found; r0 += 32) {
+          const int r = r0 + lane;
+          bool hit = false;
+          if (r < rows) {
+            const int z = b.z0 + r / nyb, y = b.y0 + r % nyb;
+            const long long base = ((long long)z * a.g.ny + y) * a.g.nx;
+            const int s = __ldg(a.g.off + base + b.x0), e = __ldg(a.g.off + base + b.x1 + 1);
+            for (int j = s; j < e; ++j)
+              if (inside(b, __ldg(a.pos + j))) {
+                hit = true;
+                break;
+              }
+          }
+          found = __any_sync(0xffffffffu, hit);
+        }
+      }
+      if (lane == 0) {
+        if (!found) {
+          t.nd_type[node] = T_EMPTY;
+          t.nd_curv[node] = 1.0f;  // area == 0
+          float4 v = __ldcg(t.nd_v + node);
+          v.w = a.iso;
+          t.nd_v[node] = v;
+        } else {
+          t.nd_type[node] = T_INTERNAL;
+          t.nd_curv[node] = -1.0f;
+        }
+        t.flag[w] = found ? 1 : 0;
+      }
+    }
+    grid.sync();
+    // exclusive scan of the flags by block 0; the next level's end
+    if (blockIdx.x == 0) {
+      if (threadIdx.x == 0) s_carry = 0;
+      __syncthreads();
+      for (long long b0 = 0; b0 < n; b0 += kTopThreads) {
+        const long long i = b0 + threadIdx.x;
+        const int v = i < n ? __ldcg(t.flag + i) : 0;
+        int inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int u = __shfl_up_sync(0xffffffffu, inc, o);
+          if (lane >= o) inc += u;
+        }
+        if (lane == 31) s_warp[threadIdx.x >> 5] = inc;
+        __syncthreads();
+        int wbase = 0, total = 0;
+        for (int k = 0; k < kTopThreads / 32; ++k) {
+          if (k < (int)(threadIdx.x >> 5)) wbase += s_warp[k];
+          total += s_warp[k];
+        }
+        if (i < n) t.flag[i] = s_carry + wbase + inc - v;
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += total;
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) t.lv[depth + 2] = le + 8LL * s_carry;
+    }
+    grid.sync();
+    // spawn (k_spawn): children of the INTERNAL nodes from the level's end on
+    for (long long w = gthread; w < n; w += nthreads) {
+      const long long i = lb + w;
+      if (__ldcg(t.nd_type + i) != T_INTERNAL) {
+        t.nd_child[i] = -1;
+        continue;
+      }
+      const long long b = le + 8LL * __ldcg(t.flag + w);
+      t.nd_child[i] = (int)b;
+      const float4 pc = __ldcg(t.nd_c + i);
+      const float hc = pc.w / 2;
+      const uint64_t pid = __ldcg(reinterpret_cast<const unsigned long long*>(t.nd_id) + i);
+      const int4 po = __ldcg(t.nd_org + i);
+      const int hs = po.w >> 1;
+      for (int k = 0; k < 8; ++k) {
+        const float sx = (k & 1) ? hc : -hc, sy = (k & 2) ? hc : -hc, sz = (k & 4) ? hc : -hc;
+        const float4 cc = make_float4(__fadd_rn(pc.x, sx), __fadd_rn(pc.y, sy), __fadd_rn(pc.z, sz), hc);
+        t.nd_c[b + k] = cc;
+        t.nd_v[b + k] = make_float4(cc.x, cc.y, cc.z, 0.f);
+        t.nd_id[b + k] = pid * 8ull + (uint64_t)k;
+        t.nd_parent[b + k] = (int)i;
+        t.nd_child[b + k] = -1;
+        t.nd_type[b + k] = T_UNCERTAIN;
+        t.nd_depth[b + k] = (int8_t)(depth + 1);
+        t.nd_sc[b + k] = 0;
+        t.nd_curv[b + k] = 0.f;
+        t.nd_org[b + k] =
+            make_int4(po.x + ((k & 1) ? hs : 0), po.y + ((k & 2) ? hs : 0), po.z + ((k & 4) ? hs : 0), hs);
+      }
+    }
+    const long long next = __ldcg(t.lv + depth + 2) - le;  // written before the last barrier
+    ++depth;
+    if (next == 0 || depth >= t.dstop || next > kTopLevelNodes) break;  // the same for every thread
+    grid.sync();
+  }
+  if (gthread == 0) *t.depth_out = depth;
+}
+
+int top_levels_grid(int device, int sm_count) {
+  int coop = 0;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device) != cudaSuccess || !coop) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_top_levels, kTopThreads, 0) != cudaSuccess ||
+      per_sm < 1) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  // the coarse levels hold at most a few thousand nodes: half the SMs, one
+  // block each, leave room for other contexts' kernels
+  return std::max(1, std::min(per_sm * sm_count, sm_count / 2));
+}
+
 __global__ void k_root(float cx, float cy, float cz, float h, int size, float4* nd_c, float4* nd_v,
                        uint64_t* nd_id, int* nd_parent, int* nd_child, int8_t* nd_type, int8_t* nd_depth,
                        int8_t* nd_sc, float* nd_curv, int4* nd_org) {
@@ -803,7 +972,49 @@ void stage_octree(pi_frame* f) {
   ucum.alloc(ctx, s, ek + 1);  // exclusive scan of ucnt (sparse levels)
   long long lb = 0, le = 1;
   bool known = false;  // emptiness and curvature of this level settled by the parents' scan
-  for (int depth = 0;; ++depth) {
+  int depth0 = 0;
+  if (f->dmin >= 2 && ctx->coop_blocks > 0) {
+    // the coarse levels 0 .. D_min - 2 in one cooperative launch
+    const int dstop = f->dmin - 1;
+    DBuf<long long> lvd;
+    DBuf<int> tflag, dout;
+    lvd.alloc(ctx, s, dstop + 3);
+    tflag.alloc(ctx, s, kTopLevelNodes + 1);
+    dout.alloc(ctx, s, 1);
+    long long* const lvh = reinterpret_cast<long long*>(ctx->hpin + kPinTopOffset);
+    lvh[0] = 0;
+    lvh[1] = 1;
+    PI_CUDA(cudaMemcpyAsync(lvd.p, lvh, 2 * sizeof(long long), cudaMemcpyHostToDevice, s));
+    TopArgs ta{LevelArgs{g, f->pos.p, f->nrm.p, f->P.radius * f->P.smooth_factor, f->iso, f->P.radius, 0, 0, 1, P},
+               dstop,
+               lvd.p,
+               tflag.p,
+               dout.p,
+               f->nd_c.p,
+               f->nd_v.p,
+               f->nd_id.p,
+               f->nd_parent.p,
+               f->nd_child.p,
+               f->nd_type.p,
+               f->nd_depth.p,
+               f->nd_sc.p,
+               f->nd_curv.p,
+               f->nd_org.p};
+    void* args[] = {&ta};
+    PI_CUDA(cudaLaunchCooperativeKernel((const void*)k_top_levels, dim3(ctx->coop_blocks), dim3(kTopThreads), args,
+                                        0, s));
+    ++g_launches;
+    int* const dh = reinterpret_cast<int*>(lvh + kPinTopWords - 1);
+    PI_CUDA(cudaMemcpyAsync(lvh, lvd.p, sizeof(long long) * (dstop + 2), cudaMemcpyDeviceToHost, s));
+    PI_CUDA(cudaMemcpyAsync(dh, dout.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PI_CUDA(cudaStreamSynchronize(s));
+    depth0 = *dh;
+    for (int d = 0; d < depth0; ++d) f->levelBegin.push_back(lvh[d]);
+    lb = lvh[depth0];
+    le = lvh[depth0 + 1];
+    f->nNodes = le;
+  }
+  for (int depth = depth0; le > lb; ++depth) {
     f->levelBegin.push_back(lb);
     const long long nl = le - lb;
     LevelArgs la{g, f->pos.p, f->nrm.p, f->P.radius * f->P.smooth_factor, f->iso, f->P.radius, lb, le,
