@@ -44,7 +44,7 @@ enum : int8_t { T_EMPTY = 0, T_INTERNAL = 1, T_LEAF = 2, T_UNCERTAIN = 3 };
 
 constexpr int kQ = 28;  // 27 samples + the centre per node
 constexpr int kEvalWarps = 8;   // warps per block of k_q_eval
-constexpr int kSpawnWarps = 8;  // warps per block of k_spawn_scan
+constexpr int kSpawnWarps = 2;  // warps per block of k_spawn_scan (small blocks: a warp that scans a whole block does not hold up seven others)
 
 struct LevelArgs {
   GridView g;
@@ -1022,7 +1022,7 @@ void stage_octree(pi_frame* f) {
     // every node of the level has half size rootH / 2^depth (children halve exactly)
     const float cell_d = 2.0f * std::ldexp(f->rootH, -depth);
     const bool leaf_level = (double)(cell_d - f->P.radius) < 1e-8;
-    const int wpb = 8;  // warps per block
+    const int wpb = 2;  // warps per block of the warp-per-node kernels (small blocks: uneven warps free their SM slots sooner)
     if (!known)
       PI_LAUNCH(k_empty, div_up(nl, wpb), 32 * wpb, 0, s, la, f->nd_c.p, f->nd_v.p, f->nd_type.p, f->nd_curv.p);
     if (depth >= f->dmin && leaf_level && !f->P.qef) {
