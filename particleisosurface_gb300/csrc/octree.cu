@@ -234,10 +234,17 @@ __global__ void k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c
   const int k = i < n ? qkey[i] : -1;
   bool uniq = false;
   int place = 0;
+  // the node's records load beside the key (the node index is valid for
+  // every i < n)
+  float4 nc = make_float4(0.f, 0.f, 0.f, 0.f), nv = nc;
+  if (i < n) {
+    const long long node = a.lb + i / kQ;
+    nc = nd_c[node];
+    nv = nd_v[node];
+  }
   if (k >= 0) {
     float qx, qy, qz;
-    const long long node = a.lb + i / kQ;
-    sample_point(nd_c[node], nd_v[node], (int)(i % kQ), qx, qy, qz);
+    sample_point(nc, nv, (int)(i % kQ), qx, qy, qz);
     const long long base = 2LL * qoff[k];
     const uint32_t m = 2u * (uint32_t)(qoff[k + 1] - qoff[k]);
     uint32_t pos = __umulhi(hash3(qx, qy, qz), m);
@@ -429,16 +436,20 @@ __global__ void k_classify(LevelArgs a, const float* __restrict__ qval, const in
   const long long node = a.lb + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (node >= a.le) return;
-  if (nd_type[node] != T_UNCERTAIN) return;  // warp-uniform
+  // the node's type and its samples' representatives are loaded together
+  // (the representative indices are valid whatever the type)
   const long long qb = (node - a.lb) * kQ;
-  const float val = lane < kQ ? qval[rep[qb + lane]] : 0.f;
+  const int8_t ntype = nd_type[node];
+  const int r = lane < kQ ? rep[qb + lane] : 0;
+  const float4 c = nd_c[node];
+  if (ntype != T_UNCERTAIN) return;  // warp-uniform
+  const float val = lane < kQ ? qval[r] : 0.f;
   // GridEval sign change against sample 0, ">= 0" (src/evaluator.cpp:169-172)
   const unsigned pos_mask = __ballot_sync(0xffffffffu, lane < 27 && val >= 0.f);
   const bool origin = pos_mask & 1u;
   const bool signchange = origin ? (pos_mask != 0x07ffffffu) : (pos_mask != 0u);
   const float vc = __shfl_sync(0xffffffffu, val, 27);
   if (qef && lane < 27) nd_samp[node * 27 + lane] = val;
-  const float4 c = nd_c[node];
   const float cellsize = 2.0f * c.w;
   const bool leaf_by_size = (double)(cellsize - a.radius) < 1e-8;
   int8_t type = T_LEAF;
