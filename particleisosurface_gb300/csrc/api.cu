@@ -382,6 +382,7 @@ int pi_ctx_create(int device, size_t budget_bytes, pi_ctx** out) {
   c->coop_blocks = top_levels_grid(device, c->smCount);
   PI_CUDA(cudaEventCreateWithFlags(&c->ev_tris_ready, cudaEventDisableTiming));
   PI_CUDA(cudaEventCreateWithFlags(&c->ev_tris_copied, cudaEventDisableTiming));
+  PI_CUDA(cudaEventCreateWithFlags(&c->ev_read, cudaEventDisableTiming));
   cudaMemPool_t pool;
   PI_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
   uint64_t thr = UINT64_MAX;
@@ -402,6 +403,7 @@ static void ctx_release(pi_ctx* c) {
   }
   if (c->ev_tris_ready) cudaEventDestroy(c->ev_tris_ready);
   if (c->ev_tris_copied) cudaEventDestroy(c->ev_tris_copied);
+  if (c->ev_read) cudaEventDestroy(c->ev_read);
   cudaStreamDestroy(c->stream);
   (void)cudaGetLastError();
   delete c;

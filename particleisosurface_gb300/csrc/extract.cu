@@ -544,6 +544,19 @@ static int read_int(pi_frame* f, const int* d) {
   return v;
 }
 
+// A count read in two halves: the copy to pinned memory is queued, the
+// caller queues a kernel that does not need the count, then waits for the
+// copy only, so the device is busy while the host takes the value.
+static void read_int_start(pi_frame* f, const int* d) {
+  int* const h = reinterpret_cast<int*>(f->ctx->hpin + kPinReadOffset);
+  PI_CUDA(cudaMemcpyAsync(h, d, sizeof(int), cudaMemcpyDeviceToHost, f->ctx->stream));
+  PI_CUDA(cudaEventRecord(f->ctx->ev_read, f->ctx->stream));
+}
+static int read_int_finish(pi_frame* f) {
+  PI_CUDA(cudaEventSynchronize(f->ctx->ev_read));
+  return *reinterpret_cast<const int*>(f->ctx->hpin + kPinReadOffset);
+}
+
 void stage_extract(pi_frame* f) {
   pi_ctx* c = f->ctx;
   cudaStream_t s = c->stream;
@@ -555,10 +568,11 @@ void stage_extract(pi_frame* f) {
   tmp.alloc(c, s, scan_tmp_ints(nn * 8 + 1));
   PI_LAUNCH(k_leaf_flag, div_up(nn + 1, 256), 256, 0, s, f->nd_child.p, nn, flag.p);
   exclusive_scan_i32(flag.p, flag.p, nn + 1, nullptr, tmp.p, s);
-  const long long nl = read_int(f, flag.p + nn);
-  f->nLeaves = nl;
-  leaves.alloc(c, s, nl > 0 ? nl : 1);
+  read_int_start(f, flag.p + nn);
+  leaves.alloc(c, s, nn > 0 ? nn : 1);  // room for every node
   PI_LAUNCH(k_leaf_list, div_up(nn, 256), 256, 0, s, f->nd_child.p, flag.p, nn, leaves.p);
+  const long long nl = read_int_finish(f);
+  f->nLeaves = nl;
   // 2. dual vertices = unique interior leaf corners
   const int B = f->dmax + 1;
   const int full = 1 << f->dmax;
@@ -668,10 +682,11 @@ void stage_extract(pi_frame* f) {
             vwhere.p);
   PI_LAUNCH(k_first_flag, div_up(ns + 1, 256), 256, 0, s, ns, vtab.p, vwhere.p, vrank.p);
   exclusive_scan_i32(vrank.p, vrank.p, ns + 1, nullptr, tmp.p, s);
-  const long long nv = read_int(f, vrank.p + ns);
+  read_int_start(f, vrank.p + ns);
   slot_vertex.alloc(c, s, ns > 0 ? ns : 1);
-  rep.alloc(c, s, nv > 0 ? nv : 1);
+  rep.alloc(c, s, ns > 0 ? ns : 1);  // room for a vertex per slot
   PI_LAUNCH(k_vertex_map, div_up(ns, 256), 256, 0, s, ns, vtab.p, vwhere.p, vrank.p, slot_vertex.p, rep.p);
+  const long long nv = read_int_finish(f);
   vtab.release();
   vwhere.release();
   vrank.release();
@@ -696,10 +711,11 @@ void stage_extract(pi_frame* f) {
   PI_LAUNCH(k_tri_insert, div_up(nt0, 256), 256, 0, s, nt0, otri.p, tmask, ttab.p, twhere.p);
   PI_LAUNCH(k_first_flag, div_up(nt0 + 1, 256), 256, 0, s, nt0, ttab.p, twhere.p, trank.p);
   exclusive_scan_i32(trank.p, trank.p, nt0 + 1, nullptr, tmp.p, s);
-  const long long nt = read_int(f, trank.p + nt0);
-  f->nT = nt;
-  f->mt.alloc(c, s, nt * 3 > 0 ? nt * 3 : 3);
+  read_int_start(f, trank.p + nt0);
+  f->mt.alloc(c, s, nt0 * 3 > 0 ? nt0 * 3 : 3);  // room for every generated triangle
   PI_LAUNCH(k_tri_write, div_up(nt0, 256), 256, 0, s, nt0, trank.p, otri.p, f->mt.p);
+  const long long nt = read_int_finish(f);
+  f->nT = nt;
   if (f->host_tris && nt > 0 && nt <= f->host_tcap) {
     PI_CUDA(cudaEventRecord(c->ev_tris_ready, s));
     PI_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_tris_ready, 0));

@@ -79,6 +79,7 @@ struct pi_ctx {
   // stream (pi_reconstruct's triangle download), and its two events
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t ev_tris_ready = nullptr, ev_tris_copied = nullptr;
+  cudaEvent_t ev_read = nullptr;  // the extraction's split count reads
 };
 
 struct pi_frame {
@@ -155,7 +156,9 @@ constexpr int kPinValid = kPinSlots;  // bit of pin_pending for the valid-key co
 // INTERNAL count; then the coarse-level kernel's level starts and depth
 constexpr int kPinTopOffset = kPinSlots * kCounterWords + 8;
 constexpr int kPinTopWords = 32;
-constexpr int kPinWords = kPinTopOffset + kPinTopWords;
+// one word for the extraction's split count reads
+constexpr int kPinReadOffset = kPinTopOffset + kPinTopWords;
+constexpr int kPinWords = kPinReadOffset + 8;
 // event that marks the INTERNAL count's copy in the octree level loop
 constexpr int kLevelEvent = 16;
 // Copies the frame's device counters into pinned slot `slot` (stream-ordered,
