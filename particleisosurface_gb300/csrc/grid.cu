@@ -51,12 +51,31 @@ __global__ void k_bbox(const float* __restrict__ xyz, long long n, unsigned* __r
     }
   }
   for (int o = 16; o > 0; o >>= 1) bad += __shfl_xor_sync(0xffffffffu, bad, o);
-  if ((threadIdx.x & 31) == 0) {
+  // the block's warps combine in shared memory, so that each block issues one
+  // set of atomics (all blocks hit the same seven words)
+  __shared__ unsigned s_v[32][7];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
     for (int k = 0; k < 3; ++k) {
-      atomicMin(misc + 2 * k, mn[k]);
-      atomicMax(misc + 2 * k + 1, mx[k]);
+      s_v[warp][2 * k] = mn[k];
+      s_v[warp][2 * k + 1] = mx[k];
     }
-    if (bad) atomicAdd(misc + 6, bad);
+    s_v[warp][6] = bad;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    for (int w = 1; w < nw; ++w)
+      for (int k = 0; k < 3; ++k) {
+        s_v[0][2 * k] = min(s_v[0][2 * k], s_v[w][2 * k]);
+        s_v[0][2 * k + 1] = max(s_v[0][2 * k + 1], s_v[w][2 * k + 1]);
+      }
+    for (int w = 1; w < nw; ++w) s_v[0][6] += s_v[w][6];
+    for (int k = 0; k < 3; ++k) {
+      atomicMin(misc + 2 * k, s_v[0][2 * k]);
+      atomicMax(misc + 2 * k + 1, s_v[0][2 * k + 1]);
+    }
+    if (s_v[0][6]) atomicAdd(misc + 6, s_v[0][6]);
   }
 }
 
@@ -126,7 +145,7 @@ void stage_hashgrid(pi_frame* f) {
   const long long n = f->N;
   f->misc.alloc(f->ctx, s, 16);
   PI_LAUNCH(k_init_misc, 1, 32, 0, s, f->misc.p);
-  int blocks = (int)std::min<long long>(div_up(n, 256), (long long)f->ctx->smCount * 8);
+  int blocks = (int)std::min<long long>(div_up(n, 256), (long long)f->ctx->smCount * 2);
   PI_LAUNCH(k_bbox, blocks, 256, 0, s, f->xyz.p, n, f->misc.p);
   unsigned h[8];
   PI_CUDA(cudaMemcpyAsync(h, f->misc.p, sizeof(unsigned) * 8, cudaMemcpyDeviceToHost, s));
