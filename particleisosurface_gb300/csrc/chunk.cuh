@@ -22,6 +22,14 @@ __device__ __forceinline__ int fkey(float v) {
 }
 __device__ __forceinline__ float fkey_inv(int k) { return __int_as_float(k >= 0 ? k : k ^ 0x7fffffff); }
 
+// 16-byte asynchronous copy global -> shared (cp.async, no register
+// staging); completed by cp_async_wait_all before the records are read.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Per-warp staging buffers (shared memory), kCandBuf records each.
 struct ChunkStage {
   float4* x;
@@ -69,6 +77,7 @@ __device__ __forceinline__ void chunk_field(const GridView& g, const PartView& P
   for (int m = 0; m < K; ++m) s[m] = c[m] = 0.f;
   int nc = 0;
   auto flush = [&]() {
+    cp_async_wait_all();
     __syncwarp();
 #pragma unroll 2
     for (int t = 0; t < nc; ++t) {
@@ -110,9 +119,9 @@ __device__ __forceinline__ void chunk_field(const GridView& g, const PartView& P
         if (pass) {
           const int p = nc + __popc(pm & lt);
           st.x[p] = x;
-          st.a[p] = __ldg(P.ga + j);
-          st.b[p] = __ldg(P.gb + j);
-          st.l[p] = __ldg(P.xlo + j);
+          cp_async16(st.a + p, P.ga + j);
+          cp_async16(st.b + p, P.gb + j);
+          cp_async16(st.l + p, P.xlo + j);
         }
         nc += __popc(pm);
         if (nc > kCandBuf - 32) flush();
