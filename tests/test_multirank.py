@@ -32,7 +32,9 @@ def _rank_main(rank, world, port, out):
 
 def test_rank_max_over_two_gloo_ranks():
     port = _free_port()
-    with mp.Manager() as m:
+    # the manager process is started with spawn, not fork: this test may run
+    # in a process that has already used the GPU
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_rank_main, args=(2, port, out), nprocs=2, join=True)
         assert dict(out) == {0: 15.0, 1: 15.0}
