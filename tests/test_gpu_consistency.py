@@ -45,3 +45,21 @@ def test_leaf_values_equal_point_evaluation(ctx, case, qef):
     bad = np.nonzero(val.view(np.uint32) != stored.view(np.uint32))[0]
     assert len(bad) == 0, (len(bad), pts[bad[:3]], val[bad[:3]], stored[bad[:3]])
     g.close()
+
+
+def test_leaf_values_equal_point_evaluation_at_full_size(ctx):
+    """The same check on the 1M-particle dam-break frame (the benchmark's
+    workload), on 200,000 leaves drawn at random: a size-independent
+    property, where the oracle would take minutes."""
+    fr = synth.dam_break(n=1_000_000, seed=2)
+    g = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz).run()
+    nodes = g.dump(N.DUMP_NODES)
+    leaves = nodes[nodes["type"] == T_LEAF]
+    assert len(leaves) > 1_000_000
+    pick = np.random.default_rng(3).choice(len(leaves), 200_000, replace=False)
+    leaves = leaves[pick]
+    pts = np.ascontiguousarray(leaves["node"][:, :3])
+    val = g.eval(pts)
+    stored = leaves["node"][:, 3]
+    assert np.array_equal(val.view(np.uint32), stored.view(np.uint32))
+    g.close()
