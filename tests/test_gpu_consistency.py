@@ -63,3 +63,53 @@ def test_leaf_values_equal_point_evaluation_at_full_size(ctx):
     stored = leaves["node"][:, 3]
     assert np.array_equal(val.view(np.uint32), stored.view(np.uint32))
     g.close()
+
+
+def test_octree_and_mesh_invariants_at_full_size(ctx):
+    """Structural properties of the 1M frame's octree and mesh: levels are
+    contiguous, every INTERNAL node has its 8 children (ids parent * 8 + k,
+    centres parent +- half / 2) and no leaf has any; every mesh vertex lies
+    on the segment between the positions of the two leaves of its key, and
+    every triangle indexes existing vertices."""
+    fr = synth.dam_break(n=1_000_000, seed=2)
+    g = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz).run()
+    nodes = g.dump(N.DUMP_NODES)
+    v, t, k = g.mesh(keys=True)
+    g.close()
+    depth = nodes["depth"].astype(np.int64)
+    assert np.all(np.diff(depth) >= 0)
+    internal = np.nonzero(nodes["type"] == 1)[0]
+    fc = nodes["first_child"]
+    assert np.all(fc[nodes["type"] != 1] == -1)
+    assert len(nodes) == 1 + 8 * len(internal)
+    kids = fc[internal][:, None] + np.arange(8)[None, :]
+    assert np.all(nodes["parent"][kids] == internal[:, None])
+    assert np.all(nodes["id"][kids] == nodes["id"][internal][:, None] * 8 + np.arange(8, dtype=np.uint64))
+    half = nodes["half"][internal][:, None, None]
+    sign = np.array([[(1 if (q >> a) & 1 else -1) for a in range(3)] for q in range(8)], np.float32)
+    want = nodes["center"][internal][:, None, :] + sign[None] * (half / 2)
+    assert np.array_equal(nodes["center"][kids], want.astype(np.float32))
+    # mesh: vertex on the segment between its two leaves' points (ids can
+    # repeat across depths, as in the reference; vertices whose leaf ids
+    # are not unique among the leaves are left out)
+    leaf = np.nonzero(fc == -1)[0]
+    order = leaf[np.argsort(nodes["id"][leaf], kind="stable")]
+    ids = nodes["id"][order]
+    uniq = np.ones(len(ids), bool)
+    dup = ids[1:] == ids[:-1]
+    uniq[1:] &= ~dup
+    uniq[:-1] &= ~dup
+    ia, ib = np.searchsorted(ids, k[:, 0]), np.searchsorted(ids, k[:, 1])
+    assert np.all(ids[ia] == k[:, 0]) and np.all(ids[ib] == k[:, 1])
+    keep = uniq[ia] & uniq[ib]
+    assert keep.mean() > 0.99
+    v = v[keep].astype(np.float64)
+    a = nodes["node"][order[ia[keep]], :3].astype(np.float64)
+    b = nodes["node"][order[ib[keep]], :3].astype(np.float64)
+    ab = b - a
+    s = np.einsum("ij,ij->i", v - a, ab) / np.einsum("ij,ij->i", ab, ab)
+    off = np.linalg.norm(v - (a + s[:, None] * ab), axis=1)
+    assert np.all((s > -1e-5) & (s < 1 + 1e-5)) and off.max() < 1e-3 * fr.radius, (s.min(), s.max(), off.max())
+    # triangles index existing vertices (a triangle may repeat a vertex, as
+    # the reference's do, where leaves of different sizes meet)
+    assert t.min() >= 0 and t.max() < len(k)
