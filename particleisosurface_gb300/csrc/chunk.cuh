@@ -88,12 +88,12 @@ __device__ __forceinline__ void chunk_field(const GridView& g, const PartView& P
         float u0, u1, u2;
         amul(ga, gb, (qx[m] - x.x) - lo.x, (qy[m] - x.y) - lo.y, (qz[m] - x.z) - lo.z, u0, u1, u2);
         const float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
-        const float y = __fsub_rn(gb.z * bspline_s2(s2), c[m]);
-        const float tt = __fadd_rn(s[m], y);
-        const float cn = __fsub_rn(__fsub_rn(tt, s[m]), y);
-        const bool hit = s2 < 4.0f;
-        s[m] = hit ? tt : s[m];
-        c[m] = hit ? cn : c[m];
+        if (s2 < 4.0f) {  // in support: one compensated step
+          const float y = __fsub_rn(gb.z * bspline_s2(s2), c[m]);
+          const float tt = __fadd_rn(s[m], y);
+          c[m] = __fsub_rn(__fsub_rn(tt, s[m]), y);
+          s[m] = tt;
+        }
       }
     }
     __syncwarp();

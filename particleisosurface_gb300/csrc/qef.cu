@@ -63,6 +63,24 @@ __device__ void sym_eig4(double A[4][4], double w[4], double V[4][4]) {
   for (int i = 0; i < 4; ++i) w[i] = A[i][i];
 }
 
+// d / 2 for a double d that is 0 or at least 2^-1021 in magnitude (here a
+// difference of two floats, so at least 2^-149), exactly, on the integer
+// pipe: the exponent field is decremented.
+__device__ __forceinline__ double half_exact(double d) {
+  const long long b = __double_as_longlong(d);
+  return (b << 1) == 0 ? d : __longlong_as_double(b - (1LL << 52));
+}
+
+// Equilibration scale of a diagonal entry v: about v^-1/2 from the FP32
+// reciprocal square root when v converts to a normal float, the FP64 value
+// otherwise, 1 for v <= 0.  Any positive scale gives the same solution.
+__device__ __forceinline__ double equil_scale(double v) {
+  if (!(v > 0.0)) return 1.0;
+  const float vf = (float)v;
+  if (vf >= 1.17549435e-38f && vf <= 3.0e38f) return (double)rsqrtf(vf);
+  return 1.0 / sqrt(v);
+}
+
 struct QefArgs {
   GridView g;
   PartView P;
@@ -70,8 +88,8 @@ struct QefArgs {
   float radius;
   long long lb, le;
   // the level's finite-difference step (every node of a level has the same
-  // half size) as 1 / step and 1 / (2 step), in FP64
-  double i1, i2;
+  // half size), in FP64, and its reciprocal
+  double step, i1;
 };
 
 constexpr int kQefThreads = 64;
@@ -132,16 +150,25 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, float4* __restri
   double* const sd = &s_sv[0][threadIdx.x];  // sd[i * kQefThreads] = sample i
 #pragma unroll
   for (int i = 0; i < 27; ++i) sd[i * kQefThreads] = (double)sv[i];
-  // sample positions (GenerateSampling): three per axis
+  // sample positions (GenerateSampling): three per axis, in units of the
+  // finite-difference step (times 1 / step, see below)
+  const double i1 = a.i1;
   auto lattice = [&](int ax, int k) {
-    return (double)__fadd_rn(__fmul_rn(1.0f - k * 0.5f, mn[ax]), __fmul_rn(k * 0.5f, mx[ax]));
+    return (double)__fadd_rn(__fmul_rn(1.0f - k * 0.5f, mn[ax]), __fmul_rn(k * 0.5f, mx[ax])) * i1;
   };
   const double px0 = lattice(0, 0), px1 = lattice(0, 1), px2 = lattice(0, 2);
   const double py0 = lattice(1, 0), py1 = lattice(1, 1), py2 = lattice(1, 2);
   const double pz0 = lattice(2, 0), pz1 = lattice(2, 1), pz2 = lattice(2, 2);
-  // GridEval's finite differences (src/evaluator.cpp:185-240), in FP64 by
-  // multiplication with the reciprocal steps
-  const double i1 = a.i1, i2 = a.i2;
+  // GridEval's finite differences (src/evaluator.cpp:185-240) are g = d / step
+  // (one-sided) and g = d / (2 step) (central), d a difference of samples.
+  // NodeCalcNode's residual of plane i at (x, v) is g.(x - p) - v + f, which
+  // with y = x / step and q = p / step reads d'.(y - q) - v + f, d' = d or
+  // d / 2: the same least-squares problem in the variables (y, v), solved
+  // below and mapped back by x = step y.  So no sample difference is scaled
+  // by the step; the central ones are halved on the integer pipe, and only
+  // the nine lattice coordinates are multiplied (FP64 instructions bound this
+  // kernel).  The pseudo-inverse rule sees the same equilibrated matrix: a
+  // diagonal change of variables cancels in D A D.
   double q[15];
 #pragma unroll
   for (int k = 0; k < 15; ++k) q[k] = 0.0;
@@ -151,13 +178,14 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, float4* __restri
     const double py = y == 0 ? py0 : y == 1 ? py1 : py2;
     const double pz = z == 0 ? pz0 : z == 1 ? pz1 : pz2;
     auto fd = [&](int d, int stride) {
-      if (d == 0) return (sd[i * kQefThreads] - sd[(i + stride) * kQefThreads]) * i1;
-      if (d == 2) return (sd[(i - stride) * kQefThreads] - sd[i * kQefThreads]) * i1;
-      return (sd[(i - stride) * kQefThreads] - sd[(i + stride) * kQefThreads]) * i2;
+      if (d == 0) return sd[i * kQefThreads] - sd[(i + stride) * kQefThreads];
+      if (d == 2) return sd[(i - stride) * kQefThreads] - sd[i * kQefThreads];
+      return half_exact(sd[(i - stride) * kQefThreads] - sd[(i + stride) * kQefThreads]);
     };
     const double gx = fd(x, 1), gy = fd(y, 3), gz = fd(z, 9);
-    // plane [g, -1, f - p.g] (NodeCalcNode) accumulated as QEFNormal::combineSelf
-    const double pl[5] = {gx, gy, gz, -1.0, -(px * gx + py * gy + pz * gz) + sd[i * kQefThreads]};
+    // plane [d', -1, f - q.d'] accumulated as QEFNormal::combineSelf
+    const double w = fma(-pz, gz, fma(-py, gy, fma(-px, gx, sd[i * kQefThreads])));
+    const double pl[5] = {gx, gy, gz, -1.0, w};
     int idx = 0;
 #pragma unroll
     for (int r = 0; r < 5; ++r)
@@ -176,39 +204,46 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, float4* __restri
   }
   // Equilibrate: the gradient rows are ~|f| / step while the w column is 1,
   // so A's condition number exceeds what FP32 or even FP64 resolves.  With
-  // D = diag(A_ii)^-1/2 the solve is (D A D) y = D B, x = D y: the same
-  // minimiser in exact arithmetic, well conditioned unless the planes are
-  // degenerate.  Afterwards every non-zero diagonal entry is 1, so the
-  // largest eigenvalue lies in [1, 4] (or A = 0).
+  // a positive diagonal D close to diag(A_ii)^-1/2 the solve is
+  // (D A D) y = D B, x = D y: the same minimiser in exact arithmetic for any
+  // such D, well conditioned unless the planes are degenerate.  D is taken
+  // from the FP32 reciprocal square root (two conversions instead of an FP64
+  // square root and division); the equilibrated diagonal is then 1 to about
+  // 1e-7, and dmax, its largest entry, bounds the largest eigenvalue from
+  // below.
   double D[4];
 #pragma unroll
-  for (int r = 0; r < 4; ++r) D[r] = A[r][r] > 0.0 ? 1.0 / sqrt(A[r][r]) : 1.0;
+  for (int r = 0; r < 4; ++r) D[r] = equil_scale(A[r][r]);
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     B[r] *= D[r];
 #pragma unroll
-    for (int s2 = 0; s2 < 4; ++s2) A[r][s2] *= D[r] * D[s2];
+    for (int s2 = r; s2 < 4; ++s2) A[r][s2] = A[s2][r] = A[r][s2] * (D[r] * D[s2]);
   }
+  const double dmax = fmax(fmax(A[0][0], A[1][1]), fmax(A[2][2], A[3][3]));
   // Pseudo-inverse rule: eigenvalues at most 1e-12 * max |eigenvalue| are
   // dropped, and a system with a dropped eigenvalue counts as singular (the
   // reference's Matrix4f::inverse gives non-finite values there and the
   // vertex is rejected).  Decided without an eigen-decomposition where the
   // bounds settle it: the smallest eigenvalue is at most every LDL^T pivot,
-  // and at least 1 / ||A^-1||_F, while the largest lies in [1, trace].
+  // and at least 1 / ||A^-1||_F, while the largest lies in [dmax, trace].
   const double tr = A[0][0] + A[1][1] + A[2][2] + A[3][3];
   bool singular, solved = false;
   double xs[4] = {0.0, 0.0, 0.0, 0.0};
   double Ai[4][4];
-  const int ok = tr > 0.0 ? ldlt_inverse4(A, 1e-12, Ai) : 0;
+  const int ok = tr > 0.0 ? ldlt_inverse4(A, 1e-12 * dmax, Ai) : 0;
   if (!(tr > 0.0) || !ok) {
-    singular = true;  // a pivot below 1e-12 <= 1e-12 * max eigenvalue
+    singular = true;  // a pivot below 1e-12 dmax <= 1e-12 * max eigenvalue
     solved = true;
   } else {
-    double f2 = 0.0;
+    double f2 = 0.0, f2o = 0.0;  // ||A^-1||_F^2: diagonal, twice the upper part
 #pragma unroll
-    for (int r = 0; r < 4; ++r)
+    for (int r = 0; r < 4; ++r) {
+      f2 = fma(Ai[r][r], Ai[r][r], f2);
 #pragma unroll
-      for (int s2 = 0; s2 < 4; ++s2) f2 += Ai[r][s2] * Ai[r][s2];
+      for (int s2 = r + 1; s2 < 4; ++s2) f2o = fma(Ai[r][s2], Ai[r][s2], f2o);
+    }
+    f2 = fma(2.0, f2o, f2);
     const double t = 1e-12 * tr;
     singular = false;
     if (f2 * t * t < 1.0) {  // smallest eigenvalue > 1e-12 * trace >= tolerance
@@ -242,6 +277,8 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, float4* __restri
   if (!singular) {
 #pragma unroll
     for (int r = 0; r < 4; ++r) xs[r] *= D[r];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) xs[r] *= a.step;  // x = step y
     const bool in_cell = xs[0] >= mn[0] && xs[0] <= mx[0] && xs[1] >= mn[1] && xs[1] <= mx[1] &&
                          xs[2] >= mn[2] && xs[2] <= mx[2];
     if (in_cell) {
@@ -292,8 +329,8 @@ void qef_level(pi_frame* f, long long lb, long long le, int depth) {
              f->P.radius,
              lb,
              le,
-             1.0 / (double)step,
-             1.0 / (2.0 * (double)step)};
+             (double)step,
+             1.0 / (double)step};
   PI_LAUNCH(k_qef, div_up(le - lb, kQefThreads), kQefThreads, 0, s, qa, f->nd_v.p, f->nd_c.p, f->nd_type.p,
             f->nd_samp.p, nullptr, f->dcount.p);
 }
