@@ -71,6 +71,17 @@ __device__ __forceinline__ double half_exact(double d) {
   return (b << 1) == 0 ? d : __longlong_as_double(b - (1LL << 52));
 }
 
+// (double)f on the integer pipe for a normal float f (the exponent rebased
+// from 127 to 1023, the 23 fraction bits moved to the top of the 52), the
+// hardware conversion for zero, subnormal, infinite and NaN inputs.
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (double)f;
+  const unsigned hi = (u & 0x80000000u) | (((u >> 3) & 0x0fffffffu) + (896u << 20));
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+
 // Equilibration scale of a diagonal entry v: about v^-1/2 from the FP32
 // reciprocal square root when v converts to a normal float, the FP64 value
 // otherwise, 1 for v <= 0.  Any positive scale gives the same solution.
@@ -135,8 +146,8 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, float4* __restri
                                                      const int8_t* __restrict__ nd_type,
                                                      const float* __restrict__ nd_samp, float* __restrict__ qef_err,
                                                      unsigned long long* __restrict__ counters) {
-  // the 27 sample values in FP64, converted once per leaf (conversions run on
-  // the FP64 pipe, which bounds this kernel)
+  // the 27 sample values in FP64, converted once per leaf on the integer
+  // pipe (the FP64 pipe bounds this kernel)
   __shared__ double s_sv[27][kQefThreads];
   const long long node = a.lb + (long long)blockIdx.x * kQefThreads + threadIdx.x;
   if (node >= a.le || nd_type[node] != Q_LEAF) return;
@@ -149,12 +160,12 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, float4* __restri
   const float* sv = nd_samp + node * 27;
   double* const sd = &s_sv[0][threadIdx.x];  // sd[i * kQefThreads] = sample i
 #pragma unroll
-  for (int i = 0; i < 27; ++i) sd[i * kQefThreads] = (double)sv[i];
+  for (int i = 0; i < 27; ++i) sd[i * kQefThreads] = f2d_exact(sv[i]);
   // sample positions (GenerateSampling): three per axis, in units of the
   // finite-difference step (times 1 / step, see below)
   const double i1 = a.i1;
   auto lattice = [&](int ax, int k) {
-    return (double)__fadd_rn(__fmul_rn(1.0f - k * 0.5f, mn[ax]), __fmul_rn(k * 0.5f, mx[ax])) * i1;
+    return f2d_exact(__fadd_rn(__fmul_rn(1.0f - k * 0.5f, mn[ax]), __fmul_rn(k * 0.5f, mx[ax]))) * i1;
   };
   const double px0 = lattice(0, 0), px1 = lattice(0, 1), px2 = lattice(0, 2);
   const double py0 = lattice(1, 0), py1 = lattice(1, 1), py2 = lattice(1, 2);
@@ -169,9 +180,17 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, float4* __restri
   // the nine lattice coordinates are multiplied (FP64 instructions bound this
   // kernel).  The pseudo-inverse rule sees the same equilibrated matrix: a
   // diagonal change of variables cancels in D A D.
+  //
+  // The plane's -1 entry makes q[3], q[7], q[10] minus the sums of the
+  // differences over the 27 samples.  Along one row of three samples
+  // s0, s1, s2 those are (s0 - s1) + (s0 - s2) / 2 + (s1 - s2) = 3 times the
+  // central one, so each is taken as -3 times the sum over the 9 central
+  // samples of its axis.
   double q[15];
+  double cx = 0.0, cy = 0.0, cz = 0.0;
 #pragma unroll
   for (int k = 0; k < 15; ++k) q[k] = 0.0;
+#pragma unroll
   for (int i = 0; i < 27; ++i) {
     const int x = i % 3, y = (i / 3) % 3, z = i / 9;
     const double px = x == 0 ? px0 : x == 1 ? px1 : px2;
@@ -186,13 +205,19 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, float4* __restri
     // plane [d', -1, f - q.d'] accumulated as QEFNormal::combineSelf
     const double w = fma(-pz, gz, fma(-py, gy, fma(-px, gx, sd[i * kQefThreads])));
     const double pl[5] = {gx, gy, gz, -1.0, w};
+    if (x == 1) cx += gx;
+    if (y == 1) cy += gy;
+    if (z == 1) cz += gz;
     int idx = 0;
 #pragma unroll
     for (int r = 0; r < 5; ++r)
 #pragma unroll
       for (int s2 = r; s2 < 5; ++s2, ++idx)
-        if (idx != 12) q[idx] += pl[r] * pl[s2];
+        if (idx != 3 && idx != 7 && idx != 10 && idx != 12) q[idx] += pl[r] * pl[s2];
   }
+  q[3] = -3.0 * cx;
+  q[7] = -3.0 * cy;
+  q[10] = -3.0 * cz;
   q[12] = 27.0;  // the (-1) x (-1) entry: 27 ones
   double A[4][4], B[4];
 #pragma unroll
