@@ -102,10 +102,17 @@ def batch64(a):
     ctx.close()
     # device-resident form: the 64 frames stay uploaded; one at a time on one
     # context versus spread over `slots` contexts (own streams) driven by as
-    # many host threads (the C calls release the GIL)
+    # many host threads (the C calls release the GIL).  Frames go to the
+    # contexts largest first, each to the least-loaded one (by particles), so
+    # that the threads finish together.
     import threading
     ctxs = [N.Context(0) for _ in range(a.slots)]
-    res = [N.Frame(ctxs[k % a.slots], N.default_params(fr.radius)).upload(fr.xyz) for k, fr in enumerate(frames)]
+    load = [0] * a.slots
+    owner = [0] * len(frames)
+    for k in sorted(range(len(frames)), key=lambda k: -frames[k].n):
+        owner[k] = min(range(a.slots), key=lambda s: load[s])
+        load[owner[k]] += frames[k].n
+    res = [N.Frame(ctxs[owner[k]], N.default_params(fr.radius)).upload(fr.xyz) for k, fr in enumerate(frames)]
     for f in res[:2]:
         f.reset().run()
     t0 = time.perf_counter()
@@ -114,7 +121,7 @@ def batch64(a):
     t_res_seq = time.perf_counter() - t0
 
     def work(k):
-        for f in res[k::a.slots]:
+        for f in sorted((res[j] for j in range(len(res)) if owner[j] == k), key=lambda f: -f.n):
             f.reset().run()
 
     t0 = time.perf_counter()
@@ -132,8 +139,9 @@ def batch64(a):
     srv = N.Server(0, slots=a.slots, budget_bytes=0)
     for fr in frames[:2]:
         srv.result(srv.submit(fr.xyz, N.default_params(fr.radius)))
+    # a batch job: submitted largest first (the request loop admits in order)
     t0 = time.perf_counter()
-    tickets = [srv.submit(fr.xyz, N.default_params(fr.radius)) for fr in frames]
+    tickets = [srv.submit(fr.xyz, N.default_params(fr.radius)) for fr in sorted(frames, key=lambda fr: -fr.n)]
     lat = [srv.result(t)[2] for t in tickets]
     t_bat = time.perf_counter() - t0
     st = srv.stats()
