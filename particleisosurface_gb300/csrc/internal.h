@@ -183,7 +183,9 @@ void stage_extract(pi_frame* f);
 // Grid (blocks) of the cooperative coarse-level octree kernel on `device`,
 // 0 where cooperative launches are not available.
 int top_levels_grid(int device, int sm_count);
-void qef_level(pi_frame* f, long long lb, long long le, int depth);
+// QEF vertices of the leaves of level [lb, le); scratch holds at least
+// le - lb + 1 ints (device memory the caller no longer needs).
+void qef_level(pi_frame* f, long long lb, long long le, int depth, int* scratch);
 // UniformGrid: lattice of the loadRootBox box; sampling into d_out (device,
 // x fastest) when cap holds it; returns the number of lattice points.
 void uniform_grid_host(const pi_frame* f, float box[6], int steps[3], int dims[3]);

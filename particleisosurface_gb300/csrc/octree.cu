@@ -1081,7 +1081,7 @@ void stage_octree(pi_frame* f) {
       prof_end(ctx, s, -1, -1);
       PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p, f->nd_type.p,
                 f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p);
-      if (f->P.qef) qef_level(f, lb, le, depth);
+      if (f->P.qef) qef_level(f, lb, le, depth, qkey.p);  // the sample keys are spent (qn >= nl + 1)
     }
     flag.alloc(ctx, s, nl + 1);
     if (f->tmp.n < scan_tmp_ints(nl + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(nl + 1));

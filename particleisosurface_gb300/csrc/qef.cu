@@ -140,17 +140,36 @@ __device__ int ldlt_inverse4(const double A[4][4], double floor, double Ai[4][4]
   return 1;
 }
 
+// The leaves of the level [lb, le), as offsets node - lb, so that k_qef's
+// threads are all leaves: the FP64 pipe issues per warp instruction, and a
+// thread that has no leaf would leave its lane of every FP64 instruction
+// idle (on a level with few leaves most of them).  One atomic per warp;
+// list[0] counts the leaves and they follow from list[1] (each warp's in
+// node order; each leaf's result does not depend on the order).
+__global__ void k_qef_pick(const int8_t* __restrict__ nd_type, long long lb, long long le, int* __restrict__ list) {
+  const long long node = lb + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool leaf = node < le && nd_type[node] == Q_LEAF;
+  const unsigned m = __ballot_sync(0xffffffffu, leaf);
+  if (m == 0u) return;  // warp-uniform
+  int base = 0;
+  if (lane == 0) base = atomicAdd(list, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (leaf) list[1 + base + __popc(m & ((1u << lane) - 1u))] = (int)(node - lb);
+}
+
 // counters: 5 QEF vertices accepted, 6 singular systems, 7 field evaluations
-__global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, float4* __restrict__ nd_v,
+__global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, const int* __restrict__ list,
+                                                     float4* __restrict__ nd_v,
                                                      const float4* __restrict__ nd_c,
-                                                     const int8_t* __restrict__ nd_type,
                                                      const float* __restrict__ nd_samp, float* __restrict__ qef_err,
                                                      unsigned long long* __restrict__ counters) {
   // the 27 sample values in FP64, converted once per leaf on the integer
   // pipe (the FP64 pipe bounds this kernel)
   __shared__ double s_sv[27][kQefThreads];
-  const long long node = a.lb + (long long)blockIdx.x * kQefThreads + threadIdx.x;
-  if (node >= a.le || nd_type[node] != Q_LEAF) return;
+  const int t = blockIdx.x * kQefThreads + threadIdx.x;
+  if (t >= __ldg(list)) return;
+  const long long node = a.lb + __ldg(list + 1 + t);
   const float4 c = nd_c[node];
   const float h = c.w;
   const float cellsize = 2.0f * h;
@@ -342,7 +361,7 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, float4* __restri
   if (qef_err) qef_err[node] = err;
 }
 
-void qef_level(pi_frame* f, long long lb, long long le, int depth) {
+void qef_level(pi_frame* f, long long lb, long long le, int depth, int* scratch) {
   cudaStream_t s = f->ctx->stream;
   const GridHost& gh = f->g;
   // half size of the level's nodes (the root's halved exactly per level);
@@ -356,7 +375,9 @@ void qef_level(pi_frame* f, long long lb, long long le, int depth) {
              le,
              (double)step,
              1.0 / (double)step};
-  PI_LAUNCH(k_qef, div_up(le - lb, kQefThreads), kQefThreads, 0, s, qa, f->nd_v.p, f->nd_c.p, f->nd_type.p,
+  PI_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int), s));
+  PI_LAUNCH(k_qef_pick, div_up(le - lb, 256), 256, 0, s, f->nd_type.p, lb, le, scratch);
+  PI_LAUNCH(k_qef, div_up(le - lb, kQefThreads), kQefThreads, 0, s, qa, scratch, f->nd_v.p, f->nd_c.p,
             f->nd_samp.p, nullptr, f->dcount.p);
 }
 
