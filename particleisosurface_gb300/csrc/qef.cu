@@ -105,12 +105,11 @@ struct QefArgs {
 
 constexpr int kQefThreads = 64;
 
-// LDL^T factorisation of the symmetric 4x4 A (no pivoting) and, when every
-// pivot is at least `floor`, the inverse A^-1 = L^-T diag(1/d) L^-1.
-// Returns 0 if a pivot is below `floor`, 1 otherwise.
-__device__ int ldlt_inverse4(const double A[4][4], double floor, double Ai[4][4]) {
+// LDL^T factorisation of the symmetric 4x4 A (no pivoting): pivots d, their
+// reciprocals id, and M = L^-1 (unit lower triangular), so that
+// A^-1 = M^T diag(id) M.  Returns 0 if a pivot is below `floor`, 1 otherwise.
+__device__ int ldlt4(const double A[4][4], double floor, double d[4], double id[4], double M[4][4]) {
   double L[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
-  double d[4], id[4];
   for (int j = 0; j < 4; ++j) {
     double dj = A[j][j];
     for (int k = 0; k < j; ++k) dj -= L[j][k] * L[j][k] * d[k];
@@ -123,19 +122,13 @@ __device__ int ldlt_inverse4(const double A[4][4], double floor, double Ai[4][4]
       L[i][j] = l * id[j];
     }
   }
-  // M = L^-1 (unit lower triangular)
-  double M[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) M[i][j] = i == j ? 1.0 : 0.0;
   for (int i = 1; i < 4; ++i)
     for (int j = 0; j < i; ++j) {
       double v = -L[i][j];
       for (int k = j + 1; k < i; ++k) v -= L[i][k] * M[k][j];
       M[i][j] = v;
-    }
-  for (int r = 0; r < 4; ++r)
-    for (int c = r; c < 4; ++c) {
-      double v = 0.0;
-      for (int k = c; k < 4; ++k) v += M[k][r] * id[k] * M[k][c];
-      Ai[r][c] = Ai[c][r] = v;
     }
   return 1;
 }
@@ -270,30 +263,70 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, const int* __res
   // reference's Matrix4f::inverse gives non-finite values there and the
   // vertex is rejected).  Decided without an eigen-decomposition where the
   // bounds settle it: the smallest eigenvalue is at most every LDL^T pivot,
-  // and at least 1 / ||A^-1||_F, while the largest lies in [dmax, trace].
+  // and at least min(d) / ||M||_F^2 and 1 / ||A^-1||_F (A^-1 = M^T D^-1 M,
+  // so ||A^-1||_2 <= ||M||_2^2 / min(d)), while the largest lies in
+  // [dmax, trace].  The first lower bound costs a few instructions and
+  // settles the dam-break leaves with a margin of 1e6 or more; the second
+  // needs the whole inverse and is the fallback.
   const double tr = A[0][0] + A[1][1] + A[2][2] + A[3][3];
   bool singular, solved = false;
   double xs[4] = {0.0, 0.0, 0.0, 0.0};
-  double Ai[4][4];
-  const int ok = tr > 0.0 ? ldlt_inverse4(A, 1e-12 * dmax, Ai) : 0;
+  double dd[4], id[4], M[4][4];
+  const int ok = tr > 0.0 ? ldlt4(A, 1e-12 * dmax, dd, id, M) : 0;
   if (!(tr > 0.0) || !ok) {
     singular = true;  // a pivot below 1e-12 dmax <= 1e-12 * max eigenvalue
     solved = true;
   } else {
-    double f2 = 0.0, f2o = 0.0;  // ||A^-1||_F^2: diagonal, twice the upper part
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      f2 = fma(Ai[r][r], Ai[r][r], f2);
-#pragma unroll
-      for (int s2 = r + 1; s2 < 4; ++s2) f2o = fma(Ai[r][s2], Ai[r][s2], f2o);
-    }
-    f2 = fma(2.0, f2o, f2);
-    const double t = 1e-12 * tr;
     singular = false;
-    if (f2 * t * t < 1.0) {  // smallest eigenvalue > 1e-12 * trace >= tolerance
+    double m2 = 4.0;
 #pragma unroll
-      for (int r = 0; r < 4; ++r) xs[r] = Ai[r][0] * B[0] + Ai[r][1] * B[1] + Ai[r][2] * B[2] + Ai[r][3] * B[3];
+    for (int r = 1; r < 4; ++r)
+#pragma unroll
+      for (int c2 = 0; c2 < r; ++c2) m2 = fma(M[r][c2], M[r][c2], m2);
+    const double dmin = fmin(fmin(dd[0], dd[1]), fmin(dd[2], dd[3]));
+    const double t = 1e-12 * tr;
+    if (dmin > t * m2) {
+      // x = M^T D^-1 M B: forward product, scaling, back product
+      double z[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        double v = B[r];
+#pragma unroll
+        for (int k = 0; k < r; ++k) v = fma(M[r][k], B[k], v);
+        z[r] = v * id[r];
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        double v = z[r];
+#pragma unroll
+        for (int k = r + 1; k < 4; ++k) v = fma(M[k][r], z[k], v);
+        xs[r] = v;
+      }
       solved = true;
+    } else {
+      double Ai[4][4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c2 = r; c2 < 4; ++c2) {
+          double v = 0.0;
+#pragma unroll
+          for (int k = c2; k < 4; ++k) v += M[k][r] * id[k] * M[k][c2];
+          Ai[r][c2] = Ai[c2][r] = v;
+        }
+      double f2 = 0.0, f2o = 0.0;  // ||A^-1||_F^2: diagonal, twice the upper part
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        f2 = fma(Ai[r][r], Ai[r][r], f2);
+#pragma unroll
+        for (int s2 = r + 1; s2 < 4; ++s2) f2o = fma(Ai[r][s2], Ai[r][s2], f2o);
+      }
+      f2 = fma(2.0, f2o, f2);
+      if (f2 * t * t < 1.0) {  // smallest eigenvalue > 1e-12 * trace >= tolerance
+#pragma unroll
+        for (int r = 0; r < 4; ++r) xs[r] = Ai[r][0] * B[0] + Ai[r][1] * B[1] + Ai[r][2] * B[2] + Ai[r][3] * B[3];
+        solved = true;
+      }
     }
   }
   if (!solved) {
