@@ -157,7 +157,7 @@ __device__ __forceinline__ void g_from_eig(const T w_in[3], const T V[3][3], flo
   *stretch = (float)(wmax / scale);
 }
 
-__global__ void k_cov_G(GridView g, const float4* __restrict__ pos, const float4* __restrict__ xm0,
+__global__ void __launch_bounds__(128, 8) k_cov_G(GridView g, const float4* __restrict__ pos, const float4* __restrict__ xm0,
                         const float4* __restrict__ xlo, float4* __restrict__ xm, long long n,
                         float nI, float nI2, float inv_h3, float h2, float inv_h, float sigma,
                         float4* __restrict__ ga, float4* __restrict__ gb, float* __restrict__ gfull,
