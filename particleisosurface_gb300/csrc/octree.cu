@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(256, 4) k_leaf_level(LevelArgs a, const float4
   }
 }
 
-__global__ void k_classify(LevelArgs a, const float* __restrict__ qval, const int* __restrict__ rep,
+__global__ void __launch_bounds__(64, 24) k_classify(LevelArgs a, const float* __restrict__ qval, const int* __restrict__ rep,
                            const float4* __restrict__ nd_c,
                            float4* __restrict__ nd_v, int8_t* __restrict__ nd_type, int8_t* __restrict__ nd_sc,
                            float* __restrict__ nd_curv, float* __restrict__ nd_samp, int qef, int curv_known,
