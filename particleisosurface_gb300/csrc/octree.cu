@@ -542,7 +542,7 @@ __global__ void k_spawn(long long lb, long long le, long long cbase, const int* 
 // would compute them (checkEmptyAndCalcCurv, src/surface_reconstructor.cpp:
 // 152-222).  One warp per parent; lane k writes child k.
 template <bool CURV>
-__global__ void __launch_bounds__(32 * kSpawnWarps, 16) k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict__ rank,
+__global__ void __launch_bounds__(32 * kSpawnWarps, CURV ? 16 : 24) k_spawn_scan(LevelArgs a, long long cbase, const int* __restrict__ rank,
                                                     int child_depth, float4* __restrict__ nd_c,
                                                     float4* __restrict__ nd_v, uint64_t* __restrict__ nd_id,
                                                     int* __restrict__ nd_parent, int* __restrict__ nd_child,
