@@ -51,7 +51,7 @@ ORACLE_PAIRS = 7205138892
 # dram__bytes_read.sum + dram__bytes_write.sum of the field-evaluation launches
 # of one 1M-particle frame (k_q_eval_thread x2, k_q_eval), one ncu capture;
 # see profiles/k_q_eval_dam_break.md
-FIELD_DRAM_BYTES_PER_FRAME = 373258752
+FIELD_DRAM_BYTES_PER_FRAME = 380755200
 
 
 def parse():
