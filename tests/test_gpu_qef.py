@@ -106,3 +106,50 @@ def test_qef_mesh_topology(pair):
     assert len(v) > 0 and t.min() >= 0 and t.max() < len(v)
     # moved leaves change values near the surface; the mesh stays close
     assert rep["verts_only_oracle"] + rep["verts_only_gpu"] <= max(8, rep["verts_oracle"] // 50)
+
+
+@pytest.fixture(scope="module")
+def stress():
+    """The precision-stress geometry (thin sheets on planes and saddles,
+    Bezier filaments): near-degenerate neighbourhoods and ill-conditioned
+    QEFs.  No oracle run is needed: the check is against the FP64 solve of
+    the frame's own samples."""
+    B.build()
+    fr = synth.sheets_and_filaments(n=20000, seed=9)
+    ctx = N.Context(0)
+    g = N.Frame(ctx, N.default_params(fr.radius, qef=True)).upload(fr.xyz).run()
+    yield fr, g
+    g.close()
+    ctx.close()
+
+
+def test_qef_vertices_match_fp64_solve_on_thin_sheets(stress):
+    """Accepted QEF vertices within QEF_VERT_TOL * r of the FP64 NumPy solve of
+    the same 27 samples, and the accept/reject decision the same, on the
+    geometry where the normal matrices are worst conditioned."""
+    fr, g = stress
+    nodes = g.dump(N.DUMP_NODES)
+    samp = g.dump(N.DUMP_QEF_SAMPLES)
+    leaves = np.nonzero(nodes["type"] == 2)[0]
+    rng = np.random.default_rng(1)
+    pick = rng.choice(leaves, size=min(20000, len(leaves)), replace=False)
+    errs, disagree, singular = [], 0, 0
+    for i in pick:
+        x, in_cell, sing, err = PR.qef_solve_f64(nodes["center"][i], nodes["half"][i], samp[i])
+        singular += sing
+        acc = in_cell and not sing
+        moved = not np.array_equal(nodes["node"][i][:3], nodes["center"][i])
+        if acc != moved:
+            disagree += 1
+            continue
+        if acc:
+            errs.append(np.abs(nodes["node"][i][:3] - x[:3]).max() / fr.radius)
+    errs = np.array(errs) if errs else np.zeros(1)
+    info = g.info()
+    print("thin sheets, QEF vs FP64: accepted %d of %d sampled leaves (singular %d), max %.3e rms %.3e (x r); "
+          "acceptance differs %d; frame accepted %d singular %d"
+          % (len(errs), len(pick), singular, errs.max(), np.sqrt(np.mean(errs ** 2)), disagree,
+             info["qef_accepted"], info["qef_singular"]))
+    assert len(errs) > 20
+    assert errs.max() <= PR.QEF_VERT_TOL
+    assert disagree <= max(2, len(pick) // 1000)
