@@ -60,7 +60,7 @@ __device__ __forceinline__ void grad_sum(const GridView& g, const PartView& P, f
   gz = az.s;
 }
 
-__global__ void k_normals(GridView g, PartView P, long long n, float gscale, float4* __restrict__ nrm) {
+__global__ void __launch_bounds__(128, 12) k_normals(GridView g, PartView P, long long n, float gscale, float4* __restrict__ nrm) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   float4 p = P.pos[t];
