@@ -41,7 +41,7 @@ struct GridRuns {
   int dims[3];
 };
 
-__global__ void __launch_bounds__(32 * kGridWarps, 2) k_grid_eval(GridView g, PartView P, float iso, GridRuns R,
+__global__ void __launch_bounds__(32 * kGridWarps, 3) k_grid_eval(GridView g, PartView P, float iso, GridRuns R,
                                                                  float* __restrict__ out,
                                                                  unsigned long long* __restrict__ counters) {
   __shared__ float4 s_x[kGridWarps][kCandBuf], s_a[kGridWarps][kCandBuf], s_b[kGridWarps][kCandBuf],
