@@ -312,7 +312,7 @@ __global__ void k_q_chunks(long long nb, const int* __restrict__ ucnt, int chunk
 // candidates against the chunk's bounding box, stages the survivors in
 // shared memory and sums in candidate order.
 template <int K>
-__global__ void __launch_bounds__(32 * kEvalWarps, (K > 2 ? 2 : 4)) k_q_eval(QArgs a, const int* __restrict__ order,
+__global__ void __launch_bounds__(32 * kEvalWarps, (K > 2 ? 3 : 4)) k_q_eval(QArgs a, const int* __restrict__ order,
                                                             const int* __restrict__ qoff,
                                                             const int* __restrict__ ucnt,
                                                             const int2* __restrict__ chunks,
