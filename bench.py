@@ -49,8 +49,8 @@ FLOPS_PER_PAIR = 38
 ORACLE_FIELD_EVALS = 147191991
 ORACLE_PAIRS = 7205138892
 # dram__bytes_read.sum + dram__bytes_write.sum of the field-evaluation launches
-# of one 1M-particle frame (k_q_eval_thread x2, k_q_eval), one ncu capture;
-# see profiles/k_q_eval_dam_break.md
+# of one 1M-particle frame (k_q_eval_thread x2, k_q_eval), one ncu capture
+# (--metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:k_q_eval -c 3)
 FIELD_DRAM_BYTES_PER_FRAME = 380755200
 
 
@@ -676,8 +676,8 @@ def ours(a):
                                 "bound": "fp32",
                                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                                 "traffic": FIELD_DRAM_BYTES_PER_FRAME if fr.n == 1_000_000 else None,
-                                "traffic_per": "frame (the same launches), ncu capture in "
-                                               "profiles/k_q_eval_dam_break.md",
+                                "traffic_per": "frame (the same launches), one ncu capture of "
+                                               "dram__bytes_read.sum + dram__bytes_write.sum",
                                 "peak_source": "measured in this run: cuBLAS FP32 GEMM 8192^3, TF32 off, best of 5 "
                                                "(MEASURED_PEAKS.json has HBM and bf16 figures only)",
                                 "nominal_fp32_peak": nominal, "frac_of_nominal": achieved / nominal,
