@@ -234,12 +234,20 @@ int pi_reconstruct(pi_ctx* ctx, const pi_params* params, const float* xyz, int64
  * image, held on every GPU that loads the library until exit; so at most
  * PI_NOALLOC_MAX_PARTICLES particles and PI_NOALLOC_MAX_CELLS hash cells
  * (PI_ERR_LIMIT beyond them; also PI_ERR_LIMIT, with *cell_num_out set, when
- * cell_offsets_len < cell count + 1).  The first call on a device looks up
- * the array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  All calls on a device
- * share the array: calls whose GPU work may overlap (unordered streams) race
- * and must be serialised by the caller.  Work runs on `stream` (a
- * cudaStream_t, 0 for the default stream) and is complete on return. */
+ * cell_offsets_len < cell count + 1; a radius so small that a hash-grid axis
+ * would exceed the cell limit is rejected the same way, *cell_num_out = -1).
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current, and with CUDA's default
+ * lazy module loading it is also the call that loads the library's device
+ * code and the array onto that device, which takes device memory once.  So
+ * make one warm-up call per device during the caller's initialisation, before
+ * it reserves its memory pool or stops allowing allocation, and before any
+ * stream capture; later calls allocate nothing.  The looked-up address is
+ * kept for the life of the process: cudaDeviceReset on a device while this
+ * library is loaded is not supported.  All calls on a device share the
+ * array: calls whose GPU work may overlap (unordered streams) race and must
+ * be serialised by the caller.  Work runs on `stream` (a cudaStream_t, 0 for
+ * the default stream) and is complete on return. */
 #define PI_NOALLOC_MAX_PARTICLES 1048576
 #define PI_NOALLOC_MAX_CELLS 16777216
 int pi_hashgrid_build_noalloc(const float* d_xyz, int64_t n, float radius, int32_t* d_keys,

@@ -425,7 +425,7 @@ int pi_ctx_destroy(pi_ctx* c) {
 int pi_ctx_stats(const pi_ctx* c, uint64_t* launches, uint64_t* bytes) {
   PI_API_BEGIN
   PI_CHECK(c, "ctx is null");
-  if (launches) *launches = g_launches;
+  if (launches) *launches = g_launches.load(std::memory_order_relaxed);
   if (bytes) *bytes = (uint64_t)c->used.load();
   PI_API_END
 }

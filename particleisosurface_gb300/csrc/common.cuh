@@ -3,14 +3,19 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cstdio>
 #include <stdexcept>
 #include <string>
 
 namespace pisurf {
 
-// Library-wide count of kernel launches (read by pi_ctx_stats).
-extern unsigned long long g_launches;
+// Library-wide count of kernel launches (read by pi_ctx_stats).  Launches
+// come from many host threads at once (the request loop's workers, one
+// caller thread per frame), so the count is atomic; relaxed order suffices
+// for a statistic.
+extern std::atomic<unsigned long long> g_launches;
+inline void count_launch() { g_launches.fetch_add(1ull, std::memory_order_relaxed); }
 
 struct CudaError : std::runtime_error {
   int code;
@@ -36,7 +41,7 @@ struct CudaError : std::runtime_error {
   do {                                                                    \
     if ((grid) > 0) {                                                     \
       kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__);         \
-      ::pisurf::g_launches++;                                             \
+      ::pisurf::count_launch();                                           \
       PI_CUDA(cudaGetLastError());                                        \
     }                                                                     \
   } while (0)

@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstring>
 #include <stdexcept>
+#include <string>
 
 #include "device.cuh"
 #include "internal.h"
@@ -134,6 +135,25 @@ void stage_upload_device(pi_frame* f, const float* d_xyz, long long n) {
   PI_CUDA(cudaMemcpyAsync(f->xyz.p, d_xyz, sizeof(float) * 3 * n, cudaMemcpyDeviceToDevice, s));
 }
 
+long long grid_cell_counts(const float bounding[6], float cell, long long max_cells, int nn[3]) {
+  double total = 1.0;
+  for (int i = 0; i < 3; ++i) {
+    // XYZCellNum (src/hash_grid.cpp:24-27): ceil of a float quotient; a
+    // tiny radius makes it too large for an int, so it is checked as a float
+    // (NaN and infinity fail the test too) before the conversion
+    const float q = std::ceil((bounding[i * 2 + 1] - bounding[i * 2]) / cell);
+    if (!(q <= (float)max_cells))
+      throw std::length_error("hash grid axis of " + std::to_string(q) + " cells exceeds the limit of " +
+                              std::to_string(max_cells) + " cells (radius too small for the particle box)");
+    nn[i] = std::max(int(q), 1);
+    total *= nn[i];
+  }
+  if (total > (double)max_cells)
+    throw std::length_error("hash grid of " + std::to_string((long long)total) + " cells exceeds the limit of " +
+                            std::to_string(max_cells) + " cells");
+  return (long long)nn[0] * nn[1] * nn[2];
+}
+
 static int bits_for(long long v) {
   int b = 0;
   while (b < 63 && (1LL << b) <= v) ++b;
@@ -166,12 +186,9 @@ void stage_hashgrid(pi_frame* f) {
     g.bounding[i * 2 + 1] = center + length / 2;
   }
   int nn[3];
-  for (int i = 0; i < 3; ++i)
-    nn[i] = std::max(int(std::ceil((g.bounding[i * 2 + 1] - g.bounding[i * 2]) / cell)), 1);
-  g.nx = nn[0], g.ny = nn[1], g.nz = nn[2];
-  g.cellNum = (long long)g.nx * g.ny * g.nz;
   // FindStartEnd stores keys in an int (src/hash_grid.cpp:105).
-  if (g.cellNum >= (1LL << 31) - 1) throw std::length_error("hash grid has >= 2^31 cells");
+  g.cellNum = grid_cell_counts(g.bounding, cell, (1LL << 31) - 2, nn);
+  g.nx = nn[0], g.ny = nn[1], g.nz = nn[2];
   g.bits = bits_for(g.cellNum + 1);
   f->key.alloc(f->ctx, s, n);
   f->skey.alloc(f->ctx, s, n);

@@ -173,6 +173,12 @@ void frame_clear(pi_frame* f, int stage);
 // counter snapshot into the frame.
 void resolve_pending(pi_frame* f);
 
+// Hash cells per axis of the grid over `bounding` (HashGrid::XYZCellNum,
+// src/hash_grid.cpp:24-27) into nn; returns their product.  Throws
+// std::length_error, before any int conversion could overflow, when an axis
+// or the product exceeds max_cells.
+long long grid_cell_counts(const float bounding[6], float cell, long long max_cells, int nn[3]);
+
 void stage_upload_host(pi_frame* f, const float* xyz, long long n);
 void stage_upload_device(pi_frame* f, const float* d_xyz, long long n);
 void stage_hashgrid(pi_frame* f);

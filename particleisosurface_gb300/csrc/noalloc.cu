@@ -122,16 +122,17 @@ extern "C" int pi_hashgrid_build_noalloc(const float* d_xyz, int64_t n, float ra
       bounding[i * 2] = center - length / 2;
       bounding[i * 2 + 1] = center + length / 2;
     }
-    int nn[3];
-    for (int i = 0; i < 3; ++i)
-      nn[i] = std::max(int(std::ceil((bounding[i * 2 + 1] - bounding[i * 2]) / cell)), 1);
-    const long long cellNum = (long long)nn[0] * nn[1] * nn[2];
     for (int k = 0; k < 6; ++k) bounding_out6[k] = bounding[k];
+    int nn[3];
+    long long cellNum = 0;
+    try {
+      cellNum = grid_cell_counts(bounding, cell, kMaxCells, nn);
+    } catch (const std::length_error& e) {
+      *cell_num_out = -1;
+      throw std::length_error(std::string("pi_hashgrid_build_noalloc: ") + e.what());
+    }
     for (int k = 0; k < 3; ++k) xyz_cell_num_out3[k] = nn[k];
     *cell_num_out = cellNum;
-    if (cellNum > kMaxCells)
-      throw std::length_error("pi_hashgrid_build_noalloc: " + std::to_string(cellNum) +
-                              " hash cells exceed the limit of " + std::to_string(kMaxCells));
     if (cell_offsets_len < cellNum + 1)
       throw std::length_error("pi_hashgrid_build_noalloc: cell offset buffer needs " +
                               std::to_string(cellNum + 1) + " entries");

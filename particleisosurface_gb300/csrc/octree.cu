@@ -1014,7 +1014,7 @@ void stage_octree(pi_frame* f) {
     void* args[] = {&ta};
     PI_CUDA(cudaLaunchCooperativeKernel((const void*)k_top_levels, dim3(ctx->coop_blocks), dim3(kTopThreads), args,
                                         0, s));
-    ++g_launches;
+    count_launch();
     int* const dh = reinterpret_cast<int*>(lvh + kPinTopWords - 1);
     PI_CUDA(cudaMemcpyAsync(lvh, lvd.p, sizeof(long long) * (dstop + 2), cudaMemcpyDeviceToHost, s));
     PI_CUDA(cudaMemcpyAsync(dh, dout.p, sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -14,7 +14,7 @@
 
 namespace pisurf {
 
-unsigned long long g_launches = 0;
+std::atomic<unsigned long long> g_launches{0};
 
 static constexpr int kThreads = 256;
 static constexpr int kItems = 8;

@@ -1,7 +1,8 @@
 """Generates the committed golden fixtures from the mounted reference.
 
-Run in the build container, where the reference sources are readable:
-    python tests/golden/make_golden.py
+Run where the reference sources are readable, naming their root:
+    python tests/golden/make_golden.py <reference root>
+(or with the root in the environment variable PI_REFERENCE).
 Writes tests/golden/dmc_table.json: a SHA-256 digest of the reference's
 dual-marching-cubes canonicalisation table (include/visitorextract.h:35-293)
 and of its per-case triangle lists (src/visitorextract.cpp:95-199), so tests
@@ -15,7 +16,7 @@ import os
 import re
 import sys
 
-REF = os.environ.get("PI_REFERENCE", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PI_REFERENCE", "")
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -49,8 +50,8 @@ def parse_reference():
 
 
 def main():
-    if not os.path.isdir(REF):
-        sys.exit("reference not mounted at %s" % REF)
+    if not REF or not os.path.isdir(REF):
+        sys.exit("usage: make_golden.py <reference root> (or set PI_REFERENCE); got %r" % REF)
     table, cases = parse_reference()
     assert all(t is not None for t in table)
     out = {

@@ -108,6 +108,22 @@ def test_non_finite_coordinate_rejected(ctx):
     f.close()
 
 
+def test_tiny_radius_rejected_before_keys(ctx):
+    """A radius so small that a hash-grid axis would hold more cells than an
+    int counts (the reference's int(ceil(...)) would overflow) is a size
+    limit, reported before any key is computed; the context stays usable."""
+    xyz = np.zeros((100, 3), np.float32)
+    xyz[:, 0] = np.arange(100) * 0.02
+    f = N.Frame(ctx, N.default_params(1e-20)).upload(xyz)
+    with pytest.raises(N.PiError) as e:
+        f.hashgrid()
+    assert e.value.code == N.PI_ERR_LIMIT
+    f.close()
+    f = N.Frame(ctx, N.default_params(0.01)).upload(xyz).run()
+    assert f.info()["num_nodes"] > 0
+    f.close()
+
+
 def test_zero_particles_rejected(ctx):
     f = N.Frame(ctx, N.default_params(0.01))
     with pytest.raises(N.PiError) as e:

@@ -34,7 +34,7 @@ def test_noalloc_hashgrid_matches_allocating_build_twice():
     fn = _noalloc_fn()
     ctx = N.Context(0)
     frames = [synth.small_blob(n=4000, seed=31), synth.slab_and_sphere(n=9000, seed=32)]
-    for fr in frames:
+    for k, fr in enumerate(frames):
         ref = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz).hashgrid()
         keys_ref = ref.dump(N.DUMP_KEYS)
         il_ref = ref.dump(N.DUMP_INDEX_LIST)
@@ -50,10 +50,16 @@ def test_noalloc_hashgrid_matches_allocating_build_twice():
         xyz_n = (C.c_int32 * 3)()
         cn = C.c_int64()
         torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         rc = fn(d_xyz.data_ptr(), n, fr.radius, d_keys.data_ptr(), d_il.data_ptr(), d_off.data_ptr(),
                 len(off_ref), bnd, xyz_n, C.byref(cn), None)
         assert rc == 0, N.lib().pi_last_error()
         torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info()[0]
+        if k > 0:
+            # the first call was the warm-up (it may load the library's device
+            # code); every later call leaves the device's free memory as it was
+            assert free_after == free_before, (free_before, free_after)
         np.testing.assert_array_equal(np.array(bnd[:], np.float32), np.array(info["bounding"], np.float32))
         assert list(xyz_n) == list(info["xyz_cell_num"]) and cn.value == info["cell_num"]
         np.testing.assert_array_equal(d_keys.cpu().numpy().astype(np.int64), keys_ref)
@@ -83,4 +89,9 @@ def test_noalloc_rejects_sizes_beyond_limit():
     rc = fn(d_xyz.data_ptr(), fr.n, fr.radius, d_keys.data_ptr(), d_il.data_ptr(), d_off.data_ptr(), 16, bnd,
             xyz_n, C.byref(cn), None)
     assert rc == -5 and cn.value + 1 > 16
+    # a radius so small that an axis of the hash grid would hold more cells
+    # than an int can count: rejected before any key is computed
+    rc = fn(d_xyz.data_ptr(), fr.n, 1e-20, d_keys.data_ptr(), d_il.data_ptr(), d_off.data_ptr(), 16, bnd,
+            xyz_n, C.byref(cn), None)
+    assert rc == -5 and b"exceeds the limit" in N.lib().pi_last_error() and cn.value == -1
     torch.cuda.synchronize()
