@@ -61,8 +61,11 @@ typedef struct pi_frame_info {
   float iso_value, max_scalar, influence2, sigma;
   int64_t num_nodes, num_leaves, num_empty;
   int64_t num_dual_cells, num_vertices, num_triangles;
-  int64_t field_evals;      /* SingleEval-equivalents: node samples, leaf values, bisection */
-  int64_t candidate_pairs;  /* particle candidates visited by those evaluations */
+  int64_t field_evals;      /* reference-equivalent evaluations: the SingleEval calls the
+                               reference makes for this frame's octree (27 lattice samples
+                               per sampled node, the leaf values, QEF vertices), plus one
+                               bisection chain per mesh vertex */
+  int64_t candidate_pairs;  /* particle candidates visited by the evaluations performed */
   int64_t bisection_evals;
   int64_t fp64_eigen;       /* particles whose eigen-decomposition ran in FP64 */
   float stage_ms[8];        /* device time of upload, hash, aniso, normals, octree, qef,
@@ -73,6 +76,9 @@ typedef struct pi_frame_info {
                                vertex is rejected, as the reference's non-finite
                                inverse is */
   int64_t grid_pairs;       /* candidate pairs of the last uniform-grid sampling */
+  int64_t field_evals_performed; /* evaluations the kernels performed: distinct sample
+                                    points (shared lattice points once), leaf values,
+                                    QEF vertices, bisection midpoints */
 } pi_frame_info;
 
 /* Parity dumps (pi_stage_dump).  Arrays are in original particle order unless
@@ -115,8 +121,18 @@ int pi_ctx_stats(const pi_ctx* ctx, uint64_t* launches, uint64_t* bytes);
  * bracketed with CUDA events on the context stream.  Read and reset with
  * pi_ctx_kernel_time. */
 int pi_ctx_profile(pi_ctx* ctx, int enable);
+/* field evaluation at octree samples: the chunked (k_q_eval), per-sample
+ * (k_q_eval_thread) and leaf-value (k_leaf_level) kernels together; evals =
+ * the evaluations they performed */
 int pi_ctx_kernel_time(pi_ctx* ctx, double* total_ms, int64_t* launches, int64_t* pairs,
                        int64_t* evals);
+/* The same per kernel group, arrays of ngroups entries: 0 chunked sampling
+ * (k_q_eval), 1 per-sample sampling (k_q_eval_thread), 2 leaf values
+ * (k_leaf_level), 3 edge bisection (k_bisect), 4 FP64 QEF (k_qef; units =
+ * leaves solved), 5 uniform grid (k_grid_eval).  Reads and resets. */
+#define PI_PROF_GROUPS 6
+int pi_ctx_kernel_groups(pi_ctx* ctx, int32_t ngroups, double* ms, int64_t* launches, int64_t* pairs,
+                         int64_t* units);
 /* Samples per lane of the chunked field evaluation at the two finest
  * octree levels (a warp evaluates chunks of 32 x that many samples sharing a
  * candidate list).  By default each context times 1, 2 and 4 on its first
@@ -163,6 +179,25 @@ int pi_mesh_write_obj(pi_frame* f, const char* path);
 /* Evaluator::SingleEval / SingleEvalWithGrad (src/evaluator.cpp:60-125) at m
  * host points; grad may be null.  Needs pi_normals_compute. */
 int pi_eval_field(pi_frame* f, const float* pts, int64_t m, float* scalar, float* grad);
+
+/* FP64 oracle on the GPU.  No counterpart in the reference, whose arithmetic
+ * is float: the reference's formulas for the smoothed centres and anisotropy
+ * matrices (compute_xMeans, compute_G_Yus, src/evaluator.cpp:465-512,585-654)
+ * and for SingleEval / SingleEvalWithGrad (:60-125) evaluated in double, one
+ * thread per particle or point over the whole 27-cell candidate list of the
+ * frame's hash grid (no support culling, no deduplication, plain sums).  It
+ * is the arbiter of the FP32 path's error reports (field, G and determinant
+ * errors) and takes no part in the reconstruction.  Needs pi_hashgrid_build;
+ * the per-particle state (104 bytes a particle) is computed on the first
+ * call after the hash grid and kept with the frame.
+ * pi_fp64_aniso: centres xmeans3[N*3], G g9[N*9] (row major), det[N], original
+ * particle order; any output may be null.
+ * pi_fp64_eval_field: field (and, when grad is not null, the normal-form
+ * gradient of SingleEvalWithGrad) at m host points.
+ * pi_fp64_scalars: iso value, MaxScalar, Influnce2, Sigma in double. */
+int pi_fp64_aniso(pi_frame* f, double* xmeans3, double* g9, double* det);
+int pi_fp64_eval_field(pi_frame* f, const float* pts, int64_t m, double* scalar, double* grad);
+int pi_fp64_scalars(const pi_frame* f, double* out4);
 
 /* HashGrid::GetPIdxList (src/hash_grid.cpp:196-214) for m host points:
  * offsets[m+1] and the concatenated particle indices; *total receives the

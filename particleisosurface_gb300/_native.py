@@ -43,7 +43,7 @@ class FrameInfo(C.Structure):
                 ("num_vertices", C.c_int64), ("num_triangles", C.c_int64), ("field_evals", C.c_int64),
                 ("candidate_pairs", C.c_int64), ("bisection_evals", C.c_int64), ("fp64_eigen", C.c_int64),
                 ("stage_ms", C.c_float * 8), ("qef_accepted", C.c_int64), ("qef_singular", C.c_int64),
-                ("grid_pairs", C.c_int64)]
+                ("grid_pairs", C.c_int64), ("field_evals_performed", C.c_int64)]
 
     def as_dict(self):
         out = {}
@@ -76,6 +76,7 @@ def _declare(L):
         "pi_ctx_stats": (C.c_int, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
         "pi_ctx_profile": (C.c_int, [P, C.c_int]),
         "pi_ctx_kernel_time": (C.c_int, [P, C.POINTER(C.c_double), pi64, pi64, pi64]),
+        "pi_ctx_kernel_groups": (C.c_int, [P, C.c_int32, C.POINTER(C.c_double), pi64, pi64, pi64]),
         "pi_ctx_stream": (P, [P]),
         "pi_ctx_tune": (C.c_int, [P, C.c_int32]),
         "pi_ctx_tuning": (C.c_int, [P, C.POINTER(C.c_int32)]),
@@ -95,6 +96,9 @@ def _declare(L):
         "pi_mesh_get": (C.c_int, [P, fp, C.POINTER(C.c_int32), C.POINTER(C.c_uint64)]),
         "pi_mesh_write_obj": (C.c_int, [P, C.c_char_p]),
         "pi_eval_field": (C.c_int, [P, fp, i64, fp, fp]),
+        "pi_fp64_aniso": (C.c_int, [P, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "pi_fp64_eval_field": (C.c_int, [P, fp, i64, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "pi_fp64_scalars": (C.c_int, [P, C.POINTER(C.c_double)]),
         "pi_grid_dims": (C.c_int, [P, C.POINTER(C.c_int32), fp, pi64]),
         "pi_load_csv": (C.c_int, [C.c_char_p, fp, fp, i64, pi64, C.POINTER(C.c_int32)]),
         "pi_write_ply": (C.c_int, [C.c_char_p, fp, i64, C.POINTER(C.c_int32), i64, C.c_int32]),
@@ -221,6 +225,17 @@ class Context:
         check(lib().pi_ctx_kernel_time(self.h, C.byref(ms), C.byref(n), C.byref(p), C.byref(e)))
         return dict(ms=ms.value, launches=n.value, pairs=p.value, evals=e.value)
 
+    GROUPS = ("chunked_sampling", "per_sample_sampling", "leaf_values", "bisection", "qef", "uniform_grid")
+
+    def kernel_groups(self):
+        """Per kernel group (GROUPS order): dict of ms, launches, pairs, units
+        accumulated since the last read (pi_ctx_kernel_groups)."""
+        n = len(self.GROUPS)
+        ms = (C.c_double * n)()
+        la, pa, un = (C.c_int64 * n)(), (C.c_int64 * n)(), (C.c_int64 * n)()
+        check(lib().pi_ctx_kernel_groups(self.h, n, ms, la, pa, un))
+        return {g: dict(ms=ms[k], launches=la[k], pairs=pa[k], units=un[k]) for k, g in enumerate(self.GROUPS)}
+
     def reconstruct(self, xyz, params, max_verts=None, max_tris=None):
         """Host in / host out: pi_reconstruct."""
         xyz = np.ascontiguousarray(xyz, dtype=np.float32)
@@ -328,6 +343,30 @@ class Frame:
         check(lib().pi_eval_field(self.h, ptr(pts, C.c_float), m, ptr(s, C.c_float),
                                   ptr(g, C.c_float) if grad else None))
         return (s, g) if grad else s
+
+    def eval_fp64(self, pts, grad=False):
+        """FP64 oracle (pi_fp64_eval_field): SingleEval in double at pts."""
+        pts = np.ascontiguousarray(pts, dtype=np.float32)
+        m = pts.shape[0]
+        s = np.empty(m, np.float64)
+        g = np.empty((m, 3), np.float64) if grad else None
+        check(lib().pi_fp64_eval_field(self.h, ptr(pts, C.c_float), m, ptr(s, C.c_double),
+                                       ptr(g, C.c_double) if grad else None))
+        return (s, g) if grad else s
+
+    def aniso_fp64(self):
+        """FP64 oracle (pi_fp64_aniso): centres [n, 3], G [n, 3, 3], det [n], original order."""
+        n = self.n
+        xm = np.empty((n, 3), np.float64)
+        g = np.empty((n, 3, 3), np.float64)
+        d = np.empty(n, np.float64)
+        check(lib().pi_fp64_aniso(self.h, ptr(xm, C.c_double), ptr(g, C.c_double), ptr(d, C.c_double)))
+        return xm, g, d
+
+    def scalars_fp64(self):
+        o = np.empty(4, np.float64)
+        check(lib().pi_fp64_scalars(self.h, ptr(o, C.c_double)))
+        return dict(iso=o[0], max_scalar=o[1], influence2=o[2], sigma=o[3])
 
     def grid_dims(self):
         """UniformGrid lattice: dims (x, y, z), box (min/max per axis), point count."""

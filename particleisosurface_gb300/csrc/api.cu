@@ -113,13 +113,13 @@ void counters_reset(pi_frame* f) {
   PI_CUDA(cudaMemsetAsync(f->dcount.p, 0, sizeof(unsigned long long) * kCounterWords, s));
 }
 
-void counters_read(pi_frame* f, unsigned long long out[8]) {
+void counters_read(pi_frame* f, unsigned long long out[kCounters]) {
   cudaStream_t s = f->ctx->stream;
   std::vector<unsigned long long> h(kCounterWords);
   PI_CUDA(cudaMemcpyAsync(h.data(), f->dcount.p, sizeof(unsigned long long) * kCounterWords,
                           cudaMemcpyDeviceToHost, s));
   PI_CUDA(cudaStreamSynchronize(s));
-  for (int w = 0; w < 8; ++w) {
+  for (int w = 0; w < kCounters; ++w) {
     out[w] = 0;
     for (int k = 0; k < kStripes; ++k) out[w] += h[((size_t)w * kStripes + k) * 4];
   }
@@ -131,8 +131,8 @@ void counters_snapshot(pi_frame* f, int slot) {
   f->pin_pending |= 1 << slot;
 }
 
-static void fold_counters(const unsigned long long* h, unsigned long long out[8]) {
-  for (int w = 0; w < 8; ++w) {
+static void fold_counters(const unsigned long long* h, unsigned long long out[kCounters]) {
+  for (int w = 0; w < kCounters; ++w) {
     out[w] = 0;
     for (int k = 0; k < kStripes; ++k) out[w] += h[((size_t)w * kStripes + k) * 4];
   }
@@ -149,28 +149,40 @@ void resolve_pending(pi_frame* f) {
     }
   f->ev_pending = 0;
   const unsigned long long* h = f->ctx->hpin;
-  unsigned long long c[8];
+  unsigned long long c[kCounters];
+  pi_ctx* ctx = f->ctx;
   if (f->pin_pending & (1 << kPinAniso)) {
     fold_counters(h + (size_t)kPinAniso * kCounterWords, c);
     f->fp64Count = (long long)c[0];
   }
   if (f->pin_pending & (1 << kPinOctree)) {
     fold_counters(h + (size_t)kPinOctree * kCounterWords, c);
-    f->fieldEvals = (long long)c[0] + (long long)c[7];
-    f->pairs = (long long)c[1];
-    f->qefAccepted = (long long)c[5];
-    f->qefSingular = (long long)c[6];
-    if (f->ctx->profile) {
-      f->ctx->kernel_pairs += f->pairs;
-      f->ctx->kernel_evals += f->fieldEvals;
+    f->fieldEvals = (long long)(c[C_REF_EVALS] + c[C_QEF_EVALS]);
+    f->doneEvals = (long long)(c[C_DONE_CHUNK] + c[C_DONE_THREAD] + c[C_DONE_LEAF] + c[C_QEF_EVALS]);
+    f->pairs = (long long)c[C_SAMPLE_PAIRS];
+    f->qefAccepted = (long long)c[C_QEF_ACCEPTED];
+    f->qefSingular = (long long)c[C_QEF_SINGULAR];
+    if (ctx->profile) {
+      ctx->group_pairs[PG_CHUNK] += (int64_t)c[C_PAIRS_CHUNK];
+      ctx->group_pairs[PG_THREAD] += (int64_t)c[C_PAIRS_THREAD];
+      ctx->group_pairs[PG_LEAF] += (int64_t)c[C_PAIRS_LEAF];
+      ctx->group_units[PG_CHUNK] += (int64_t)c[C_DONE_CHUNK];
+      ctx->group_units[PG_THREAD] += (int64_t)c[C_DONE_THREAD];
+      ctx->group_units[PG_LEAF] += (int64_t)c[C_DONE_LEAF];
+      ctx->group_units[PG_QEF] += (int64_t)c[C_QEF_LEAVES];
     }
   }
   if (f->pin_pending & (1 << kPinExtract)) {
     fold_counters(h + (size_t)kPinExtract * kCounterWords, c);
-    f->nDual = (long long)c[2];
-    f->bisectEvals = (long long)c[3];
-    f->fieldEvals += (long long)c[3];
-    f->pairs += (long long)c[4];
+    f->nDual = (long long)c[C_DUAL];
+    f->bisectEvals = (long long)c[C_BISECT_EVALS];
+    f->fieldEvals += (long long)c[C_BISECT_EVALS];
+    f->doneEvals += (long long)c[C_BISECT_EVALS];
+    f->pairs += (long long)c[C_BISECT_PAIRS];
+    if (ctx->profile) {
+      ctx->group_pairs[PG_BISECT] += (int64_t)c[C_BISECT_PAIRS];
+      ctx->group_units[PG_BISECT] += (int64_t)c[C_BISECT_EVALS];
+    }
   }
   if (f->pin_pending & (1 << kPinValid)) {
     const int valid = *reinterpret_cast<const int*>(h + (size_t)kPinSlots * kCounterWords);
@@ -179,20 +191,34 @@ void resolve_pending(pi_frame* f) {
   f->pin_pending = 0;
 }
 
-void prof_begin(pi_ctx* c, cudaStream_t s) {
+void prof_begin(pi_ctx* c, cudaStream_t s, int g) {
   if (!c->profile) return;
   cudaEvent_t e;
   PI_CUDA(cudaEventCreate(&e));
   PI_CUDA(cudaEventRecord(e, s));
-  c->prof_events.push_back(e);
+  c->prof_events[g].push_back(e);
 }
-void prof_end(pi_ctx* c, cudaStream_t s, long long, long long) {
+void prof_end(pi_ctx* c, cudaStream_t s, int g) {
   if (!c->profile) return;
   cudaEvent_t e;
   PI_CUDA(cudaEventCreate(&e));
   PI_CUDA(cudaEventRecord(e, s));
-  c->prof_events.push_back(e);
-  c->kernel_launches++;
+  c->prof_events[g].push_back(e);
+  c->group_launches[g]++;
+}
+
+// Reads every pending event pair into the group times.
+static void prof_collect(pi_ctx* c) {
+  for (int g = 0; g < kProfGroups; ++g) {
+    auto& ev = c->prof_events[g];
+    for (size_t i = 0; i + 1 < ev.size(); i += 2) {
+      float t = 0;
+      PI_CUDA(cudaEventElapsedTime(&t, ev[i], ev[i + 1]));
+      c->group_ms[g] += t;
+    }
+    for (auto e : ev) cudaEventDestroy(e);
+    ev.clear();
+  }
 }
 
 // resizeRootBoxConstR (src/surface_reconstructor.cpp:97-122),
@@ -289,8 +315,10 @@ void check_params(const pi_params* p) {
 // result and counter cleared; device buffers are kept for reuse.
 void frame_clear(pi_frame* f, int stage) {
   f->stage = stage;
+  f->f64_ready = false;
   f->nNodes = f->nV = f->nT = f->nDual = 0;
   f->fieldEvals = f->pairs = f->bisectEvals = f->fp64Count = f->nLeaves = f->nEmpty = 0;
+  f->doneEvals = 0;
   f->qefAccepted = f->qefSingular = 0;
   f->ev_pending = f->pin_pending = 0;
   for (int k = 0; k < 8; ++k) f->stage_ms[k] = 0;
@@ -395,7 +423,8 @@ static void ctx_release(pi_ctx* c) {
   if (c->refs.fetch_sub(1) != 1) return;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
-  for (auto e : c->prof_events) cudaEventDestroy(e);
+  for (auto& ev : c->prof_events)
+    for (auto e : ev) cudaEventDestroy(e);
   if (c->hpin) cudaFreeHost(c->hpin);
   if (c->copy_stream) {
     cudaStreamSynchronize(c->copy_stream);
@@ -442,21 +471,42 @@ int pi_ctx_kernel_time(pi_ctx* c, double* total_ms, int64_t* launches, int64_t* 
   PI_CHECK(c, "ctx is null");
   set_device(c);
   PI_CUDA(cudaStreamSynchronize(c->stream));
+  prof_collect(c);
+  // field evaluation at octree samples: the chunked, per-sample and
+  // leaf-value groups together
   double ms = 0;
-  for (size_t i = 0; i + 1 < c->prof_events.size(); i += 2) {
-    float t = 0;
-    PI_CUDA(cudaEventElapsedTime(&t, c->prof_events[i], c->prof_events[i + 1]));
-    ms += t;
+  int64_t l = 0, p = 0, u = 0;
+  for (int g : {PG_CHUNK, PG_THREAD, PG_LEAF}) {
+    ms += c->group_ms[g];
+    l += c->group_launches[g];
+    p += c->group_pairs[g];
+    u += c->group_units[g];
+    c->group_ms[g] = 0;
+    c->group_launches[g] = c->group_pairs[g] = c->group_units[g] = 0;
   }
-  for (auto e : c->prof_events) cudaEventDestroy(e);
-  c->prof_events.clear();
-  c->kernel_ms += ms;
-  if (total_ms) *total_ms = c->kernel_ms;
-  if (launches) *launches = c->kernel_launches;
-  if (pairs) *pairs = c->kernel_pairs;
-  if (evals) *evals = c->kernel_evals;
-  c->kernel_ms = 0;
-  c->kernel_launches = c->kernel_pairs = c->kernel_evals = 0;
+  if (total_ms) *total_ms = ms;
+  if (launches) *launches = l;
+  if (pairs) *pairs = p;
+  if (evals) *evals = u;
+  PI_API_END
+}
+
+int pi_ctx_kernel_groups(pi_ctx* c, int32_t ngroups, double* ms, int64_t* launches, int64_t* pairs,
+                         int64_t* units) {
+  PI_API_BEGIN
+  PI_CHECK(c && ms && launches && pairs && units, "null argument");
+  PI_CHECK(ngroups >= 1 && ngroups <= kProfGroups, "ngroups out of range");
+  set_device(c);
+  PI_CUDA(cudaStreamSynchronize(c->stream));
+  prof_collect(c);
+  for (int g = 0; g < ngroups; ++g) {
+    ms[g] = c->group_ms[g];
+    launches[g] = c->group_launches[g];
+    pairs[g] = c->group_pairs[g];
+    units[g] = c->group_units[g];
+    c->group_ms[g] = 0;
+    c->group_launches[g] = c->group_pairs[g] = c->group_units[g] = 0;
+  }
   PI_API_END
 }
 
@@ -590,10 +640,12 @@ static void metrics_record(const pi_frame* f) {
   std::fprintf(fp,
                "{\"particles\": %lld, \"depth_max\": %d, \"nodes\": %lld, \"leaves\": %lld, "
                "\"dual_cells\": %lld, \"vertices\": %lld, \"triangles\": %lld, \"field_evals\": %lld, "
-               "\"candidate_pairs\": %lld, \"qef_accepted\": %lld, \"stage_ms\": {\"hash\": %.4f, "
-               "\"aniso\": %.4f, \"normals\": %.4f, \"octree\": %.4f, \"extract\": %.4f}}\n",
-               f->N, f->dmax, f->nNodes, f->nLeaves, f->nDual, f->nV, f->nT, f->fieldEvals, f->pairs,
-               f->qefAccepted, f->stage_ms[1], f->stage_ms[2], f->stage_ms[3], f->stage_ms[4], f->stage_ms[6]);
+               "\"field_evals_performed\": %lld, \"candidate_pairs\": %lld, \"qef_accepted\": %lld, "
+               "\"stage_ms\": {\"hash\": %.4f, \"aniso\": %.4f, \"normals\": %.4f, \"octree\": %.4f, "
+               "\"qef\": %.4f, \"extract\": %.4f}}\n",
+               f->N, f->dmax, f->nNodes, f->nLeaves, f->nDual, f->nV, f->nT, f->fieldEvals, f->doneEvals, f->pairs,
+               f->qefAccepted, f->stage_ms[1], f->stage_ms[2], f->stage_ms[3], f->stage_ms[4], f->stage_ms[5],
+               f->stage_ms[6]);
   std::fclose(fp);
 }
 
@@ -644,6 +696,7 @@ int pi_frame_info_get(const pi_frame* f, pi_frame_info* o) {
   o->qef_accepted = f->qefAccepted;
   o->qef_singular = f->qefSingular;
   o->grid_pairs = f->gridPairs;
+  o->field_evals_performed = f->doneEvals;
   PI_API_END
 }
 
@@ -683,6 +736,41 @@ int pi_mesh_write_obj(pi_frame* f, const char* path) {
   for (long long i = 0; i < f->nV; ++i) std::fprintf(fp, "v %f %f %f\n", v[3 * i], v[3 * i + 1], v[3 * i + 2]);
   for (long long i = 0; i < f->nT; ++i) std::fprintf(fp, "f %d %d %d\n", t[3 * i] + 1, t[3 * i + 1] + 1, t[3 * i + 2] + 1);
   std::fclose(fp);
+  PI_API_END
+}
+
+int pi_fp64_aniso(pi_frame* f, double* xmeans3, double* g9, double* det) {
+  PI_API_BEGIN
+  PI_CHECK(f, "frame is null");
+  need(f, 2);
+  set_device(f->ctx);
+  fp64_aniso_get(f, xmeans3, g9, det);
+  PI_API_END
+}
+
+int pi_fp64_eval_field(pi_frame* f, const float* pts, int64_t m, double* scalar, double* grad) {
+  PI_API_BEGIN
+  PI_CHECK(f && pts && scalar && m > 0, "bad arguments");
+  need(f, 2);
+  set_device(f->ctx);
+  cudaStream_t s = f->ctx->stream;
+  DBuf<float> dp;
+  DBuf<double> dv, dg;
+  dp.alloc(f->ctx, s, m * 3);
+  dv.alloc(f->ctx, s, m);
+  if (grad) dg.alloc(f->ctx, s, m * 3);
+  PI_CUDA(cudaMemcpyAsync(dp.p, pts, sizeof(float) * 3 * m, cudaMemcpyHostToDevice, s));
+  fp64_eval(f, dp.p, m, dv.p, grad ? dg.p : nullptr);
+  PI_CUDA(cudaMemcpyAsync(scalar, dv.p, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
+  if (grad) PI_CUDA(cudaMemcpyAsync(grad, dg.p, sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, s));
+  PI_CUDA(cudaStreamSynchronize(s));
+  PI_API_END
+}
+
+int pi_fp64_scalars(const pi_frame* f, double* out4) {
+  PI_API_BEGIN
+  PI_CHECK(f && out4, "null argument");
+  fp64_scalars(f, out4);
   PI_API_END
 }
 

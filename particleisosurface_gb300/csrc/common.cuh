@@ -48,10 +48,35 @@ struct CudaError : std::runtime_error {
 
 inline unsigned int div_up(long long a, long long b) { return (unsigned int)((a + b - 1) / b); }
 
-// Striped device event counters (see stripe_add in device.cuh): 8 counters x
-// 64 stripes, 32 bytes apart.
+// Striped device event counters (see stripe_add in device.cuh): kCounters
+// counters x 64 stripes, 32 bytes apart.
 constexpr int kStripes = 64;
-constexpr int kCounterWords = 8 * kStripes * 4;
+enum Counter : int {
+  C_REF_EVALS = 0,     // SingleEval calls the reference makes for octree samples and leaf values
+  C_SAMPLE_PAIRS = 1,  // candidate pairs of every octree sampling kernel
+  C_DUAL = 2,          // dual cells
+  C_BISECT_EVALS = 3,  // bisection midpoints evaluated (one chain per mesh vertex)
+  C_BISECT_PAIRS = 4,  // their candidate pairs
+  C_QEF_ACCEPTED = 5,
+  C_QEF_SINGULAR = 6,
+  C_QEF_EVALS = 7,     // SingleEval at accepted QEF vertices
+  C_PAIRS_CHUNK = 8,   // candidate pairs of the chunked sampling kernel (k_q_eval)
+  C_PAIRS_THREAD = 9,  // ... of the per-sample kernel (k_q_eval_thread)
+  C_PAIRS_LEAF = 10,   // ... of the leaf-value kernel (k_leaf_level)
+  C_DONE_CHUNK = 11,   // evaluations performed by k_q_eval (distinct samples)
+  C_QEF_LEAVES = 12,   // leaves whose QEF k_qef solved
+  C_DONE_THREAD = 13,  // evaluations performed by k_q_eval_thread (distinct samples)
+  C_DONE_LEAF = 14,    // evaluations performed by k_leaf_level (one per leaf)
+  kCounters = 16
+};
+constexpr int kCounterWords = kCounters * kStripes * 4;
+
+// Kernel groups timed with CUDA events when a context profiles (roofline
+// reporting): field evaluation at octree samples in chunks (k_q_eval), one
+// thread per sample (k_q_eval_thread), leaf values (k_leaf_level); edge
+// bisection (k_bisect); the FP64 QEF (k_qef); the uniform-grid sampler
+// (k_grid_eval).
+enum ProfGroup : int { PG_CHUNK = 0, PG_THREAD = 1, PG_LEAF = 2, PG_BISECT = 3, PG_QEF = 4, PG_GRID = 5, kProfGroups = 6 };
 
 // ---------------------------------------------------------------------------
 // Scan (exclusive, int32) and stable LSD radix sort (u32/u64 keys, u32

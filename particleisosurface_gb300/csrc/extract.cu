@@ -382,7 +382,7 @@ __global__ void k_dual(const uint64_t* __restrict__ verts, long long nu, int B, 
   if (code != 0 && code != 255) {
     nt = c_ntri[code];
     for (int c = 0; c < 8; ++c) cells[8 * u + c] = n8[c_trans[index][c]];
-    stripe_add(ndual, 2, 1ull);
+    stripe_add(ndual, C_DUAL, 1ull);
   }
   procs[u] = index;
   tcount[u] = nt;
@@ -515,8 +515,8 @@ __global__ void k_bisect(BisectArgs a, long long nv, const int* __restrict__ ord
   uint64_t ia = nd_id[A], ib = nd_id[B];
   vkeys[2 * v] = ia < ib ? ia : ib;
   vkeys[2 * v + 1] = ia < ib ? ib : ia;
-  stripe_add(counters, 3, (unsigned long long)steps);
-  stripe_add(counters, 4, (unsigned long long)pairs);
+  stripe_add(counters, C_BISECT_EVALS, (unsigned long long)steps);
+  stripe_add(counters, C_BISECT_PAIRS, (unsigned long long)pairs);
 }
 
 // Oriented triangle in Mesh::insert_tri argument order.
@@ -745,8 +745,10 @@ void stage_extract(pi_frame* f) {
               vcnt.p, vkey.p);
     exclusive_scan_i32(vcnt.p, vcnt.p, nc + 1, nullptr, tmp.p, s);
     PI_LAUNCH(k_vcell_place, div_up(nv, 256), 256, 0, s, nv, vkey.p, vcnt.p, vfill.p, vorder.p);
+    prof_begin(c, s, PG_BISECT);
     PI_LAUNCH(k_bisect, div_up(nv, 128), 128, 0, s, ba, nv, vorder.p, rep.p, slotA.p, slotB.p, f->nd_v.p,
               f->nd_id.p, f->mv.p, f->mk.p, f->dcount.p);
+    prof_end(c, s, PG_BISECT);
   }
   counters_snapshot(f, kPinExtract);
 }

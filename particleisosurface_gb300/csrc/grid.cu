@@ -162,6 +162,7 @@ static int bits_for(long long v) {
 
 void stage_hashgrid(pi_frame* f) {
   cudaStream_t s = f->ctx->stream;
+  f->f64_ready = false;
   const long long n = f->N;
   f->misc.alloc(f->ctx, s, 16);
   PI_LAUNCH(k_init_misc, 1, 32, 0, s, f->misc.p);

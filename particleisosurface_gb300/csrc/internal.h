@@ -51,9 +51,13 @@ struct pi_ctx {
   size_t budget = 0;
   std::atomic<long long> used{0};
   bool profile = false;
-  std::vector<cudaEvent_t> prof_events;  // pairs (start, stop)
-  double kernel_ms = 0;
-  int64_t kernel_launches = 0, kernel_pairs = 0, kernel_evals = 0;
+  // per kernel group (ProfGroup): event pairs (start, stop) not read yet, and
+  // the accumulated device time, launches, candidate pairs and work units
+  // (evaluations, or leaves for the QEF) since the last read
+  std::vector<cudaEvent_t> prof_events[pisurf::kProfGroups];
+  double group_ms[pisurf::kProfGroups] = {};
+  int64_t group_launches[pisurf::kProfGroups] = {}, group_pairs[pisurf::kProfGroups] = {},
+          group_units[pisurf::kProfGroups] = {};
   int smCount = 0;
   // one reference for the owner plus one per live frame; the context is
   // released when the last reference goes
@@ -100,6 +104,10 @@ struct pi_frame {
   pisurf::DBuf<float> gfull;     // N*9, sorted order (dumps)
   pisurf::DBuf<float> det;       // N, sorted order (dumps)
   pisurf::DBuf<int8_t> f64flag;  // N, sorted order
+  // FP64 oracle state (fp64.cu), sorted order: centres, G, det; computed on
+  // demand and invalid once the hash grid changes
+  pisurf::DBuf<double> x64, g64, det64;
+  bool f64_ready = false;
   pisurf::DBuf<int> tmp;         // scan / sort scratch
   pisurf::DBuf<uint32_t> u32a, u32b, u32c;  // sort ping-pong scratch
 
@@ -130,6 +138,7 @@ struct pi_frame {
 
   // counters
   long long fieldEvals = 0, pairs = 0, bisectEvals = 0, fp64Count = 0, nLeaves = 0, nEmpty = 0;
+  long long doneEvals = 0;  // evaluations the kernels performed (after deduplication)
   long long qefAccepted = 0, qefSingular = 0;
   long long gridPairs = 0;  // candidate pairs of the last uniform-grid sampling
   pisurf::DBuf<unsigned long long> dcount;  // device counters
@@ -202,17 +211,25 @@ long long load_csv(const char* path, float* xyz, float* radius, long long cap, i
 void write_ply(const char* path, const float* verts, long long nv, const int32_t* tris, long long nt,
                int one_based);
 void eval_points(pi_frame* f, const float* d_pts, long long m, float* d_val, float* d_grad);
+// FP64 oracle (fp64.cu): per-particle state on demand; values at device
+// points; the state in original particle order into host arrays (each may be
+// null); iso, MaxScalar, Influnce2, Sigma in double.
+void fp64_state(pi_frame* f);
+void fp64_eval(pi_frame* f, const float* d_pts, long long m, double* d_val, double* d_grad);
+void fp64_aniso_get(pi_frame* f, double* h_x3, double* h_g9, double* h_det);
+void fp64_scalars(const pi_frame* f, double out4[4]);
 long long neighbors(pi_frame* f, const float* h_pts, long long m, long long* h_off, int* h_idx,
                     long long cap);
 long long in_box(pi_frame* f, const float* b1, const float* b2, int* h_idx, long long cap);
 void dmc_host_table(int trans[256][8], bool flip[256], int code[256]);
-void prof_begin(pi_ctx* c, cudaStream_t s);
-void prof_end(pi_ctx* c, cudaStream_t s, long long pairs, long long evals);
+// Events around the launches of kernel group g when the context profiles.
+void prof_begin(pi_ctx* c, cudaStream_t s, int g);
+void prof_end(pi_ctx* c, cudaStream_t s, int g);
 
 // Striped device counters of a frame: zero them / read and sum the stripes
 // (synchronises the context stream).
 void counters_reset(pi_frame* f);
-void counters_read(pi_frame* f, unsigned long long out[8]);
+void counters_read(pi_frame* f, unsigned long long out[kCounters]);
 
 // Host scalar constants with the reference's float/double semantics.
 float bspline_host(float ratio, float sigma);

@@ -328,10 +328,11 @@ __global__ void __launch_bounds__(32 * kEvalWarps, (K > 2 ? 3 : 4)) k_q_eval(QAr
   const ChunkStage st{s_x[wib], s_a[wib], s_b[wib], s_l[wib]};
   const int nchunks = *nchunks_ptr;
   const int nwarps = gridDim.x * kEvalWarps;
-  long long pairs = 0;
+  long long pairs = 0, done = 0;
   for (int ci = blockIdx.x * kEvalWarps + wib; ci < nchunks; ci += nwarps) {
     const int2 ch = chunks[ci];
     const int len = min(32 * K, __ldg(ucnt + ch.x) - ch.y);
+    done += len;
     const int* ord = order + __ldg(qoff + ch.x) + ch.y;
     int q[K];
     float x[K], y[K], z[K];
@@ -359,7 +360,11 @@ __global__ void __launch_bounds__(32 * kEvalWarps, (K > 2 ? 3 : 4)) k_q_eval(QAr
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
-  if (lane == 0 && pairs) stripe_add(counters, 1, (unsigned long long)pairs);
+  if (lane == 0) {
+    stripe_add(counters, C_SAMPLE_PAIRS, (unsigned long long)pairs);
+    stripe_add(counters, C_PAIRS_CHUNK, (unsigned long long)pairs);
+    stripe_add(counters, C_DONE_CHUNK, (unsigned long long)done);
+  }
 }
 
 // Sparse levels (a few distinct samples per bucket): one thread per distinct
@@ -372,17 +377,25 @@ __global__ void __launch_bounds__(256, 4) k_q_eval_thread(QArgs a, const int* __
                                                        const float4* __restrict__ nd_v, float* __restrict__ qval,
                                                        unsigned long long* __restrict__ counters) {
   const int n = *count_ptr;
-  long long pairs = 0;
+  long long pairs = 0, done = 0;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
     const int q = list[t];
     const long long node = a.lb + q / kQ;
     float qx, qy, qz;
     sample_point(nd_c[node], nd_v[node], q % kQ, qx, qy, qz);
     qval[q] = a.iso - field_sum(a.g, a.P, qx, qy, qz, &pairs);
+    ++done;
   }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
-  if ((threadIdx.x & 31) == 0 && pairs) stripe_add(counters, 1, (unsigned long long)pairs);
+  for (int o = 16; o > 0; o >>= 1) {
+    pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+    done += __shfl_xor_sync(0xffffffffu, done, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    stripe_add(counters, C_SAMPLE_PAIRS, (unsigned long long)pairs);
+    stripe_add(counters, C_PAIRS_THREAD, (unsigned long long)pairs);
+    stripe_add(counters, C_DONE_THREAD, (unsigned long long)done);
+  }
 }
 
 // Sparse levels: the distinct samples, placed per bucket by k_q_dedupe, made
@@ -423,8 +436,12 @@ __global__ void __launch_bounds__(256, 4) k_leaf_level(LevelArgs a, const float4
     evals += __shfl_xor_sync(0xffffffffu, evals, o);
   }
   if ((threadIdx.x & 31) == 0) {
-    if (pairs) stripe_add(counters, 1, (unsigned long long)pairs);
-    if (evals) stripe_add(counters, 0, (unsigned long long)evals);
+    stripe_add(counters, C_SAMPLE_PAIRS, (unsigned long long)pairs);
+    stripe_add(counters, C_PAIRS_LEAF, (unsigned long long)pairs);
+    stripe_add(counters, C_DONE_LEAF, (unsigned long long)evals);
+    // the reference evaluates the 27 lattice samples (GridEval) and the
+    // leaf value of each of these nodes
+    stripe_add(counters, C_REF_EVALS, (unsigned long long)(28 * evals));
   }
 }
 
@@ -490,7 +507,7 @@ __global__ void __launch_bounds__(64, 24) k_classify(LevelArgs a, const float* _
       v.w = vc;
       nd_v[node] = v;
     }
-    stripe_add(counters, 0, (unsigned long long)(27 + (type == T_LEAF ? 1 : 0)));
+    stripe_add(counters, C_REF_EVALS, (unsigned long long)(27 + (type == T_LEAF ? 1 : 0)));
   }
 }
 
@@ -1037,8 +1054,10 @@ void stage_octree(pi_frame* f) {
     if (!known)
       PI_LAUNCH(k_empty, div_up(nl, wpb), 32 * wpb, 0, s, la, f->nd_c.p, f->nd_v.p, f->nd_type.p, f->nd_curv.p);
     if (depth >= f->dmin && leaf_level && !f->P.qef) {
+      prof_begin(ctx, s, PG_LEAF);
       PI_LAUNCH(k_leaf_level, (int)std::min<long long>((long long)ctx->smCount * 8, div_up(nl, 256)), 256, 0, s, la,
                 f->nd_c.p, f->nd_v.p, f->nd_type.p, f->dcount.p);
+      prof_end(ctx, s, PG_LEAF);
     } else if (depth >= f->dmin) {
       const long long qn = nl * kQ;
       // buckets: cell octants on the leaf level, whole cells above it
@@ -1072,13 +1091,14 @@ void stage_octree(pi_frame* f) {
       if (dense)
         lanes = eval_lanes_for(f, depth == f->dmax ? 0 : 1, qa, qn, nb, order.p, qcnt.p, ucnt.p, chunks.p,
                                qcnt.p + nb + 1, qval.p);
-      prof_begin(ctx, s);
+      const int pg = dense ? PG_CHUNK : PG_THREAD;
+      prof_begin(ctx, s, pg);
       if (dense)
         dense_eval(f, lanes, qa, qn, nb, order.p, qcnt.p, ucnt.p, chunks.p, qcnt.p + nb + 1, qval.p, f->dcount.p);
       else
         PI_LAUNCH(k_q_eval_thread, (int)std::min<long long>((long long)ctx->smCount * 8, div_up(qn, 256)), 256, 0,
                   s, qa, list, ucum.p + nb, f->nd_c.p, f->nd_v.p, qval.p, f->dcount.p);
-      prof_end(ctx, s, -1, -1);
+      prof_end(ctx, s, pg);
       PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p, f->nd_type.p,
                 f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p);
       if (f->P.qef) qef_level(f, lb, le, depth, qkey.p);  // the sample keys are spent (qn >= nl + 1)

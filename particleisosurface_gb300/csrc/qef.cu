@@ -151,7 +151,7 @@ __global__ void k_qef_pick(const int8_t* __restrict__ nd_type, long long lb, lon
   if (leaf) list[1 + base + __popc(m & ((1u << lane) - 1u))] = (int)(node - lb);
 }
 
-// counters: 5 QEF vertices accepted, 6 singular systems, 7 field evaluations
+// counters: QEF vertices accepted, singular systems, field evaluations, leaves solved
 __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, const int* __restrict__ list,
                                                      float4* __restrict__ nd_v,
                                                      const float4* __restrict__ nd_c,
@@ -162,6 +162,10 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, const int* __res
   __shared__ double s_sv[27][kQefThreads];
   const int t = blockIdx.x * kQefThreads + threadIdx.x;
   if (t >= __ldg(list)) return;
+  {
+    const unsigned am = __activemask();  // the warp's lanes that hold a leaf
+    if ((int)(threadIdx.x & 31) == __ffs(am) - 1) stripe_add(counters, C_QEF_LEAVES, (unsigned long long)__popc(am));
+  }
   const long long node = a.lb + __ldg(list + 1 + t);
   const float4 c = nd_c[node];
   const float h = c.w;
@@ -380,12 +384,12 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, const int* __res
       accepted = true;
     }
   } else {
-    stripe_add(counters, 6, 1ull);
+    stripe_add(counters, C_QEF_SINGULAR, 1ull);
   }
   if (accepted) {
     v.w = a.iso - field_sum(a.g, a.P, v.x, v.y, v.z, nullptr);
-    stripe_add(counters, 7, 1ull);
-    stripe_add(counters, 5, 1ull);
+    stripe_add(counters, C_QEF_EVALS, 1ull);
+    stripe_add(counters, C_QEF_ACCEPTED, 1ull);
   }
   // leaf by size keeps the zeroing (no SingleEval follows it)
   const bool leaf_by_size = (double)(cellsize - a.radius) < 1e-8;
@@ -410,8 +414,10 @@ void qef_level(pi_frame* f, long long lb, long long le, int depth, int* scratch)
              1.0 / (double)step};
   PI_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int), s));
   PI_LAUNCH(k_qef_pick, div_up(le - lb, 256), 256, 0, s, f->nd_type.p, lb, le, scratch);
+  prof_begin(f->ctx, s, PG_QEF);
   PI_LAUNCH(k_qef, div_up(le - lb, kQefThreads), kQefThreads, 0, s, qa, scratch, f->nd_v.p, f->nd_c.p,
             f->nd_samp.p, nullptr, f->dcount.p);
+  prof_end(f->ctx, s, PG_QEF);
 }
 
 }  // namespace pisurf

@@ -157,10 +157,10 @@ long long grid_sample(pi_frame* f, float* d_out, long long cap) {
   counters_reset(f);
   GridView g{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p};
   PartView P{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p};
-  prof_begin(ctx, s);
+  prof_begin(ctx, s, PG_GRID);
   PI_LAUNCH(k_grid_eval, blocks, 32 * kGridWarps, 0, s, g, P, f->iso, R, d_out, f->dcount.p);
-  prof_end(ctx, s, -1, -1);
-  unsigned long long cnt[8];
+  prof_end(ctx, s, PG_GRID);
+  unsigned long long cnt[kCounters];
   counters_read(f, cnt);
   f->gridPairs = (long long)cnt[1];
   return total;

@@ -167,6 +167,16 @@ def _sphere_or_slab(rng, n, radius, jitter, domain=1.0):
     return _jitter(pts, jitter * radius, rng)
 
 
+def _sorted_unique(a):
+    """np.unique of an int64 array (sorted distinct values) by a sort and a
+    neighbour comparison, which is several times faster than numpy's
+    hash-based unique on millions of lattice keys."""
+    a = np.sort(a)
+    if len(a) == 0:
+        return a
+    return a[np.concatenate([[True], a[1:] != a[:-1]])]
+
+
 def mixed_frame(seed, n_target, radius=0.01, jitter=0.2) -> Frame:
     """Batched-form frame: a seeded union of 1-6 jittered-lattice spheres and
     slabs in a unit box.  The shapes are drawn first; the whole set is then
@@ -193,7 +203,7 @@ def mixed_frame(seed, n_target, radius=0.01, jitter=0.2) -> Frame:
         ijk = np.round(pts / sp).astype(np.int64)
         ijk -= ijk.min(0) if len(ijk) else 0
         m = int(ijk.max()) + 1 if len(ijk) else 1
-        key = np.unique((ijk[:, 0] * m + ijk[:, 1]) * m + ijk[:, 2])
+        key = _sorted_unique((ijk[:, 0] * m + ijk[:, 1]) * m + ijk[:, 2])
         return np.stack([key // (m * m), (key // m) % m, key % m], -1) * sp + \
             (np.round(pts.min(0) / sp) * sp if len(pts) else 0.0)
 
@@ -215,6 +225,19 @@ def batch_frames(count=64, seed=100, n_min=50_000, n_max=2_000_000, radius=0.01)
     rng = np.random.default_rng(seed)
     ns = np.exp(rng.uniform(np.log(n_min), np.log(n_max), size=count)).astype(int)
     return [mixed_frame(seed + 1 + i, int(n), radius) for i, n in enumerate(ns)]
+
+
+def batch_frame(k, count=64, seed=100, n_min=50_000, n_max=2_000_000, radius=0.01):
+    """Frame k of batch_frames(count, seed, ...) without building the others."""
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(np.log(n_min), np.log(n_max), size=count)).astype(int)
+    return mixed_frame(seed + 1 + k, int(ns[k]), radius)
+
+
+def batch_sizes(count=64, seed=100, n_min=50_000, n_max=2_000_000):
+    """Particle counts of batch_frames(count, seed, ...)."""
+    rng = np.random.default_rng(seed)
+    return np.exp(rng.uniform(np.log(n_min), np.log(n_max), size=count)).astype(int)
 
 
 def _bezier(rng, t, scale):

@@ -183,3 +183,176 @@ def qef_solve_f64(center, half, samples):
     in_cell = bool(np.all(x[:3] >= mn) and np.all(x[:3] <= mx))
     err = float(np.sum((g @ x[:3] - (pts * g).sum(1) - x[3]) ** 2 / (1 + (g * g).sum(1))))
     return x, in_cell, singular, err
+
+
+# ---------------------------------------------------------------------------
+# Vectorised forms of the comparisons above, for frames of millions of nodes
+# (the headline configurations).  Same rules and bounds.
+# ---------------------------------------------------------------------------
+
+def node_keys(depth, ids):
+    """(depth, id) -> one uint64 (depth in the top 5 bits; ids < 8^19)."""
+    d = np.asarray(depth).astype(np.uint64)
+    i = np.asarray(ids).astype(np.uint64)
+    assert d.size == 0 or int(d.max()) < 20
+    return (d << np.uint64(59)) | i
+
+
+def _under(keys_depth, keys_id, skip):
+    """Mask of nodes (depth, id arrays) strictly below one of the skip nodes."""
+    mask = np.zeros(len(keys_depth), bool)
+    if not skip:
+        return mask
+    sk = np.array(skip, dtype=np.int64)
+    d = keys_depth.astype(np.int64)
+    ids = keys_id.astype(np.uint64)
+    for d0 in np.unique(sk[:, 0]):
+        sel = d > d0
+        if not sel.any():
+            continue
+        anc = ids[sel] >> (np.uint64(3) * (d[sel] - d0).astype(np.uint64))
+        want = np.array(sorted(set(int(x) for x in sk[sk[:, 0] == d0, 1])), np.uint64)
+        mask[np.nonzero(sel)[0][np.isin(anc, want)]] = True
+    return mask
+
+
+def compare_octrees_fast(o_nodes, g_nodes, oracle, max_scalar, depth_min, fp64_eval=None):
+    """compare_octrees over arrays.  o_nodes: the oracle's nodes() dict;
+    g_nodes: the library's pi_node dump.  A type mismatch is explained when a
+    curvature lies within CURV_EPS of 0.99 or (at depth >= D_min) a sample of
+    the node lies within ISO_EPS * MaxScalar of the isovalue (oracle values);
+    its subtree is then skipped.  Leaf values beyond FIELD_TOL * MaxScalar of
+    the float oracle must be within FIELD_TOL_FP64 of fp64_eval (when given)."""
+    od, oi, ot = o_nodes["depth"], o_nodes["id"], o_nodes["type"]
+    gd, gi, gt = g_nodes["depth"], g_nodes["id"], g_nodes["type"]
+    ka = node_keys(od, oi)
+    kb = node_keys(gd, gi)
+    assert len(np.unique(ka)) == len(ka) and len(np.unique(kb)) == len(kb)
+    common, ia, ib = np.intersect1d(ka, kb, assume_unique=True, return_indices=True)
+    rep = dict(nodes_oracle=len(ka), nodes_gpu=len(kb), type_mismatch=0, explained=0, unexplained=[],
+               leaf_value_maxdiff=0.0, compared=0, leaves_beyond_float_tol=0, leaf_far_vs_fp64_max=0.0)
+    mism = np.nonzero(ot[ia] != gt[ib])[0]
+    mism = mism[np.argsort(od[ia[mism]], kind="stable")]
+    rep["type_mismatch"] = int(len(mism))
+    skip = []
+    for m in mism:
+        a, b = ia[m], ib[m]
+        d, i = int(od[a]), int(oi[a])
+        if any(d > d0 and (i >> (3 * (d - d0))) == i0 for d0, i0 in skip):
+            continue
+        ca, cb = float(o_nodes["curv"][a]), float(g_nodes["curv"][b])
+        near = abs(ca - 0.99) < CURV_EPS
+        if not near and d >= depth_min:
+            vals = oracle.eval(sample_points(o_nodes["center"][a], o_nodes["half"][a]))
+            near = np.min(np.abs(vals)) < ISO_EPS * max_scalar
+        if near:
+            rep["explained"] += 1
+            skip.append((d, i))
+        else:
+            rep["unexplained"].append(("type", (d, i), int(ot[a]), int(gt[b]), ca, cb))
+    only_a = np.setdiff1d(np.arange(len(ka)), ia, assume_unique=True)
+    only_b = np.setdiff1d(np.arange(len(kb)), ib, assume_unique=True)
+    for idx, dd, ii, tag in ((only_a, od, oi, "missing"), (only_b, gd, gi, "extra")):
+        bad = idx[~_under(dd[idx], ii[idx], skip)]
+        rep["unexplained"] += [(tag, (int(dd[k]), int(ii[k]))) for k in bad[:20]]
+        if len(bad) > 20:
+            rep["unexplained"].append((tag, "%d more" % (len(bad) - 20)))
+    live = ~_under(od[ia], oi[ia], skip)
+    rep["compared"] = int(live.sum())
+    leaf = live & (ot[ia] == 2) & (gt[ib] == 2)
+    va = o_nodes["node"][ia[leaf], 3].astype(np.float64)
+    vb = g_nodes["node"][ib[leaf]][:, 3].astype(np.float64)
+    dv = np.abs(va - vb)
+    rep["leaf_value_maxdiff"] = float(dv.max()) if len(dv) else 0.0
+    far = dv > FIELD_TOL * max_scalar
+    rep["leaves_beyond_float_tol"] = int(far.sum())
+    if far.any() and fp64_eval is not None:
+        pos = g_nodes["node"][ib[leaf][far]][:, :3].astype(np.float32)
+        v64 = fp64_eval(pos)
+        rep["leaf_far_vs_fp64_max"] = float((np.abs(vb[far] - v64) / max_scalar).max())
+    return rep
+
+
+def _pair_view(k):
+    k = np.ascontiguousarray(np.asarray(k, np.uint64).reshape(-1, 2))
+    return k.view([("a", "<u8"), ("b", "<u8")]).ravel()
+
+
+def _tri_view(t):
+    """Triangles (n, 3) of global vertex ids, rotated so that the smallest id
+    comes first (orientation kept), as a structured array for set operations."""
+    t = np.asarray(t, np.int64).reshape(-1, 3)
+    r = np.argmin(t, axis=1)
+    rows = np.arange(len(t))
+    out = np.stack([t[rows, r], t[rows, (r + 1) % 3], t[rows, (r + 2) % 3]], 1)
+    out = np.ascontiguousarray(out)
+    return out.view([("a", "<i8"), ("b", "<i8"), ("c", "<i8")]).ravel()
+
+
+def compare_meshes_fast(o_mesh, g_mesh, radius):
+    """compare_meshes over arrays: vertices keyed by their leaf-id pair,
+    triangles as rotated triples of vertex keys."""
+    ov, ot, ok = o_mesh
+    gv, gt, gk = g_mesh
+    allk = np.concatenate([_pair_view(ok), _pair_view(gk)])
+    uniq, inv = np.unique(allk, return_inverse=True)
+    io, ig = inv[:len(ok)], inv[len(ok):]
+    assert len(np.unique(io)) == len(io) and len(np.unique(ig)) == len(ig)
+    so = np.zeros(len(uniq), bool)
+    sg = np.zeros(len(uniq), bool)
+    so[io] = True
+    sg[ig] = True
+    po = np.zeros((len(uniq), 3), np.float32)
+    pg = np.zeros((len(uniq), 3), np.float32)
+    po[io] = ov
+    pg[ig] = gv
+    both = so & sg
+    d = np.abs(po[both] - pg[both]).max(1) if both.any() else np.zeros(1)
+    to = np.unique(_tri_view(io[np.asarray(ot, np.int64) - 1]))
+    tg = np.unique(_tri_view(ig[np.asarray(gt, np.int64)]))
+    tc = np.intersect1d(to, tg, assume_unique=True)
+    return dict(verts_oracle=int(so.sum()), verts_gpu=int(sg.sum()), verts_only_oracle=int((so & ~sg).sum()),
+                verts_only_gpu=int((sg & ~so).sum()), tris_oracle=len(to), tris_gpu=len(tg),
+                tris_only_oracle=len(to) - len(tc), tris_only_gpu=len(tg) - len(tc),
+                vert_maxdiff_over_r=float(d.max() / radius),
+                vert_rmsdiff_over_r=float(np.sqrt(np.mean(d.astype(np.float64) ** 2)) / radius),
+                verts_off_tol=int(np.sum(d > VERT_TOL * radius)))
+
+
+def qef_solve_f64_batch(centers, halves, samples):
+    """qef_solve_f64 for many leaves at once: returns x [n, 4], in_cell [n],
+    singular [n]."""
+    c = np.asarray(centers, np.float32).reshape(-1, 3)
+    h = np.asarray(halves, np.float32).reshape(-1)
+    n = len(c)
+    mn = c - h[:, None]
+    mx = c + h[:, None]
+    t = np.array([[x, y, z] for z in range(3) for y in range(3) for x in range(3)], np.float32) / np.float32(2)
+    pts = ((np.float32(1) - t)[None] * mn[:, None, :] + t[None] * mx[:, None, :]).astype(np.float64)
+    f = np.asarray(samples, np.float64).reshape(n, 27)
+    step = (np.float32(2.0) * h / np.float32(2)).astype(np.float64)[:, None, None]
+    v = f.reshape(n, 3, 3, 3)  # [node, z, y, x]
+    g = np.zeros((n, 3, 3, 3, 3))
+    for ax, axis in ((0, 3), (1, 2), (2, 1)):
+        vv = np.moveaxis(v, axis, 1)
+        gg = np.empty_like(vv)
+        gg[:, 0] = (vv[:, 0] - vv[:, 1]) / step
+        gg[:, 2] = (vv[:, 1] - vv[:, 2]) / step
+        gg[:, 1] = (vv[:, 0] - vv[:, 2]) / (2 * step)
+        g[..., ax] = np.moveaxis(gg, 1, axis)
+    g = g.reshape(n, 27, 3)
+    pl = np.concatenate([g, -np.ones((n, 27, 1)), (-(pts * g).sum(2) + f)[:, :, None]], axis=2)
+    M = np.einsum("nki,nkj->nij", pl, pl)
+    A = M[:, :4, :4]
+    B = -M[:, :4, 4]
+    dg = np.diagonal(A, axis1=1, axis2=2)
+    d = np.where(dg > 0, 1.0 / np.sqrt(np.where(dg > 0, dg, 1.0)), 1.0)
+    As = A * d[:, :, None] * d[:, None, :]
+    w, V = np.linalg.eigh(As)
+    wmax = np.abs(w).max(1)
+    keep = np.abs(w) > (1e-12 * wmax)[:, None]
+    y = np.einsum("nji,nj->ni", V, d * B)
+    y = np.where(keep, y / np.where(keep, w, 1.0), 0.0)
+    x = d * np.einsum("nij,nj->ni", V, y)
+    in_cell = np.all(x[:, :3] >= mn, axis=1) & np.all(x[:, :3] <= mx, axis=1)
+    return x, in_cell, ~keep.all(1)

@@ -167,6 +167,12 @@ def test_octree_identical_except_near_iso(ctx, name):
           rep["unexplained"][:5])
     assert not rep["unexplained"]
     assert rep["explained"] <= max(2, rep["compared"] // 10000)
+    if rep["explained"] == 0:
+        # the library counts the SingleEval calls the reference makes for the
+        # octree (the oracle's counter 0 minus its bisection calls)
+        info = g.info()
+        assert info["field_evals"] - info["bisection_evals"] == o.counter(0) - o.counter(3)
+        assert 0 < info["field_evals_performed"] <= info["field_evals"]
     ms = o.scalars()["max_scalar"]
     if rep["leaf_value_maxdiff"] > PR.FIELD_TOL * ms:
         # leaves where the float oracle and the library differ by more than

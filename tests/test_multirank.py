@@ -44,7 +44,7 @@ def test_reference_arm_under_torchrun_prints_one_line():
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
-           "--gpus", "2", "--steps", "1", "--warmup", "1", "--particles", "3000", "--cpu-sample-evals", "2000"]
+           "--gpus", "2", "--steps", "2", "--warmup", "1", "--particles", "3000", "--ref-budget-s", "60"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
@@ -52,3 +52,5 @@ def test_reference_arm_under_torchrun_prints_one_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+    # whole frames timed: the line's steps is the number of frames it timed
+    assert 1 <= d["steps"] <= 2 and len(d["frames_timed_s"]) == d["steps"]
