@@ -242,7 +242,7 @@ def make_frame(n):
 def time_resident(N, torch, ctx, f, stream, flush, steps, warmup, barrier, profile=False, clocks=None):
     """Steps of pi_frame_reset + pi_run on a resident frame, each bracketed
     by CUDA events on the library stream after an L2 flush.  Returns the
-    per-step ms, the library's kernel launches per step and (profile) the
+    per-step ms, the library's kernel launches over the timed steps and (profile) the
     per-group kernel times."""
     for _ in range(warmup):
         f.reset().run()
@@ -268,7 +268,7 @@ def time_resident(N, torch, ctx, f, stream, flush, steps, warmup, barrier, profi
     if profile:
         groups = ctx.kernel_groups()
         ctx.profile(False)
-    return [s.elapsed_time(e) for s, e in ev], launches // max(1, steps), groups, ck
+    return [s.elapsed_time(e) for s, e in ev], launches, groups, ck
 
 
 def time_e2e(N, torch, ctx, params, fr, info, stream, flush, steps, warmup, barrier):

@@ -157,7 +157,10 @@ void resolve_pending(pi_frame* f) {
   }
   if (f->pin_pending & (1 << kPinOctree)) {
     fold_counters(h + (size_t)kPinOctree * kCounterWords, c);
-    f->fieldEvals = (long long)(c[C_REF_EVALS] + c[C_QEF_EVALS]);
+    // the reference's NodeCalcNode evaluates the field at the leaf's node
+    // point whether or not its vertex is accepted (src/iso_method_ours.cpp:
+    // 161-173): one more reference call per leaf solved
+    f->fieldEvals = (long long)(c[C_REF_EVALS] + c[C_QEF_LEAVES]);
     f->doneEvals = (long long)(c[C_DONE_CHUNK] + c[C_DONE_THREAD] + c[C_DONE_LEAF] + c[C_QEF_EVALS]);
     f->pairs = (long long)c[C_SAMPLE_PAIRS];
     f->qefAccepted = (long long)c[C_QEF_ACCEPTED];

@@ -30,19 +30,48 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// Per-warp staging buffers (shared memory), kCandBuf records each.
-struct ChunkStage {
-  float4* x;
-  float4* a;
-  float4* b;
-  float4* l;
+// Per-warp staging buffer (shared memory): the staged candidates' records,
+// one array of kCandBuf floats per component (structure of arrays), so that a
+// component of two consecutive candidates is one 8-byte load feeding the
+// packed FP32 instructions below.
+enum : int {
+  SC_X, SC_Y, SC_Z,        // centre, high part (xm)
+  SC_LX, SC_LY, SC_LZ,     // centre, low part (xlo)
+  SC_A0, SC_A1, SC_A2, SC_A3,  // A = G / h: a00 a01 a02 a11
+  SC_B0, SC_B1, SC_B2,     // a12 a22 det * Sigma
+  kStageComps
 };
+constexpr int kStageFloats = kStageComps * kCandBuf;  // per warp
+
+struct ChunkStage {
+  float* c;  // c[k * kCandBuf + t]: component k of staged candidate t
+};
+
+// 4-byte asynchronous copy global -> shared.
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ float2 ld_pair(const ChunkStage& st, int k, int t) {
+  return *reinterpret_cast<const float2*>(st.c + k * kCandBuf + t);
+}
 
 // Sums over the chunk's candidates for the K points of this lane.  act[m]
 // marks the lane's valid points, and an invalid point's coordinates must be
 // NaN (its s2 is then NaN and no term passes s2 < 4); slots[m]
-// (warp-uniform) tells whether any lane holds a point m.  Returns the compensated sums in sum[]; adds the
-// algorithmic candidate pairs of the lane's points to pairs.
+// (warp-uniform) tells whether any lane holds a point m.  Returns the
+// compensated sums in sum[]; adds the algorithmic candidate pairs of the
+// lane's points to pairs.
+//
+// Two consecutive staged candidates are evaluated together with Blackwell's
+// packed FP32 instructions (__ffma2_rn, __fmul2_rn, __fadd2_rn: two IEEE
+// round-to-nearest operations per instruction, each element rounded as the
+// scalar instruction rounds it), from the offset q - x through the kernel
+// term det * Sigma * B(|A d|).  The expressions are those of field_sum (a - b
+// as fma(b, -1, a), exact in the product, one rounding), so every term is
+// bit for bit the scalar one; the compensated sum then takes the two terms
+// one after the other, in candidate order.
 template <int K>
 __device__ __forceinline__ void chunk_field(const GridView& g, const PartView& P, int cx, int cy, int cz,
                                             const float (&qx)[K], const float (&qy)[K], const float (&qz)[K],
@@ -71,28 +100,62 @@ __device__ __forceinline__ void chunk_field(const GridView& g, const PartView& P
   const float bhx = fkey_inv(__reduce_max_sync(0xffffffffu, hx));
   const float bhy = fkey_inv(__reduce_max_sync(0xffffffffu, hy));
   const float bhz = fkey_inv(__reduce_max_sync(0xffffffffu, hz));
+  // the lane's points as packed pairs (q, q), built once per chunk
+  float2 QX[K], QY[K], QZ[K];
+#pragma unroll
+  for (int m = 0; m < K; ++m) {
+    QX[m] = make_float2(qx[m], qx[m]);
+    QY[m] = make_float2(qy[m], qy[m]);
+    QZ[m] = make_float2(qz[m], qz[m]);
+  }
+  const float2 M1 = make_float2(-1.0f, -1.0f);
   // compensated sums (Kahan), updated only for in-support terms
   float s[K], c[K];
 #pragma unroll
   for (int m = 0; m < K; ++m) s[m] = c[m] = 0.f;
   int nc = 0;
+  auto kahan = [&](int m, float term) {
+    const float y = __fsub_rn(term, c[m]);
+    const float tt = __fadd_rn(s[m], y);
+    c[m] = __fsub_rn(__fsub_rn(tt, s[m]), y);
+    s[m] = tt;
+  };
   auto flush = [&]() {
     cp_async_wait_all();
     __syncwarp();
-#pragma unroll 2
-    for (int t = 0; t < nc; ++t) {
-      const float4 x = st.x[t], ga = st.a[t], gb = st.b[t], lo = st.l[t];
+#pragma unroll 1
+    for (int t = 0; t < nc; t += 2) {
+      const bool two = t + 1 < nc;  // warp-uniform: a second candidate in this pair
+      const float2 X = ld_pair(st, SC_X, t), Y = ld_pair(st, SC_Y, t), Z = ld_pair(st, SC_Z, t);
+      const float2 LX = ld_pair(st, SC_LX, t), LY = ld_pair(st, SC_LY, t), LZ = ld_pair(st, SC_LZ, t);
+      const float2 A0 = ld_pair(st, SC_A0, t), A1 = ld_pair(st, SC_A1, t), A2 = ld_pair(st, SC_A2, t),
+                   A3 = ld_pair(st, SC_A3, t);
+      const float2 B0 = ld_pair(st, SC_B0, t), B1 = ld_pair(st, SC_B1, t), B2 = ld_pair(st, SC_B2, t);
 #pragma unroll
       for (int m = 0; m < K; ++m) {
         if (!slots[m]) continue;  // warp-uniform
-        float u0, u1, u2;
-        amul(ga, gb, (qx[m] - x.x) - lo.x, (qy[m] - x.y) - lo.y, (qz[m] - x.z) - lo.z, u0, u1, u2);
-        const float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
-        if (s2 < 4.0f) {  // in support: one compensated step
-          const float y = __fsub_rn(gb.z * bspline_s2(s2), c[m]);
-          const float tt = __fadd_rn(s[m], y);
-          c[m] = __fsub_rn(__fsub_rn(tt, s[m]), y);
-          s[m] = tt;
+        // d = (q - x) - lo
+        const float2 dx = __ffma2_rn(LX, M1, __ffma2_rn(X, M1, QX[m]));
+        const float2 dy = __ffma2_rn(LY, M1, __ffma2_rn(Y, M1, QY[m]));
+        const float2 dz = __ffma2_rn(LZ, M1, __ffma2_rn(Z, M1, QZ[m]));
+        // u = A d (amul), s2 = |u|^2
+        const float2 u0 = __ffma2_rn(A0, dx, __ffma2_rn(A1, dy, __fmul2_rn(A2, dz)));
+        const float2 u1 = __ffma2_rn(A1, dx, __ffma2_rn(A3, dy, __fmul2_rn(B0, dz)));
+        const float2 u2 = __ffma2_rn(A2, dx, __ffma2_rn(B0, dy, __fmul2_rn(B1, dz)));
+        const float2 s2 = __ffma2_rn(u0, u0, __ffma2_rn(u1, u1, __fmul2_rn(u2, u2)));
+        const bool in0 = s2.x < 4.0f, in1 = two && s2.y < 4.0f;
+        if (in0 || in1) {
+          // bspline_s2 on both: q = s2 / sqrt(s2), b1 = 1 + s2 (0.75 q - 1.5),
+          // b2 = 0.25 (2 - q)^3, q <= 1 ? b1 : b2
+          const float2 r = make_float2(rsqrtf(fmaxf(s2.x, 1e-30f)), rsqrtf(fmaxf(s2.y, 1e-30f)));
+          const float2 q = __fmul2_rn(s2, r);
+          const float2 b1 = __ffma2_rn(s2, __ffma2_rn(make_float2(0.75f, 0.75f), q, make_float2(-1.5f, -1.5f)),
+                                       make_float2(1.0f, 1.0f));
+          const float2 tq = __ffma2_rn(q, M1, make_float2(2.0f, 2.0f));
+          const float2 b2 = __fmul2_rn(__fmul2_rn(__fmul2_rn(make_float2(0.25f, 0.25f), tq), tq), tq);
+          const float2 term = __fmul2_rn(B2, make_float2(q.x <= 1.0f ? b1.x : b2.x, q.y <= 1.0f ? b1.y : b2.y));
+          if (in0) kahan(m, term.x);
+          if (in1) kahan(m, term.y);
         }
       }
     }
@@ -118,10 +181,23 @@ __device__ __forceinline__ void chunk_field(const GridView& g, const PartView& P
         const unsigned pm = __ballot_sync(0xffffffffu, pass);
         if (pass) {
           const int p = nc + __popc(pm & lt);
-          st.x[p] = x;
-          cp_async16(st.a + p, P.ga + j);
-          cp_async16(st.b + p, P.gb + j);
-          cp_async16(st.l + p, P.xlo + j);
+          float* const c0 = st.c + p;
+          c0[SC_X * kCandBuf] = x.x;
+          c0[SC_Y * kCandBuf] = x.y;
+          c0[SC_Z * kCandBuf] = x.z;
+          const float* ga = reinterpret_cast<const float*>(P.ga + j);
+          const float* gb = reinterpret_cast<const float*>(P.gb + j);
+          const float* gl = reinterpret_cast<const float*>(P.xlo + j);
+          cp_async4(c0 + SC_LX * kCandBuf, gl);
+          cp_async4(c0 + SC_LY * kCandBuf, gl + 1);
+          cp_async4(c0 + SC_LZ * kCandBuf, gl + 2);
+          cp_async4(c0 + SC_A0 * kCandBuf, ga);
+          cp_async4(c0 + SC_A1 * kCandBuf, ga + 1);
+          cp_async4(c0 + SC_A2 * kCandBuf, ga + 2);
+          cp_async4(c0 + SC_A3 * kCandBuf, ga + 3);
+          cp_async4(c0 + SC_B0 * kCandBuf, gb);
+          cp_async4(c0 + SC_B1 * kCandBuf, gb + 1);
+          cp_async4(c0 + SC_B2 * kCandBuf, gb + 2);
         }
         nc += __popc(pm);
         if (nc > kCandBuf - 32) flush();

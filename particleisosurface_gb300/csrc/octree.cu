@@ -321,11 +321,10 @@ __global__ void __launch_bounds__(32 * kEvalWarps, (K > 2 ? 3 : 4)) k_q_eval(QAr
                                                             const float4* __restrict__ nd_v,
                                                             float* __restrict__ qval,
                                                             unsigned long long* __restrict__ counters) {
-  __shared__ float4 s_x[kEvalWarps][kCandBuf], s_a[kEvalWarps][kCandBuf], s_b[kEvalWarps][kCandBuf],
-      s_l[kEvalWarps][kCandBuf];
+  __shared__ __align__(16) float s_stage[kEvalWarps][kStageFloats];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  const ChunkStage st{s_x[wib], s_a[wib], s_b[wib], s_l[wib]};
+  const ChunkStage st{s_stage[wib]};
   const int nchunks = *nchunks_ptr;
   const int nwarps = gridDim.x * kEvalWarps;
   long long pairs = 0, done = 0;

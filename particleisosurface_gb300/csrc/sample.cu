@@ -44,11 +44,10 @@ struct GridRuns {
 __global__ void __launch_bounds__(32 * kGridWarps, 3) k_grid_eval(GridView g, PartView P, float iso, GridRuns R,
                                                                  float* __restrict__ out,
                                                                  unsigned long long* __restrict__ counters) {
-  __shared__ float4 s_x[kGridWarps][kCandBuf], s_a[kGridWarps][kCandBuf], s_b[kGridWarps][kCandBuf],
-      s_l[kGridWarps][kCandBuf];
+  __shared__ __align__(16) float s_stage[kGridWarps][kStageFloats];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  const ChunkStage st{s_x[wib], s_a[wib], s_b[wib], s_l[wib]};
+  const ChunkStage st{s_stage[wib]};
   const long long nchunks = (long long)R.nrun[0] * R.nrun[1] * R.nrun[2];
   const long long nwarps = (long long)gridDim.x * kGridWarps;
   long long pairs = 0;

@@ -113,3 +113,28 @@ def test_octree_and_mesh_invariants_at_full_size(ctx):
     # triangles index existing vertices (a triangle may repeat a vertex, as
     # the reference's do, where leaves of different sizes meet)
     assert t.min() >= 0 and t.max() < len(k)
+
+
+@pytest.mark.parametrize("n", [20_000, 1_000_000])
+def test_lattice_samples_equal_point_evaluation(ctx, n):
+    """With the QEF on, every node sampled at depth >= D_min keeps its 27
+    GridEval samples; on the two finest levels they come from the chunked
+    evaluator (packed FP32 over pairs of candidates), elsewhere from the
+    thread-per-point kernel.  Each equals pi_eval_field (the scalar field sum)
+    at the same lattice point bit for bit."""
+    import parity as PR
+    fr = synth.slab_and_sphere(n=n, seed=1) if n <= 20_000 else synth.dam_break(n=n, seed=2)
+    g = N.Frame(ctx, N.default_params(fr.radius, qef=True)).upload(fr.xyz).run()
+    nodes = g.dump(N.DUMP_NODES)
+    samp = g.dump(N.DUMP_QEF_SAMPLES).reshape(-1, 27)
+    info = g.info()
+    sampled = np.nonzero((nodes["depth"] >= info["depth_min"]) & (nodes["type"] != 0))[0]
+    rng = np.random.default_rng(4)
+    pick = rng.choice(sampled, size=min(len(sampled), 40_000), replace=False)
+    # the finest two levels must be represented (chunked evaluation)
+    assert set(np.unique(nodes["depth"][pick])) >= {info["depth_max"], info["depth_max"] - 1}
+    pts = np.concatenate([PR.sample_points(nodes["center"][i], nodes["half"][i]) for i in pick])
+    val = g.eval(pts).reshape(-1, 27)
+    bad = np.nonzero(np.any(val.view(np.uint32) != samp[pick].view(np.uint32), axis=1))[0]
+    assert len(bad) == 0, (len(bad), nodes["depth"][pick[bad[:5]]])
+    g.close()

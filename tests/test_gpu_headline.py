@@ -109,25 +109,29 @@ def _check_stages(fr, o, g):
 
 
 def _check_aniso_field(name, fr, o, g):
-    # anisotropy against the float oracle (reference semantics)
+    # anisotropy against the float oracle (reference semantics) and the FP64
+    # GPU oracle.  The float reference's own centres are a few float ulps off
+    # FP64 (coordinates up to ~3.5 here, so ~1e-6 absolute, the size of
+    # XMEAN_TOL * r); against it the bound is its own error plus ours.
     xm, G, det = o.aniso()
-    gx, gG, gd = g.dump(N.DUMP_XMEANS), g.dump(N.DUMP_G), g.dump(N.DUMP_DET)
-    assert np.abs(gx - xm).max() <= PR.XMEAN_TOL * fr.radius
+    gx, gG, gd = g.dump(N.DUMP_XMEANS), g.dump(N.DUMP_G).reshape(fr.n, 9), g.dump(N.DUMP_DET)
+    x64, G64, d64 = g.aniso_fp64()
+    assert np.all(np.abs(gx - xm) <= np.abs(xm - x64) + PR.XMEAN_TOL * fr.radius)
     assert np.abs(gG - G.reshape(len(G), -1)).max() <= PR.G_TOL
     assert np.abs(gd - det).max() <= PR.G_TOL
     no = o.normals()
     assert np.abs(g.dump(N.DUMP_NORMALS) - no).max() <= PR.NORMAL_TOL * np.abs(no).max()
-    # against the FP64 GPU oracle
-    x64, G64, d64 = g.aniso_fp64()
     eG = np.abs(gG - G64.reshape(len(G64), -1)).max(1)
+    exo = np.abs(xm - x64).max(1) / fr.radius
     eGo = np.abs(G.reshape(len(G), -1) - G64.reshape(len(G64), -1)).max(1)
     ed = np.abs(gd - d64)
     ex = np.abs(gx - x64).max(1) / fr.radius
     flags = g.dump(N.DUMP_FP64_FLAGS).astype(bool)
     print("%s: G vs FP64 max %.3e rms %.3e (FP32 eigen path max %.3e, FP64 path max %.3e, %d of %d particles); "
-          "float reference G vs FP64 max %.3e; det max %.3e; centres max %.3e r"
+          "float reference G vs FP64 max %.3e; det max %.3e; centres max %.3e r (float reference %.3e r)"
           % (name, eG.max(), np.sqrt(np.mean(eG ** 2)), eG[~flags].max() if (~flags).any() else 0.0,
-             eG[flags].max() if flags.any() else 0.0, int(flags.sum()), fr.n, eGo.max(), ed.max(), ex.max()))
+             eG[flags].max() if flags.any() else 0.0, int(flags.sum()), fr.n, eGo.max(), ed.max(), ex.max(),
+             exo.max()))
     assert eG.max() <= PR.G_TOL and ed.max() <= PR.G_TOL and ex.max() <= PR.XMEAN_TOL
     # field at points near the particles
     rng = np.random.default_rng(12)
@@ -207,15 +211,22 @@ def _check_qef_vertices(name, fr, o, g):
     mo = np.any(on["node"][io[lv], :3] != on["center"][io[lv]], axis=1)
     mg = moved[ig[lv]]
     only_here = int(np.sum(mg & ~mo))
-    only_ref = int(np.sum(mo & ~mg))
+    # leaves the reference's float inverse accepts and the library rejects:
+    # the FP64 solve of the same samples must reject them too (a float
+    # inverse of a matrix of condition ~1e20 can land inside the cell by
+    # accident)
+    ref_only = ig[lv][mo & ~mg]
+    only_ref = len(ref_only)
+    if only_ref:
+        _, ic, sg = PR.qef_solve_f64_batch(gn["center"][ref_only], gn["half"][ref_only], samp[ref_only])
+        assert not np.any(ic & ~sg), "leaves accepted by the reference and by the FP64 solve but not here
     print("%s QEF: accepted %d (singular %d) of %d leaves; vs FP64 solve of %d leaves: max %.3e rms %.3e (x r), "
           "decision differs %d; float reference accepts %d, accepted here and rejected by the reference %d, "
-          "accepted by the reference only %d"
+          "accepted by the reference only %d (all rejected by the FP64 solve)"
           % (name, len(acc_g), info["qef_singular"], len(leaves), len(pick), err.max() if len(err) else 0.0,
              np.sqrt(np.mean(err ** 2)) if len(err) else 0.0, disagree, int(mo.sum()), only_here, only_ref))
     assert len(err) > 20 and err.max() <= PR.QEF_VERT_TOL
     assert disagree <= max(2, len(pick) // 1000)
-    assert only_ref <= max(2, int(mo.sum()) // 1000)
     assert only_here == int(mg.sum()) - int(np.sum(mg & mo))
 
 
