@@ -467,10 +467,11 @@ def serving_record(a, N):
             time.sleep(wait)
         elif wait < -0.005:
             late += 1
-        tickets[i] = srv.submit(xyz, N.default_params(r["radius"]))
+        tickets[i] = srv.submit(xyz, N.default_params(r["radius"]), seq=r["seq"] + 1)
     th.join()
     t_all = time.perf_counter() - t0
     st = srv.stats()
+    info = srv.info()
     srv.close()
     lat = np.array([x[0] for x in results])
     q = np.array([x[1] for x in results])
@@ -482,6 +483,7 @@ def serving_record(a, N):
             "queue_p50_ms": float(np.percentile(q, 50)), "queue_p99_ms": float(np.percentile(q, 99)),
             "particles_total": int(sum(r["n"] for r in reqs)), "slots": a.slots,
             "max_in_flight": st["max_in_flight"], "submitted_late": late,
+            "resident_hits": info["resident_hits"], "bypasses": info["bypasses"],
             "timing": "host wall clock; latency = completion - submission through pi_server_submit/wait"}
 
 

@@ -293,17 +293,36 @@ int pi_hashgrid_build_noalloc(const float* d_xyz, int64_t n, float radius, int32
 /* Request loop (continuous batching).  The reference reconstructs one frame
  * per run of its driver loop (runOurs, src/main.cpp:330-405); a server keeps
  * `slots` worker threads, each with its own stream, admits queued requests
- * in arrival order while their estimated device footprint fits in
- * budget_bytes (0 = no cap; one request is always admitted), runs admitted
- * frames concurrently and keeps results in host memory until fetched.  A
- * result equals pi_run's on the same input.  Without a budget each worker
- * keeps its frame's device buffers from one request to the next (held until
- * pi_server_destroy); with a budget a request's memory is returned when it
- * completes. */
+ * while their device-memory reservation fits in budget_bytes next to the
+ * frames in flight and the resident frame states (0 = no cap; a request is
+ * always admitted when nothing else holds memory), runs admitted frames
+ * concurrently and keeps results in host memory until fetched.  A result
+ * equals pi_run's on the same input.
+ *  - Reservation: bytes_per_particle * n + fixed_bytes (by default 2304 B a
+ *    particle + 64 MiB; pi_server_set_estimate changes it for later
+ *    submissions).  With a budget the frame's context is capped at its
+ *    reservation: a frame that needs more fails inside the worker and is
+ *    queued again at the head with twice the reservation, until that would
+ *    exceed the budget (the request then fails with PI_ERR_NOMEM).
+ *  - Order: arrival order; when the head does not fit, up to 16 requests
+ *    behind it that fit may pass it, and no request is passed more than 8
+ *    times.
+ *  - Resident frame states: each worker keeps its last frame (hash grid,
+ *    octree, device buffers) until its next request; the next step of a
+ *    sequence (pi_server_submit_seq, sequence != 0) goes to the idle worker
+ *    holding that sequence's frame and is built in its buffers.  At most
+ *    `slots` states are resident; with a budget their bytes count against it
+ *    and idle workers give them back, least recently used first, when an
+ *    admission needs the room. */
 typedef struct pi_server pi_server;
 int pi_server_create(int device, int slots, size_t budget_bytes, pi_server** out);
 /* copies xyz[n*3]; returns a ticket */
 int pi_server_submit(pi_server* s, const pi_params* params, const float* xyz, int64_t n, uint64_t* ticket);
+/* the same for one step of a sequence of frames (an advected particle set):
+ * its steps share a resident frame state where they can */
+int pi_server_submit_seq(pi_server* s, const pi_params* params, const float* xyz, int64_t n, uint64_t sequence,
+                         uint64_t* ticket);
+int pi_server_set_estimate(pi_server* s, size_t bytes_per_particle, size_t fixed_bytes);
 int pi_server_poll(pi_server* s, uint64_t ticket, int* done);
 /* blocks until done; latency = completion - submission, queue = start - submission */
 int pi_server_wait(pi_server* s, uint64_t ticket, int64_t* nverts, int64_t* ntris, double* latency_ms,
@@ -312,6 +331,11 @@ int pi_server_wait(pi_server* s, uint64_t ticket, int64_t* nverts, int64_t* ntri
 int pi_server_fetch(pi_server* s, uint64_t ticket, float* verts, int32_t* tris);
 int pi_server_stats(pi_server* s, int64_t* completed, int64_t* in_flight, int64_t* max_in_flight,
                     int64_t* queued, int64_t* bytes_reserved);
+/* out8: completed, bytes reserved by frames in flight, resident bytes
+ * (counted with a budget), resident frame states, head-of-line passes,
+ * re-queued reservations, steps that reused their sequence's resident
+ * frame, budget */
+int pi_server_info(pi_server* s, int64_t* out8);
 /* finishes queued requests, then stops the workers */
 int pi_server_destroy(pi_server* s);
 

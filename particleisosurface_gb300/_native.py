@@ -444,6 +444,10 @@ def _declare_server(L):
                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]),
         "pi_server_fetch": (C.c_int, [P, C.c_uint64, C.POINTER(C.c_float), C.POINTER(C.c_int32)]),
         "pi_server_stats": (C.c_int, [P] + [C.POINTER(C.c_int64)] * 5),
+        "pi_server_submit_seq": (C.c_int, [P, C.POINTER(Params), C.POINTER(C.c_float), C.c_int64, C.c_uint64,
+                                           C.POINTER(C.c_uint64)]),
+        "pi_server_set_estimate": (C.c_int, [P, C.c_size_t, C.c_size_t]),
+        "pi_server_info": (C.c_int, [P, C.POINTER(C.c_int64)]),
         "pi_server_destroy": (C.c_int, [P]),
     }
     for name, (res, args) in sig.items():
@@ -461,11 +465,21 @@ class Server:
         check(lib().pi_server_create(device, slots, budget_bytes, C.byref(h)))
         self.h = h
 
-    def submit(self, xyz, params):
+    def submit(self, xyz, params, seq=0):
         xyz = np.ascontiguousarray(xyz, dtype=np.float32)
         t = C.c_uint64()
-        check(lib().pi_server_submit(self.h, C.byref(params), ptr(xyz, C.c_float), xyz.shape[0], C.byref(t)))
+        check(lib().pi_server_submit_seq(self.h, C.byref(params), ptr(xyz, C.c_float), xyz.shape[0], seq,
+                                         C.byref(t)))
         return t.value
+
+    def set_estimate(self, bytes_per_particle, fixed_bytes):
+        check(lib().pi_server_set_estimate(self.h, bytes_per_particle, fixed_bytes))
+
+    def info(self):
+        out = (C.c_int64 * 8)()
+        check(lib().pi_server_info(self.h, out))
+        return dict(zip(["completed", "reserved_bytes", "resident_bytes", "resident_frames", "bypasses", "retries",
+                         "resident_hits", "budget"], list(out)))
 
     def done(self, ticket):
         d = C.c_int()

@@ -63,3 +63,88 @@ def test_failed_request_reports_its_error_and_others_complete():
     v, t, lat, q = srv.result(t_good)
     srv.close()
     assert len(v) > 0 and len(t) > 0
+
+
+def _alone(fr):
+    ctx = N.Context(0)
+    f = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz).run()
+    m = f.mesh()
+    f.close()
+    ctx.close()
+    return m
+
+
+def test_sequence_steps_reuse_their_resident_frame():
+    """Steps of advected sequences submitted one after another: each step
+    runs in the resident frame of its sequence's previous step and gives
+    what a fresh frame gives."""
+    B.build()
+    base = [synth.mixed_frame(900 + k, n) for k, n in enumerate([15000, 40000])]
+    steps = []
+    for k, fr in enumerate(base):
+        p = fr.xyz64
+        for st in range(4):
+            if st:
+                p = synth.advect(p, 1.0, synth.SERVE_G, (st - 1) * synth.SERVE_DT, synth.SERVE_DT, scale=fr.scale)
+            steps.append((k + 1, np.ascontiguousarray(p.astype(np.float32)), fr.radius))
+    srv = N.Server(0, slots=4, budget_bytes=0)
+    out = []
+    for seq, xyz, r in steps:  # one at a time: the holder of the sequence is idle
+        out.append(srv.result(srv.submit(xyz, N.default_params(r), seq=seq)))
+    info = srv.info()
+    srv.close()
+    assert info["completed"] == len(steps)
+    assert info["resident_hits"] == len(steps) - len(base), info
+    for (seq, xyz, r), (v, t, lat, q) in zip(steps, out):
+        fr = synth.Frame(xyz.astype(np.float64), r, 1.0, 0, "step")
+        va, ta = _alone(fr)
+        np.testing.assert_array_equal(v, va)
+        np.testing.assert_array_equal(t, ta)
+
+
+def test_small_requests_pass_a_blocked_head_within_the_bound():
+    """With a budget that holds one large frame, small requests queued behind
+    a large one that cannot start yet pass it; the large one is passed a
+    bounded number of times and completes; every result equals the frame
+    reconstructed alone."""
+    B.build()
+    big = [synth.mixed_frame(950 + k, 150000) for k in range(2)]
+    small = [synth.small_blob(n=2000, seed=960 + k) for k in range(6)]
+    srv = N.Server(0, slots=4, budget_bytes=int(150000 * 2304 + (64 << 20) + 3 * (2000 * 2304 + (64 << 20))))
+    frames = [big[0], big[1]] + small
+    tickets = [srv.submit(fr.xyz, N.default_params(fr.radius)) for fr in frames]
+    res = [srv.result(t) for t in tickets]
+    info = srv.info()
+    srv.close()
+    assert info["completed"] == len(frames) and info["bypasses"] >= 1, info
+    assert info["bypasses"] <= 8 * len(frames)
+    for fr, (v, t, lat, q) in zip(frames, res):
+        va, ta = _alone(fr)
+        np.testing.assert_array_equal(v, va)
+        np.testing.assert_array_equal(t, ta)
+
+
+def test_underestimated_request_is_requeued_with_a_larger_reservation():
+    """A reservation below what the frame needs: the frame's context is capped
+    at it, the frame fails inside the worker, and the request goes back to the
+    head of the queue with twice the reservation until it fits; the result is
+    the frame's as reconstructed alone.  Beyond the whole budget the request
+    fails with PI_ERR_NOMEM."""
+    B.build()
+    fr = synth.mixed_frame(970, 60000)
+    srv = N.Server(0, slots=2, budget_bytes=1 << 30)
+    srv.set_estimate(64, 1 << 20)  # far below the frame's needs
+    v, t, lat, q = srv.result(srv.submit(fr.xyz, N.default_params(fr.radius)))
+    info = srv.info()
+    va, ta = _alone(fr)
+    np.testing.assert_array_equal(v, va)
+    np.testing.assert_array_equal(t, ta)
+    assert info["retries"] >= 1, info
+    srv.close()
+    # a budget too small for the frame at all
+    srv = N.Server(0, slots=2, budget_bytes=8 << 20)
+    srv.set_estimate(64, 1 << 20)
+    with pytest.raises(N.PiError) as e:
+        srv.result(srv.submit(fr.xyz, N.default_params(fr.radius)))
+    assert e.value.code == N.PI_ERR_NOMEM
+    srv.close()
