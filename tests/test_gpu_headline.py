@@ -219,7 +219,7 @@ def _check_qef_vertices(name, fr, o, g):
     only_ref = len(ref_only)
     if only_ref:
         _, ic, sg = PR.qef_solve_f64_batch(gn["center"][ref_only], gn["half"][ref_only], samp[ref_only])
-        assert not np.any(ic & ~sg), "leaves accepted by the reference and by the FP64 solve but not here
+        assert not np.any(ic & ~sg), "leaves accepted by the reference and by the FP64 solve but not here"
     print("%s QEF: accepted %d (singular %d) of %d leaves; vs FP64 solve of %d leaves: max %.3e rms %.3e (x r), "
           "decision differs %d; float reference accepts %d, accepted here and rejected by the reference %d, "
           "accepted by the reference only %d (all rejected by the FP64 solve)"
