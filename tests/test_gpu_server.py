@@ -39,8 +39,9 @@ def test_results_same_alone_and_in_the_mix():
 def test_budget_admission_serialises_large_requests():
     B.build()
     frames = [synth.mixed_frame(800 + k, 40000) for k in range(4)]
-    # a budget below two frames' estimates admits one frame at a time
-    srv = N.Server(0, slots=4, budget_bytes=100 << 20)
+    # a budget below two frames' reservations admits one frame at a time
+    # (reservation 40000 * 3072 B + 128 MiB each)
+    srv = N.Server(0, slots=4, budget_bytes=400 << 20)
     tickets = [srv.submit(fr.xyz, N.default_params(fr.radius)) for fr in frames]
     for t in tickets:
         srv.result(t)
@@ -110,7 +111,8 @@ def test_small_requests_pass_a_blocked_head_within_the_bound():
     B.build()
     big = [synth.mixed_frame(950 + k, 150000) for k in range(2)]
     small = [synth.small_blob(n=2000, seed=960 + k) for k in range(6)]
-    srv = N.Server(0, slots=4, budget_bytes=int(150000 * 2304 + (64 << 20) + 3 * (2000 * 2304 + (64 << 20))))
+    est = lambda n: n * 3072 + (128 << 20)  # the default reservation
+    srv = N.Server(0, slots=4, budget_bytes=int(est(150000) + 3 * est(2000)))
     frames = [big[0], big[1]] + small
     tickets = [srv.submit(fr.xyz, N.default_params(fr.radius)) for fr in frames]
     res = [srv.result(t) for t in tickets]
