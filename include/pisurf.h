@@ -79,6 +79,9 @@ typedef struct pi_frame_info {
   int64_t field_evals_performed; /* evaluations the kernels performed: distinct sample
                                     points (shared lattice points once), leaf values,
                                     QEF vertices, bisection midpoints */
+  int32_t num_grids;        /* hash grids: 1, or the non-empty radius bins (per-particle radii) */
+  float radius_min, radius_max; /* the radius, or the searcher's min / max radius
+                                   (smallest * 0.99, largest * 1.01) */
 } pi_frame_info;
 
 /* Parity dumps (pi_stage_dump).  Arrays are in original particle order unless
@@ -93,6 +96,7 @@ typedef struct pi_frame_info {
 #define PI_DUMP_NODES 8       /* pi_node[num_nodes], creation (level) order */
 #define PI_DUMP_FP64_FLAGS 9  /* int8[N] 1 where the eigen step ran in FP64 */
 #define PI_DUMP_QEF_SAMPLES 10 /* float[num_nodes*27] GridEval sample values (qef mode) */
+#define PI_DUMP_GRID_OF 11    /* int32[N]  hash grid (radius bin) of each particle */
 
 typedef struct pi_node {
   uint64_t id;      /* TNode::id */
@@ -152,6 +156,26 @@ int pi_frame_create(pi_ctx* ctx, const pi_params* params, pi_frame** out);
 int pi_frame_destroy(pi_frame* f);
 int pi_frame_upload(pi_frame* f, const float* xyz, int64_t n);        /* host xyz[n*3] */
 int pi_frame_upload_device(pi_frame* f, const float* d_xyz, int64_t n); /* device xyz[n*3] */
+/* Per-particle radii (radii[n], n = the particle count): the reference's
+ * variable-radius SurfReconstructor (IS_CONST_RADIUS false) with its
+ * neighbour query switched on.  Particles are binned by radius into bins of
+ * about half the smallest radius (MultiLevelSearcher,
+ * src/multi_level_reseacher.cpp:6-77), one hash grid per non-empty bin with
+ * the bin's largest radius times 4 as its cell; a point's candidates are
+ * the bins' 27-cell lists in bin order; each particle's kernel uses its own
+ * radius (src/evaluator.cpp:16-29); the root box and depths follow
+ * resizeRootBoxVarR (src/surface_reconstructor.cpp:124-149), a node is a
+ * leaf by size when it is no larger than the smallest radius reaching it,
+ * and the bisection stops at half the searcher's smallest radius.  The
+ * radius of pi_params is not used.  The per-particle radii stay with the
+ * frame until the next upload; not available with them: the QEF
+ * (PI_ERR_INVALID), the uniform grid, pi_hashgrid_in_box and the FP64 oracle
+ * (PI_ERR_STATE).  pi_frame_grid describes hash grid k (the grid's cells
+ * start at offset_base in PI_DUMP_CELL_OFFSETS; radius_id is the particle
+ * whose radius sets its cell, -1 for a constant radius). */
+int pi_frame_upload_radii(pi_frame* f, const float* radii, int64_t n);
+int pi_frame_grid(const pi_frame* f, int32_t k, float* bounding6, int32_t* dims3, float* cell_size, int64_t* count,
+                  int64_t* offset_base, int32_t* radius_id);
 /* Keeps the uploaded particles on the device and discards every later stage,
  * so pi_run reconstructs the same frame again (a new Run on resident input). */
 int pi_frame_reset(pi_frame* f);
@@ -298,12 +322,13 @@ int pi_hashgrid_build_noalloc(const float* d_xyz, int64_t n, float radius, int32
  * always admitted when nothing else holds memory), runs admitted frames
  * concurrently and keeps results in host memory until fetched.  A result
  * equals pi_run's on the same input.
- *  - Reservation: bytes_per_particle * n + fixed_bytes (by default 2304 B a
- *    particle + 64 MiB; pi_server_set_estimate changes it for later
+ *  - Reservation: bytes_per_particle * n + fixed_bytes (by default 3072 B a
+ *    particle + 128 MiB; pi_server_set_estimate changes it for later
  *    submissions).  With a budget the frame's context is capped at its
- *    reservation: a frame that needs more fails inside the worker and is
- *    queued again at the head with twice the reservation, until that would
- *    exceed the budget (the request then fails with PI_ERR_NOMEM).
+ *    reservation (at most the budget): a frame that needs more fails inside
+ *    the worker and is queued again at the head with twice the reservation,
+ *    up to the whole budget; a frame that needs more than the whole budget
+ *    fails with PI_ERR_NOMEM.
  *  - Order: arrival order; when the head does not fit, up to 16 requests
  *    behind it that fit may pass it, and no request is passed more than 8
  *    times.

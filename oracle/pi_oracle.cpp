@@ -88,6 +88,12 @@ struct HashGrid {
   std::vector<int> IndexList;
   std::vector<long long> Keys;  // per particle, kept for dumps
   std::map<long long, int> StartList, EndList;
+  // variable radius: one grid per radius bin over the bin's particles
+  // (src/hash_grid.cpp:36-69); indices below are bin-local, PIndexes maps
+  // them to particles
+  bool var = false;
+  std::vector<int> PIndexes;
+  int RadiusId = -1;
 
   // src/hash_grid.cpp:4-34
   void init(const std::vector<F3>* particles, const float* bounding, float radius,
@@ -98,6 +104,34 @@ struct HashGrid {
     CellSize = radius * inf_factor;
     for (int i = 0; i < 3; ++i) {
       float length = (std::ceil((bounding[i * 2 + 1] - bounding[i * 2]) / CellSize)) * CellSize;
+      float center = (bounding[i * 2] + bounding[i * 2 + 1]) / 2;
+      Bounding[i * 2] = center - length / 2;
+      Bounding[i * 2 + 1] = center + length / 2;
+    }
+    for (int i = 0; i < 3; ++i)
+      XYZCellNum[i] =
+          std::max(int(std::ceil((Bounding[i * 2 + 1] - Bounding[i * 2]) / CellSize)), 1);
+    CellNum = (long long)XYZCellNum[0] * (long long)XYZCellNum[1] * (long long)XYZCellNum[2];
+    HashList.assign(ParticlesNum, 0);
+    IndexList.assign(ParticlesNum, 0);
+    BuildTable(std_sort);
+    HashList.clear();
+  }
+
+  // src/hash_grid.cpp:36-69: the grid of one radius bin; the cell size is
+  // the bin's largest radius times inf_factor, over the bin's bounding box
+  void init_var(const std::vector<F3>* particles, const std::vector<float>& radiuses,
+                const std::vector<int>& pIndexes, const float* bounding, int radiusId, float inf_factor,
+                bool std_sort) {
+    var = true;
+    Particles = particles;
+    PIndexes = pIndexes;
+    ParticlesNum = (unsigned int)PIndexes.size();
+    RadiusId = radiusId;
+    Radius = radiuses[radiusId];
+    CellSize = Radius * inf_factor;
+    for (int i = 0; i < 3; ++i) {
+      float length = ((std::ceil((bounding[i * 2 + 1] - bounding[i * 2]) / CellSize)) * CellSize);
       float center = (bounding[i * 2] + bounding[i * 2 + 1]) / 2;
       Bounding[i * 2] = center - length / 2;
       Bounding[i * 2 + 1] = center + length / 2;
@@ -132,7 +166,7 @@ struct HashGrid {
   void CalcHashList() {
     int xyz[3];
     for (size_t index = 0; index < ParticlesNum; index++) {
-      CalcXYZIdx((*Particles)[index].data(), xyz);
+      CalcXYZIdx((*Particles)[var ? PIndexes[index] : index].data(), xyz);
       HashList[index] = CalcCellHash(xyz);
       IndexList[index] = (int)index;
     }
@@ -180,7 +214,7 @@ struct HashGrid {
     } else {
       return;
     }
-    for (int c = startIndex; c < endIndex; c++) out.push_back(IndexList[c]);
+    for (int c = startIndex; c < endIndex; c++) out.push_back(var ? PIndexes[IndexList[c]] : IndexList[c]);
   }
 
   // src/hash_grid.cpp:164-194 (x outer, z inner)
@@ -214,6 +248,73 @@ struct HashGrid {
           if (h < 0) continue;
           GetInCellList(h, out);
         }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// MultiLevelSearcher (src/multi_level_reseacher.cpp:6-117): particles binned
+// by radius into bins of width about minRadius / 2, a HashGrid per non-empty
+// bin.  GetNeighbors is the reference's with its query switched on.  Two
+// departures where the reference's dead code is broken: it indexes its
+// searcher list with the bin index, which picks the wrong grid once an
+// earlier bin is empty (its GetInBoxParticles keeps a separate searcher
+// counter), and its GetInBoxParticles maps the grid's answers, which are
+// already particle indices (HashGrid::GetInCellList, src/hash_grid.cpp:
+// 155-160), through the bin's index list a second time.  Here each non-empty
+// bin's grid is queried in bin order and its particle indices are kept.
+// ---------------------------------------------------------------------------
+struct MultiLevelSearcher {
+  float maxRadius = 0, minRadius = 0, avgRadius = 0;
+  std::vector<std::vector<int>> sortedIndex;
+  std::vector<HashGrid> searchers;  // one per non-empty bin, in bin order
+
+  void init(const std::vector<F3>* particles, const std::vector<float>& radiuses, float inf_factor,
+            bool std_sort) {
+    maxRadius = *std::max_element(radiuses.begin(), radiuses.end()) * 1.01;
+    minRadius = *std::min_element(radiuses.begin(), radiuses.end()) * 0.99;
+    std::vector<std::pair<float, float>> bin_bounds;
+    float bin_extent = minRadius * 0.5;
+    int bins = std::max(int(std::ceil((maxRadius - minRadius) / bin_extent)), 1);
+    bin_extent = (maxRadius - minRadius) / bins;
+    for (int i = 0; i < bins; i++)
+      bin_bounds.push_back({minRadius + (i * bin_extent), std::min(minRadius + ((i + 1) * bin_extent), maxRadius)});
+    auto whichBin = [&](const float r) {
+      for (size_t k = 0; k < bin_bounds.size(); ++k)
+        if (r >= bin_bounds[k].first && r <= bin_bounds[k].second) return (int)k;
+      return -1;
+    };
+    sortedIndex.assign(bins, {});
+    avgRadius = 0;
+    for (size_t i = 0; i < radiuses.size(); i++) {
+      sortedIndex[whichBin(radiuses[i])].push_back((int)i);
+      avgRadius += radiuses[i];
+    }
+    avgRadius /= radiuses.size();
+    if (avgRadius < minRadius) avgRadius = minRadius;
+    if (avgRadius > maxRadius) avgRadius = maxRadius;
+    searchers.clear();
+    for (int i = 0; i < bins; i++) {
+      if (sortedIndex[i].empty()) continue;
+      float b[6] = {FLT_MAX, -FLT_MAX, FLT_MAX, -FLT_MAX, FLT_MAX, -FLT_MAX};
+      for (int pI : sortedIndex[i])
+        for (int k = 0; k < 3; ++k) {
+          if ((*particles)[pI][k] < b[2 * k]) b[2 * k] = (*particles)[pI][k];
+          if ((*particles)[pI][k] > b[2 * k + 1]) b[2 * k + 1] = (*particles)[pI][k];
+        }
+      // the bin's largest radius (std::max_element: the first of equal maxima)
+      int rid = *std::max_element(sortedIndex[i].begin(), sortedIndex[i].end(),
+                                  [&](int a, int c) { return radiuses[a] < radiuses[c]; });
+      searchers.emplace_back();
+      searchers.back().init_var(particles, radiuses, sortedIndex[i], b, rid, inf_factor, std_sort);
+    }
+  }
+
+  void GetNeighbors(const float* pos, std::vector<int>& out) {
+    for (HashGrid& g : searchers) g.GetPIdxList(pos, out);
+  }
+
+  void GetInBoxParticles(const F3& box1, const F3& box2, std::vector<int>& insides) {
+    for (HashGrid& g : searchers) g.GetInBoxParticles(box1, box2, insides);
   }
 };
 
@@ -411,6 +512,18 @@ static void inv4(const R a[4][4], R out[4][4]) {
 template <class R>
 struct Evaluator {
   HashGrid* grid = nullptr;
+  MultiLevelSearcher* searcher = nullptr;  // variable radius (grid unused)
+  const std::vector<float>* GlobalRadius = nullptr;
+  std::vector<R> GlobalInflunce2, GlobalSigma;
+  void neighbors(const float* p, std::vector<int>& out) {
+    if (searcher)
+      searcher->GetNeighbors(p, out);
+    else
+      grid->GetPIdxList(p, out);
+  }
+  R influ2(int j) const { return searcher ? GlobalInflunce2[j] : Influnce2; }
+  R sigma(int j) const { return searcher ? GlobalSigma[j] : Sigma; }
+  R rad(int j) const { return searcher ? (R)(*GlobalRadius)[j] : Radius; }
   const std::vector<F3>* P = nullptr;
   int N = 0;
   float _NEIGHBOR_FACTOR = 4.0f;
@@ -439,6 +552,21 @@ struct Evaluator {
       Sigma = (R)(1 / std::pow((double)(radius * _SMOOTH_FACTOR), 6));
     }
     _XMEAN_DELTA = (float)0.9;
+    if (searcher) {
+      // src/evaluator.cpp:16-29: per particle, from that particle's radius
+      GlobalInflunce2.resize(N);
+      GlobalSigma.resize(N);
+      for (int i = 0; i < N; ++i) {
+        const float smooth = (*GlobalRadius)[i] * _SMOOTH_FACTOR;
+        if (sizeof(R) == sizeof(float)) {
+          GlobalInflunce2[i] = (R)(float)std::pow(smooth, 2);
+          GlobalSigma[i] = (R)(float)(1 / std::pow(smooth, 6));
+        } else {
+          GlobalInflunce2[i] = (R)std::pow((double)smooth, 2);
+          GlobalSigma[i] = (R)(1 / std::pow((double)smooth, 6));
+        }
+      }
+    }
     Normals.assign(N, V3<R>{{0, 0, 0}});
     xMeans.resize(N);
     Gs.resize(N);
@@ -478,8 +606,8 @@ struct Evaluator {
   // src/evaluator.cpp:437-453
   R AnisotropicInterpolate(int j, const V3<R>& diff) const {
     V3<R> gd = matvec(Gs[j], diff);
-    R ratio = std::sqrt(sqnorm3<R>(gd[0], gd[1], gd[2]) / Influnce2);
-    R k = Bspline_kernel(ratio, Sigma);
+    R ratio = std::sqrt(sqnorm3<R>(gd[0], gd[1], gd[2]) / influ2(j));
+    R k = Bspline_kernel(ratio, sigma(j));
     return Dets[j] * k;
   }
 
@@ -487,10 +615,10 @@ struct Evaluator {
   V3<R> AnisotropicInterpolateGrad(int j, const V3<R>& diff) const {
     V3<R> gd = matvec(Gs[j], diff);
     R d2 = sqnorm3<R>(gd[0], gd[1], gd[2]);
-    R h2 = Influnce2;
+    R h2 = influ2(j);
     V3<R> g;
     for (int k = 0; k < 3; ++k)
-      g[k] = Sigma * (-6 * gd[k]) * (d2 > h2 ? (R)0.0f : ((h2 - d2) * (h2 - d2)));
+      g[k] = sigma(j) * (-6 * gd[k]) * (d2 > h2 ? (R)0.0f : ((h2 - d2) * (h2 - d2)));
     for (int k = 0; k < 3; ++k) g[k] = Dets[j] * g[k];
     return g;
   }
@@ -499,7 +627,7 @@ struct Evaluator {
   R SingleEval(const float* p) {
     R scalar = 0;
     std::vector<int> nb;
-    grid->GetPIdxList(p, nb);
+    neighbors(p, nb);
     V3<R> q{{(R)p[0], (R)p[1], (R)p[2]}};
     for (int j : nb) {
       V3<R> diff{{q[0] - xMeans[j][0], q[1] - xMeans[j][1], q[2] - xMeans[j][2]}};
@@ -517,7 +645,7 @@ struct Evaluator {
       grad = V3<R>{{0, 0, 0}};
     }
     std::vector<int> nb;
-    grid->GetPIdxList(p, nb);
+    neighbors(p, nb);
     V3<R> q{{(R)p[0], (R)p[1], (R)p[2]}};
     for (int j : nb) {
       V3<R> diff{{q[0] - xMeans[j][0], q[1] - xMeans[j][1], q[2] - xMeans[j][2]}};
@@ -535,7 +663,7 @@ struct Evaluator {
     V3<R> pp = pos(p);
     for (int n : temp) {
       if (n == p) continue;
-      R nR = Radius;
+      R nR = rad(n);
       R nD = (R)(_SMOOTH_FACTOR * (double)nR * 1.6);
       R nD2 = nD * nD;
       R nI = nR * (R)_NEIGHBOR_FACTOR;
@@ -569,9 +697,9 @@ struct Evaluator {
     R wSum = 0;
     M3<R> cov;
     for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) cov(i, j) = (i == j) ? Influnce2 : (R)0;
+      for (int j = 0; j < 3; ++j) cov(i, j) = (i == j) ? influ2(p) : (R)0;
     for (int n : nb) {
-      R nR = Radius;
+      R nR = rad(n);
       R nI = nR * (R)_NEIGHBOR_FACTOR;
       R nI2 = nI * nI;
       const V3<R>& xn = xMeans[n];
@@ -622,7 +750,7 @@ struct Evaluator {
       std::vector<int> temp;
       int nn = 0;
       V3<R> xMean{{0, 0, 0}};
-      grid->GetPIdxList((*P)[p].data(), temp);
+      neighbors((*P)[p].data(), temp);
       if (temp.size() <= 2) {
         xMeans[p] = pos(p);
         continue;
@@ -634,7 +762,7 @@ struct Evaluator {
     for (int p = 0; p < N; p++) {
       std::vector<int> temp;
       M3<R> G;
-      grid->GetPIdxList((*P)[p].data(), temp);
+      neighbors((*P)[p].data(), temp);
       compute_G_Yus(p, xMeans[p], temp, G);
       Gs[p] = G;
       Dets[p] = det3<R>(G);
@@ -655,6 +783,35 @@ struct Evaluator {
 
   // src/evaluator.cpp:323-335
   void RecommendIsoValueConstR() { _ISO_VALUE = Bspline_kernel((R)0.01, Sigma); }
+
+  // src/evaluator.cpp:293-321: the largest MaxScalar over the searchers'
+  // radius particles
+  void CalculateMaxScalarVarR() {
+    const float sqrt2 = 1.4142135623730950488016887242097f;
+    const float sqrt3 = 1.7320508075688772935274463415059f;
+    R mx = 0;
+    for (const HashGrid& g : searcher->searchers) {
+      const R sg = GlobalSigma[g.RadiusId];
+      R k = 0;
+      k += Bspline_kernel(0.0, sg);
+      k += Bspline_kernel(1.0, sg) * 6;
+      k += Bspline_kernel(sizeof(R) == sizeof(float) ? (R)sqrt2 : (R)1.4142135623730950488, sg) * 12;
+      k += Bspline_kernel(sizeof(R) == sizeof(float) ? (R)sqrt3 : (R)1.7320508075688772935, sg) * 8;
+      if (k > mx) mx = k;
+    }
+    _MAX_SCALAR = mx;
+  }
+
+  // src/evaluator.cpp:337-361: the largest Bspline_kernel(0.25) over the
+  // searchers' radius particles
+  void RecommendIsoValueVarR() {
+    R rec = 0;
+    for (const HashGrid& g : searcher->searchers) {
+      const R v = Bspline_kernel((R)0.25, GlobalSigma[g.RadiusId]);
+      if (v > rec) rec = v;
+    }
+    _ISO_VALUE = rec;
+  }
 
   // src/evaluator.cpp:363-375
   void CalcParticlesNormal() {
@@ -709,6 +866,11 @@ struct FrameBase {
   int stage_done = 0;
   double seconds[6] = {0, 0, 0, 0, 0, 0};
   HashGrid grid;
+  // variable radius (SurfReconstructor with per-particle radii): the radii
+  // and the multi-level searcher in place of the grid
+  bool varR = false;
+  std::vector<float> radii;
+  MultiLevelSearcher searcher;
   float BoundingBox[6];
   float RawBox[6];  // loadRootBox's box before resizeRootBoxConstR (UniformGrid reads it)
   bool single_layer = false;
@@ -783,25 +945,55 @@ struct Frame : FrameBase {
     DEPTH_MIN = (DEPTH_MAX - (single_layer ? 1 : 3));
   }
 
-  // src/surface_reconstructor.cpp:152-222
-  void checkEmptyAndCalcCurv(TNode<R>& t, unsigned char& empty, R& curv) {
+  // src/surface_reconstructor.cpp:124-149
+  void resizeRootBoxVarR() {
+    const float minR = searcher.minRadius, maxR = searcher.maxRadius;
+    float maxLen = std::max({(BoundingBox[1] - BoundingBox[0]), (BoundingBox[3] - BoundingBox[2]),
+                             (BoundingBox[5] - BoundingBox[4])});
+    const float cells = std::ceil(maxLen / minR);
+    DEPTH_MAX = cells >= 1.0f ? int(std::ceil(std::log2(cells))) : 0;
+    float resizeLen = (float)(std::pow(2, DEPTH_MAX) * minR);
+    while (resizeLen - maxLen < (ev._NEIGHBOR_FACTOR * maxR * 2)) {
+      DEPTH_MAX++;
+      resizeLen = (float)(std::pow(2, DEPTH_MAX) * minR);
+    }
+    RootHalfLength = resizeLen / 2;
+    for (int i = 0; i < 3; i++) {
+      float center = (BoundingBox[i * 2] + BoundingBox[i * 2 + 1]) / 2;
+      BoundingBox[i * 2] = center - RootHalfLength;
+      BoundingBox[i * 2 + 1] = center + RootHalfLength;
+      RootCenter[i] = center;
+    }
+    const float cmax = std::ceil(maxLen / maxR);
+    const int dmaxr = cmax >= 1.0f ? int(std::ceil(std::log2(cmax))) : 0;
+    DEPTH_MIN = std::min(dmaxr - 1, DEPTH_MAX - 2);
+  }
+
+  // src/surface_reconstructor.cpp:152-222.  min_radius: the smallest radius
+  // of the particles inside the grown box (variable radius), else the radius
+  void checkEmptyAndCalcCurv(TNode<R>& t, unsigned char& empty, R& curv, float& min_radius) {
     V3<R> norms{{0, 0, 0}};
     R area = 0;
     std::vector<int> insides;
+    min_radius = varR ? FLT_MAX : radius;
     F3 box1 = {t.center[0] - t.half_length, t.center[1] - t.half_length, t.center[2] - t.half_length};
     F3 box2 = {t.center[0] + t.half_length, t.center[1] + t.half_length, t.center[2] + t.half_length};
-    grid.GetInBoxParticles(box1, box2, insides);
+    if (varR)
+      searcher.GetInBoxParticles(box1, box2, insides);
+    else
+      grid.GetInBoxParticles(box1, box2, insides);
     empty = insides.empty();
     if (!empty) {
       bool all_splash = true;
-      const float e = radius * ev._SMOOTH_FACTOR;
       for (const int& in : insides) {
+        const float e = (varR ? radii[in] : radius) * ev._SMOOTH_FACTOR;
         const F3& p = P[in];
         if (p[0] > (box1[0] - e) && p[0] < (box2[0] + e) && p[1] > (box1[1] - e) &&
             p[1] < (box2[1] + e) && p[2] > (box1[2] - e) && p[2] < (box2[2] + e)) {
           const V3<R>& n = ev.Normals[in];
           for (int k = 0; k < 3; ++k) norms[k] += n[k];
           area += std::sqrt(sqnorm3<R>(n[0], n[1], n[2]));
+          if (varR && min_radius > radii[in]) min_radius = radii[in];
           all_splash = false;
         }
       }
@@ -919,7 +1111,7 @@ struct Frame : FrameBase {
   }
 
   // src/surface_reconstructor.cpp:237-273
-  void afterSampleEval(TNode<R>& t, R curv, float* sp, R* vals, R* grads) {
+  void afterSampleEval(TNode<R>& t, R curv, float min_radius, float* sp, R* vals, R* grads) {
     const bool qef = (flags & PIO_QEF) != 0;
     bool isbig = (t.depth < DEPTH_MIN);
     bool signchange = false;
@@ -930,7 +1122,7 @@ struct Frame : FrameBase {
     }
     t.signchange = signchange;
     float np[3];
-    if ((cellsize - radius) < 1e-8) {
+    if ((cellsize - min_radius) < 1e-8) {
       t.type = LEAF;
       np[0] = (float)t.node[0], np[1] = (float)t.node[1], np[2] = (float)t.node[2];
       t.node[3] = ev.SingleEval(np);
@@ -984,6 +1176,7 @@ struct Frame : FrameBase {
     const size_t inProcessSize = 10000000;
     std::vector<int> waiting{0}, batch;
     std::vector<R> curvs;
+    std::vector<float> minrs;
     std::vector<unsigned char> emptys;
     std::vector<float> sps;
     std::vector<R> vals, grads;
@@ -995,6 +1188,7 @@ struct Frame : FrameBase {
       }
       const size_t nb = batch.size();
       curvs.assign(nb, 0);
+      minrs.assign(nb, 0);
       emptys.assign(nb, 0);
 #pragma omp parallel
       {
@@ -1004,7 +1198,7 @@ struct Frame : FrameBase {
 #pragma omp task firstprivate(i)
             {
               TNode<R>& t = nodes[batch[i]];
-              checkEmptyAndCalcCurv(t, emptys[i], curvs[i]);
+              checkEmptyAndCalcCurv(t, emptys[i], curvs[i], minrs[i]);
               t.curv = (float)curvs[i];
               if (emptys[i]) {
                 t.node[3] = ev._ISO_VALUE;
@@ -1024,7 +1218,7 @@ struct Frame : FrameBase {
           for (size_t i = 0; i < nb; i++) {
             if (emptys[i]) continue;
 #pragma omp task firstprivate(i)
-            afterSampleEval(nodes[batch[i]], curvs[i], &sps[i * 108], &vals[i * 27], &grads[i * 81]);
+            afterSampleEval(nodes[batch[i]], curvs[i], minrs[i], &sps[i * 108], &vals[i * 27], &grads[i * 81]);
           }
         }
       }
@@ -1162,7 +1356,8 @@ struct Frame : FrameBase {
   // VisitorExtract::calc_vertices (src/visitorextract.cpp:41-201)
   void calc_vertices() {
     dual_cells.assign(dual_grids.size(), DualCell<R>());
-    const float rr = radius / 2;
+    // src/visitorextract.cpp:54: half the (searcher's minimum) radius
+    const float rr = (varR ? searcher.minRadius : radius) / 2;
 #pragma omp parallel for
     for (long long i = 0; i < (long long)dual_grids.size(); i++) {
       DualCell<R>& dc = dual_cells[i];
@@ -1261,17 +1456,30 @@ struct Frame : FrameBase {
     switch (s) {
       case 1:  // src/surface_reconstructor.cpp:418-424
         loadRootBox();
-        grid.init(&P, BoundingBox, radius, 4.0f, (flags & PIO_STD_SORT) != 0);
+        if (varR)
+          searcher.init(&P, radii, 4.0f, (flags & PIO_STD_SORT) != 0);
+        else
+          grid.init(&P, BoundingBox, radius, 4.0f, (flags & PIO_STD_SORT) != 0);
         break;
       case 2:  // :432-435
+        if (varR) {
+          ev.searcher = &searcher;
+          ev.GlobalRadius = &radii;
+        }
         ev.init(&grid, &P, radius);
         ev._SMOOTH_FACTOR = smooth_factor;
         ev.compute_Gs_xMeans();
         break;
       case 3:  // :453-470
-        resizeRootBoxConstR();
-        ev.CalculateMaxScalarConstR();
-        ev.RecommendIsoValueConstR();
+        if (varR) {
+          resizeRootBoxVarR();
+          ev.CalculateMaxScalarVarR();
+          ev.RecommendIsoValueVarR();
+        } else {
+          resizeRootBoxConstR();
+          ev.CalculateMaxScalarConstR();
+          ev.RecommendIsoValueConstR();
+        }
         ev.CalcParticlesNormal();
         break;
       case 4:
@@ -1336,6 +1544,48 @@ pio_frame* pio_create(const float* xyz, int64_t n, float radius, float smooth_fa
   return h;
 }
 
+pio_frame* pio_create_var(const float* xyz, const float* radii, int64_t n, float smooth_factor, float iso_factor,
+                          int flags) {
+  pio_frame* h = pio_create(xyz, n, radii[0], smooth_factor, iso_factor, flags);
+  h->f->varR = true;
+  h->f->radii.assign(radii, radii + n);
+  return h;
+}
+
+int pio_num_bins(const pio_frame* h) { return h->f->varR ? (int)h->f->searcher.searchers.size() : 1; }
+
+int pio_bin_info(const pio_frame* h, int b, float* b6, int64_t* xyz3, int64_t* cn, float* cs, int64_t* count,
+                 int32_t* radius_id) {
+  if (h->f->stage_done < 1) return -1;
+  const HashGrid& g = h->f->varR ? h->f->searcher.searchers.at(b) : h->f->grid;
+  for (int i = 0; i < 6; ++i) b6[i] = g.Bounding[i];
+  for (int i = 0; i < 3; ++i) xyz3[i] = g.XYZCellNum[i];
+  *cn = (int64_t)g.CellNum;
+  *cs = g.CellSize;
+  *count = (int64_t)g.ParticlesNum;
+  *radius_id = g.RadiusId;
+  return 0;
+}
+
+int pio_bin_lists(const pio_frame* h, int b, int32_t* particles, int64_t* keys, int32_t* index_list) {
+  if (h->f->stage_done < 1) return -1;
+  const HashGrid& g = h->f->varR ? h->f->searcher.searchers.at(b) : h->f->grid;
+  for (unsigned i = 0; i < g.ParticlesNum; ++i) {
+    if (particles) particles[i] = g.var ? g.PIndexes[i] : (int32_t)i;
+    if (keys) keys[i] = g.Keys[i];
+    if (index_list) index_list[i] = g.var ? g.PIndexes[g.IndexList[i]] : g.IndexList[i];
+  }
+  return 0;
+}
+
+int pio_searcher_radii(const pio_frame* h, float* out3) {
+  if (!h->f->varR || h->f->stage_done < 1) return -1;
+  out3[0] = h->f->searcher.minRadius;
+  out3[1] = h->f->searcher.maxRadius;
+  out3[2] = h->f->searcher.avgRadius;
+  return 0;
+}
+
 void pio_destroy(pio_frame* f) { delete f; }
 void pio_set_threads(int n) {
   if (n > 0) omp_set_num_threads(n);
@@ -1390,7 +1640,10 @@ int64_t pio_neighbors(pio_frame* h, const float* pts, int64_t m, int64_t* offset
   std::vector<int> nb;
   for (int64_t i = 0; i < m; ++i) {
     nb.clear();
-    g.GetPIdxList(pts + 3 * i, nb);
+    if (h->f->varR)
+      h->f->searcher.GetNeighbors(pts + 3 * i, nb);
+    else
+      g.GetPIdxList(pts + 3 * i, nb);
     if (tot + (int64_t)nb.size() > cap) return -1;
     for (int j : nb) out[tot++] = j;
     offsets[i + 1] = tot;
@@ -1400,7 +1653,10 @@ int64_t pio_neighbors(pio_frame* h, const float* pts, int64_t m, int64_t* offset
 int64_t pio_in_box(pio_frame* h, const float* b1, const float* b2, int32_t* out, int64_t cap) {
   HashGrid& g = h->f->grid;
   std::vector<int> nb;
-  g.GetInBoxParticles(F3{b1[0], b1[1], b1[2]}, F3{b2[0], b2[1], b2[2]}, nb);
+  if (h->f->varR)
+    h->f->searcher.GetInBoxParticles(F3{b1[0], b1[1], b1[2]}, F3{b2[0], b2[1], b2[2]}, nb);
+  else
+    g.GetInBoxParticles(F3{b1[0], b1[1], b1[2]}, F3{b2[0], b2[1], b2[2]}, nb);
   if ((int64_t)nb.size() > cap) return -1;
   for (size_t j = 0; j < nb.size(); ++j) out[j] = nb[j];
   return (int64_t)nb.size();

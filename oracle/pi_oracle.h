@@ -39,6 +39,22 @@ typedef struct pio_frame pio_frame;
 
 pio_frame* pio_create(const float* xyz, int64_t n, float radius, float smooth_factor,
                       float iso_factor, int flags);
+/* Variable radius (per-particle radii, the reference's non-constant-radius
+ * SurfReconstructor with its neighbour query switched on): the same stages
+ * with the MultiLevelSearcher in place of the hash grid. */
+pio_frame* pio_create_var(const float* xyz, const float* radii, int64_t n, float smooth_factor,
+                          float iso_factor, int flags);
+/* grids: 1 for a constant radius, else the searcher's non-empty bins in bin
+ * order; per grid its bounding box, cell counts, cell size, particle count,
+ * the particle whose radius sets the cell (-1 for a constant radius), and
+ * its particles (bin-local order), their keys, and IndexList as particle
+ * indices */
+int pio_num_bins(const pio_frame* f);
+int pio_bin_info(const pio_frame* f, int bin, float* bounding6, int64_t* xyz_cell_num3, int64_t* cell_num,
+                 float* cell_size, int64_t* count, int32_t* radius_id);
+int pio_bin_lists(const pio_frame* f, int bin, int32_t* particles, int64_t* keys, int32_t* index_list);
+/* MultiLevelSearcher min / max / average radius */
+int pio_searcher_radii(const pio_frame* f, float* out3);
 void pio_destroy(pio_frame* f);
 void pio_set_threads(int nthreads);
 

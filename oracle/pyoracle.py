@@ -68,6 +68,12 @@ def lib():
             "pio_dmc_table": (C.c_int, [C.POINTER(C.c_int32), C.POINTER(C.c_int8), C.POINTER(C.c_int32)]),
             "pio_uniform_grid": (C.c_int, [P, fp, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
             "pio_grid_sample": (C.c_int, [P, dp, i64]),
+            "pio_create_var": (P, [fp, fp, i64, C.c_float, C.c_float, C.c_int]),
+            "pio_num_bins": (C.c_int, [P]),
+            "pio_bin_info": (C.c_int, [P, C.c_int, fp, C.POINTER(i64), C.POINTER(i64), fp, C.POINTER(i64),
+                                       C.POINTER(C.c_int32)]),
+            "pio_bin_lists": (C.c_int, [P, C.c_int, C.POINTER(C.c_int32), C.POINTER(i64), C.POINTER(C.c_int32)]),
+            "pio_searcher_radii": (C.c_int, [P, fp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -97,10 +103,18 @@ class OracleFrame:
     """One reconstruction (SurfReconstructor + Run) on the CPU oracle."""
 
     def __init__(self, xyz, radius, smooth_factor=2.0, iso_factor=1.9, flags=0):
+        """radius: a float (constant radius) or an array of per-particle radii
+        (the variable-radius path)."""
         xyz = np.ascontiguousarray(xyz, dtype=np.float32)
         self.n = xyz.shape[0]
         self.flags = flags
-        self.h = lib().pio_create(_p(xyz, C.c_float), self.n, radius, smooth_factor, iso_factor, flags)
+        if np.ndim(radius) == 0:
+            self.h = lib().pio_create(_p(xyz, C.c_float), self.n, radius, smooth_factor, iso_factor, flags)
+        else:
+            r = np.ascontiguousarray(radius, dtype=np.float32)
+            assert r.shape == (self.n,)
+            self.h = lib().pio_create_var(_p(xyz, C.c_float), _p(r, C.c_float), self.n, smooth_factor, iso_factor,
+                                          flags)
 
     def close(self):
         if self.h:
@@ -137,6 +151,32 @@ class OracleFrame:
         cs = C.c_float()
         lib().pio_grid_info(self.h, _p(b, C.c_float), _p(x, C.c_int64), C.byref(cn), C.byref(cs))
         return dict(bounding=b, xyz_cell_num=x, cell_num=cn.value, cell_size=cs.value)
+
+    def bins(self):
+        """Per grid (one for a constant radius, else one per non-empty radius
+        bin): dict of bounding, xyz_cell_num, cell_num, cell_size, radius_id,
+        particles (bin-local order), keys, index_list (particle indices)."""
+        out = []
+        for b in range(lib().pio_num_bins(self.h)):
+            bb = np.zeros(6, np.float32)
+            x = np.zeros(3, np.int64)
+            cn, cnt = C.c_int64(), C.c_int64()
+            cs = C.c_float()
+            rid = C.c_int32()
+            lib().pio_bin_info(self.h, b, _p(bb, C.c_float), _p(x, C.c_int64), C.byref(cn), C.byref(cs),
+                               C.byref(cnt), C.byref(rid))
+            parts = np.zeros(cnt.value, np.int32)
+            keys = np.zeros(cnt.value, np.int64)
+            il = np.zeros(cnt.value, np.int32)
+            lib().pio_bin_lists(self.h, b, _p(parts, C.c_int32), _p(keys, C.c_int64), _p(il, C.c_int32))
+            out.append(dict(bounding=bb, xyz_cell_num=x, cell_num=cn.value, cell_size=cs.value,
+                            radius_id=rid.value, particles=parts, keys=keys, index_list=il))
+        return out
+
+    def searcher_radii(self):
+        o = np.zeros(3, np.float32)
+        rc = lib().pio_searcher_radii(self.h, _p(o, C.c_float))
+        return None if rc else dict(min=o[0], max=o[1], avg=o[2])
 
     def keys(self):
         k = np.zeros(self.n, np.int64)

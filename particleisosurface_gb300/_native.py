@@ -19,7 +19,7 @@ PI_OK, PI_ERR_INVALID, PI_ERR_CUDA, PI_ERR_NOMEM, PI_ERR_STATE, PI_ERR_LIMIT = 0
 ERRORS = {-1: "PI_ERR_INVALID", -2: "PI_ERR_CUDA", -3: "PI_ERR_NOMEM", -4: "PI_ERR_STATE", -5: "PI_ERR_LIMIT"}
 
 DUMP_KEYS, DUMP_INDEX_LIST, DUMP_CELL_OFFSETS, DUMP_XMEANS, DUMP_G, DUMP_DET, DUMP_NORMALS, DUMP_NODES, \
-    DUMP_FP64_FLAGS, DUMP_QEF_SAMPLES = range(1, 11)
+    DUMP_FP64_FLAGS, DUMP_QEF_SAMPLES, DUMP_GRID_OF = range(1, 12)
 
 
 class PiError(RuntimeError):
@@ -43,7 +43,8 @@ class FrameInfo(C.Structure):
                 ("num_vertices", C.c_int64), ("num_triangles", C.c_int64), ("field_evals", C.c_int64),
                 ("candidate_pairs", C.c_int64), ("bisection_evals", C.c_int64), ("fp64_eigen", C.c_int64),
                 ("stage_ms", C.c_float * 8), ("qef_accepted", C.c_int64), ("qef_singular", C.c_int64),
-                ("grid_pairs", C.c_int64), ("field_evals_performed", C.c_int64)]
+                ("grid_pairs", C.c_int64), ("field_evals_performed", C.c_int64), ("num_grids", C.c_int32),
+                ("radius_min", C.c_float), ("radius_max", C.c_float)]
 
     def as_dict(self):
         out = {}
@@ -85,6 +86,8 @@ def _declare(L):
         "pi_frame_upload": (C.c_int, [P, fp, i64]),
         "pi_frame_upload_device": (C.c_int, [P, P, i64]),
         "pi_frame_reset": (C.c_int, [P]),
+        "pi_frame_upload_radii": (C.c_int, [P, fp, i64]),
+        "pi_frame_grid": (C.c_int, [P, C.c_int32, fp, C.POINTER(C.c_int32), fp, pi64, pi64, C.POINTER(C.c_int32)]),
         "pi_hashgrid_build": (C.c_int, [P]),
         "pi_aniso_compute": (C.c_int, [P]),
         "pi_normals_compute": (C.c_int, [P]),
@@ -283,6 +286,25 @@ class Frame:
         check(lib().pi_frame_upload(self.h, ptr(xyz, C.c_float), self.n))
         return self
 
+    def upload_radii(self, radii):
+        """Per-particle radii (pi_frame_upload_radii): the variable-radius path."""
+        r = np.ascontiguousarray(radii, dtype=np.float32)
+        check(lib().pi_frame_upload_radii(self.h, ptr(r, C.c_float), r.shape[0]))
+        return self
+
+    def grid(self, k):
+        """Hash grid k (pi_frame_grid): bounding, dims, cell_size, count,
+        offset_base, radius_id."""
+        b = np.zeros(6, np.float32)
+        d = np.zeros(3, np.int32)
+        cs = C.c_float()
+        cnt, ob = C.c_int64(), C.c_int64()
+        rid = C.c_int32()
+        check(lib().pi_frame_grid(self.h, k, ptr(b, C.c_float), ptr(d, C.c_int32), C.byref(cs), C.byref(cnt),
+                                  C.byref(ob), C.byref(rid)))
+        return dict(bounding=b, dims=d, cell_size=cs.value, count=cnt.value, offset_base=ob.value,
+                    radius_id=rid.value)
+
     def upload_device(self, dptr, n):
         self.n = n
         check(lib().pi_frame_upload_device(self.h, C.c_void_p(dptr), n))
@@ -427,6 +449,7 @@ class Frame:
             DUMP_G: (np.float32, (-1, 3, 3)), DUMP_DET: (np.float32, (-1,)),
             DUMP_NORMALS: (np.float32, (-1, 3)), DUMP_NODES: (NODE_DTYPE, (-1,)),
             DUMP_FP64_FLAGS: (np.int8, (-1,)), DUMP_QEF_SAMPLES: (np.float32, (-1, 27)),
+            DUMP_GRID_OF: (np.int32, (-1,)),
         }[what]
         buf = np.empty(nb.value // np.dtype(dtype).itemsize, dtype)
         check(lib().pi_stage_dump(self.h, what, buf.ctypes.data_as(C.c_void_p), nb.value))

@@ -246,6 +246,166 @@ __global__ void __launch_bounds__(128, 8) k_cov_G(GridView g, const float4* __re
   f64flag[t] = degenerate ? 1 : 0;
 }
 
+// ---------------------------------------------------------------------------
+// Variable radius (compute_xMeans / compute_G_Yus with per-particle radii,
+// src/evaluator.cpp:465-512, 585-654): a neighbour j counts within its own
+// neighbour radius nI_j = 4 r_j with weight wij(d, nI_j); the covariance
+// starts from the particle's own Influnce2 = (2 r_i)^2; A = G / (2 r_i) and
+// det * Sigma_i per particle.  The radius rides in pos.w.  Candidates are the
+// bins' 27-cell lists in bin order.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_vr_xmean(const MultiGridView* __restrict__ mg,
+                                                  const float4* __restrict__ pos, const float4* __restrict__ vrc,
+                                                  long long n, float c_mean, float4* __restrict__ xm,
+                                                  float4* __restrict__ xlo) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const MultiGridView& m = *mg;
+  const float4 p = pos[t];
+  long long cand = 0;
+  Kahan ws, sx, sy, sz;
+  for (int b = 0; b < m.nb; ++b) {
+    const BinGrid g = m.g[b];
+    const int cx = cell_coord(p.x, g.b0, g.cell, g.nx), cy = cell_coord(p.y, g.b2, g.cell, g.ny),
+              cz = cell_coord(p.z, g.b4, g.cell, g.nz);
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy) {
+        int s, e;
+        if (!bin_row(g, m.off, cx, cy + dy, cz + dz, &s, &e)) continue;
+        cand += e - s;
+        for (int j = s; j < e; ++j) {
+          if (j == t) continue;
+          const float4 q = __ldg(pos + j);
+          const float4 cj = __ldg(vrc + j);  // (Influnce2, Sigma, nI, 1 / nI^3) of the neighbour
+          const float dx = __fsub_rn(q.x, p.x), dy2 = __fsub_rn(q.y, p.y), dz2 = __fsub_rn(q.z, p.z);
+          const float d2 = d2_exact(dx, dy2, dz2);
+          if (!(d2 < __fmul_rn(cj.z, cj.z))) continue;
+          const float w = wij_f(__fsqrt_rn(d2), cj.z, cj.w);
+          ws.add(w);
+          sx.add(dx * w);
+          sy.add(dy2 * w);
+          sz.add(dz2 * w);
+        }
+      }
+  }
+  float4 hi = make_float4(p.x, p.y, p.z, 0.f), lo = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (cand > 2 && ws.s > 0.f) {
+    const float ox = c_mean * ((sx.s - sx.c) / ws.s), oy = c_mean * ((sy.s - sy.c) / ws.s),
+                oz = c_mean * ((sz.s - sz.c) / ws.s);
+    hi.x = __fadd_rn(p.x, ox);
+    hi.y = __fadd_rn(p.y, oy);
+    hi.z = __fadd_rn(p.z, oz);
+    lo.x = __fadd_rn(__fsub_rn(p.x, hi.x), ox);
+    lo.y = __fadd_rn(__fsub_rn(p.y, hi.y), oy);
+    lo.z = __fadd_rn(__fsub_rn(p.z, hi.z), oz);
+  }
+  xm[t] = hi;
+  xlo[t] = lo;
+}
+
+__global__ void __launch_bounds__(128) k_vr_cov_G(const MultiGridView* __restrict__ mg,
+                                                  const float4* __restrict__ pos, const float4* __restrict__ vrc,
+                                                  const float4* __restrict__ xm0,
+                                                  const float4* __restrict__ xlo, float4* __restrict__ xm, long long n,
+                                                  float4* __restrict__ ga, float4* __restrict__ gb,
+                                                  float* __restrict__ gfull, float* __restrict__ det_out,
+                                                  int8_t* __restrict__ f64flag, unsigned long long* __restrict__ f64count) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const MultiGridView& m = *mg;
+  const float4 p = pos[t];
+  const float4 xp = xm0[t];
+  const float4 lp = xlo[t];
+  const float4 ci = vrc[t];
+  const float h = p.w * 2.0f;  // 2 r_i
+  const float h2 = ci.x;       // Influnce2_i
+  const float sigma = ci.y;    // Sigma_i
+  const float inv_h = 1.0f / h;
+  Kahan ws, c00, c01, c02, c11, c12, c22;
+  for (int b = 0; b < m.nb; ++b) {
+    const BinGrid g = m.g[b];
+    const int cx = cell_coord(p.x, g.b0, g.cell, g.nx), cy = cell_coord(p.y, g.b2, g.cell, g.ny),
+              cz = cell_coord(p.z, g.b4, g.cell, g.nz);
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy) {
+        int s, e;
+        if (!bin_row(g, m.off, cx, cy + dy, cz + dz, &s, &e)) continue;
+        for (int j = s; j < e; ++j) {
+          const float4 q = __ldg(xm0 + j);
+          const float4 lq = __ldg(xlo + j);
+          const float4 cj = __ldg(vrc + j);
+          const float nI = cj.z;
+          const float dx = __fadd_rn(__fsub_rn(q.x, xp.x), __fsub_rn(lq.x, lp.x));
+          const float dy2 = __fadd_rn(__fsub_rn(q.y, xp.y), __fsub_rn(lq.y, lp.y));
+          const float dz2 = __fadd_rn(__fsub_rn(q.z, xp.z), __fsub_rn(lq.z, lp.z));
+          const float d2 = d2_exact(dx, dy2, dz2);
+          if (!(d2 < __fmul_rn(nI, nI))) continue;
+          const float w = wij_f(__fsqrt_rn(d2), nI, cj.w);
+          ws.add(w);
+          c00.add(dx * dx * w);
+          c01.add(dx * dy2 * w);
+          c02.add(dx * dz2 * w);
+          c11.add(dy2 * dy2 * w);
+          c12.add(dy2 * dz2 * w);
+          c22.add(dz2 * dz2 * w);
+        }
+      }
+  }
+  const float iw = 1.0f / ws.s;
+  float a6[6] = {(h2 + c00.s) * iw, c01.s * iw, c02.s * iw, (h2 + c11.s) * iw, c12.s * iw, (h2 + c22.s) * iw};
+  float w[3], V[3][3];
+  float G[9], stretch;
+  bool degenerate = false;
+  if (!(ws.s > 0.f)) {
+    for (int k = 0; k < 9; ++k) G[k] = (k % 4 == 0) ? 1.0f : 0.0f;
+    stretch = 1.0f;
+  } else {
+    sym_eig3<float>(a6, w, V);
+    const float aw0 = fabsf(w[0]), aw1 = fabsf(w[1]), aw2 = fabsf(w[2]);
+    const float wmx = fmaxf(aw0, fmaxf(aw1, aw2)), wmn = fminf(aw0, fminf(aw1, aw2));
+    degenerate = wmn < 0.25f * wmx;
+    if (degenerate) {
+      double a6d[6], wd[3], Vd[3][3];
+      for (int k = 0; k < 6; ++k) a6d[k] = (double)a6[k];
+      sym_eig3<double>(a6d, wd, Vd);
+      g_from_eig<double>(wd, Vd, G, &stretch);
+      stripe_add(f64count, 0, 1ull);
+    } else {
+      g_from_eig<float>(w, V, G, &stretch);
+    }
+  }
+  const float det = G[0] * (G[4] * G[8] - G[5] * G[7]) - G[1] * (G[3] * G[8] - G[5] * G[6]) +
+                    G[2] * (G[3] * G[7] - G[4] * G[6]);
+  const float R = 2.0f * stretch / inv_h;
+  const float h5 = h * h * h * h * h;
+  xm[t] = make_float4(xp.x, xp.y, xp.z, R * R * 1.002f);
+  ga[t] = make_float4(G[0] * inv_h, G[1] * inv_h, G[2] * inv_h, G[4] * inv_h);
+  // gb.w: -6 h_i^5, the factor of the normal's gradient form in A units
+  gb[t] = make_float4(G[5] * inv_h, G[8] * inv_h, det * sigma, -6.0f * h5);
+  for (int k = 0; k < 9; ++k) gfull[9 * t + k] = G[k];
+  det_out[t] = det;
+  f64flag[t] = degenerate ? 1 : 0;
+}
+
+void stage_aniso_vr(pi_frame* f) {
+  cudaStream_t s = f->ctx->stream;
+  const long long n = f->N;
+  f->xm.alloc(f->ctx, s, n);
+  f->nrm.alloc(f->ctx, s, n);  // holds the pass-1 centres until the normals overwrite it
+  f->ga.alloc(f->ctx, s, n);
+  f->gb.alloc(f->ctx, s, n);
+  f->xlo.alloc(f->ctx, s, n);
+  f->gfull.alloc(f->ctx, s, n * 9);
+  f->det.alloc(f->ctx, s, n);
+  f->f64flag.alloc(f->ctx, s, n);
+  counters_reset(f);
+  PI_LAUNCH(k_vr_xmean, div_up(n, 128), 128, 0, s, f->mgv.p, f->pos.p, f->vrcs.p, n, (float)0.9, f->nrm.p,
+            f->xlo.p);
+  PI_LAUNCH(k_vr_cov_G, div_up(n, 128), 128, 0, s, f->mgv.p, f->pos.p, f->vrcs.p, f->nrm.p, f->xlo.p, f->xm.p, n,
+            f->ga.p, f->gb.p, f->gfull.p, f->det.p, f->f64flag.p, f->dcount.p);
+  counters_snapshot(f, kPinAniso);
+}
+
 void stage_aniso(pi_frame* f) {
   cudaStream_t s = f->ctx->stream;
   const long long n = f->N;

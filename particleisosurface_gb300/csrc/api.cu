@@ -95,6 +95,7 @@ template struct DBuf<int8_t>;
 template struct DBuf<uint64_t>;
 template struct DBuf<unsigned long long>;
 template struct DBuf<long long>;
+template struct DBuf<MultiGridView>;
 
 // Bspline_kernel (src/evaluator.cpp:383-396) with the reference's types:
 // float in, polynomial in double, float out.
@@ -284,13 +285,22 @@ static void run_stage(pi_frame* f, int target) {
   ev_record(f, 2 * slot);
   switch (target) {
     case 2:
-      stage_hashgrid(f);
+      if (f->varR)
+        stage_hashgrid_vr(f);
+      else
+        stage_hashgrid(f);
       break;
     case 3:
-      stage_aniso(f);
+      if (f->varR)
+        stage_aniso_vr(f);
+      else
+        stage_aniso(f);
       break;
     case 4:
-      host_root_and_scalars(f);
+      if (f->varR)
+        host_root_and_scalars_vr(f);
+      else
+        host_root_and_scalars(f);
       if (f->P.max_depth > 0 && f->dmax > f->P.max_depth)
         throw std::length_error("octree depth " + std::to_string(f->dmax) + " exceeds max_depth " +
                                 std::to_string(f->P.max_depth));
@@ -568,6 +578,43 @@ int pi_frame_upload(pi_frame* f, const float* xyz, int64_t n) {
   ev_record(f, 1);
   ev_close(f, 0);
   f->stage = 1;
+  f->varR = false;
+  PI_API_END
+}
+
+int pi_frame_upload_radii(pi_frame* f, const float* radii, int64_t n) {
+  PI_API_BEGIN
+  PI_CHECK(f && radii && n > 0, "bad radii arguments");
+  need(f, 1);
+  set_device(f->ctx);
+  stage_upload_radii(f, radii, n);
+  frame_clear(f, 1);
+  PI_API_END
+}
+
+int pi_frame_grid(const pi_frame* f, int32_t k, float* bounding6, int32_t* dims3, float* cell_size, int64_t* count,
+                  int64_t* offset_base, int32_t* radius_id) {
+  PI_API_BEGIN
+  PI_CHECK(f && bounding6 && dims3 && cell_size && count && offset_base && radius_id, "null argument");
+  need(f, 2);
+  if (!f->varR) {
+    PI_CHECK(k == 0, "no such grid");
+    for (int q = 0; q < 6; ++q) bounding6[q] = f->g.bounding[q];
+    dims3[0] = f->g.nx, dims3[1] = f->g.ny, dims3[2] = f->g.nz;
+    *cell_size = f->g.cell;
+    *count = f->N;
+    *offset_base = 0;
+    *radius_id = -1;
+  } else {
+    PI_CHECK(k >= 0 && k < (int)f->bins.size(), "no such grid");
+    const BinHost& b = f->bins[k];
+    for (int q = 0; q < 6; ++q) bounding6[q] = b.bounding[q];
+    dims3[0] = b.nx, dims3[1] = b.ny, dims3[2] = b.nz;
+    *cell_size = b.cell;
+    *count = b.count;
+    *offset_base = b.offBase;
+    *radius_id = b.radius_id;
+  }
   PI_API_END
 }
 
@@ -578,6 +625,7 @@ int pi_frame_upload_device(pi_frame* f, const float* d_xyz, int64_t n) {
   set_device(f->ctx);
   stage_upload_device(f, d_xyz, n);
   f->stage = 1;
+  f->varR = false;
   PI_API_END
 }
 
@@ -700,6 +748,9 @@ int pi_frame_info_get(const pi_frame* f, pi_frame_info* o) {
   o->qef_singular = f->qefSingular;
   o->grid_pairs = f->gridPairs;
   o->field_evals_performed = f->doneEvals;
+  o->num_grids = f->varR ? (int32_t)f->bins.size() : (f->stage >= 2 ? 1 : 0);
+  o->radius_min = f->varR ? f->vrMinR : f->P.radius;
+  o->radius_max = f->varR ? f->vrMaxR : f->P.radius;
   PI_API_END
 }
 
@@ -951,7 +1002,8 @@ static size_t dump_size(const pi_frame* f, int what) {
   switch (what) {
     case PI_DUMP_KEYS: return sizeof(int64_t) * f->N;
     case PI_DUMP_INDEX_LIST: return sizeof(int32_t) * f->N;
-    case PI_DUMP_CELL_OFFSETS: return sizeof(int32_t) * (f->g.cellNum + 1);
+    case PI_DUMP_CELL_OFFSETS: return sizeof(int32_t) * (f->varR ? f->off.n : f->g.cellNum + 1);
+    case PI_DUMP_GRID_OF: return sizeof(int32_t) * f->N;
     case PI_DUMP_XMEANS: return sizeof(float) * 3 * f->N;
     case PI_DUMP_G: return sizeof(float) * 9 * f->N;
     case PI_DUMP_DET: return sizeof(float) * f->N;
@@ -1000,8 +1052,19 @@ int pi_stage_dump(pi_frame* f, int what, void* buf, size_t bytes) {
     }
     case PI_DUMP_CELL_OFFSETS: {
       need(f, 2);
-      auto k = d2h(f->off.p, f->g.cellNum + 1, s);
-      std::memcpy(buf, k.data(), sizeof(int32_t) * (f->g.cellNum + 1));
+      const size_t m = f->varR ? f->off.n : (size_t)f->g.cellNum + 1;
+      auto k = d2h(f->off.p, m, s);
+      std::memcpy(buf, k.data(), sizeof(int32_t) * m);
+      break;
+    }
+    case PI_DUMP_GRID_OF: {
+      need(f, 2);
+      if (f->varR) {
+        auto k = d2h(f->pbin.p, N, s);
+        std::memcpy(buf, k.data(), sizeof(int32_t) * N);
+      } else {
+        std::memset(buf, 0, sizeof(int32_t) * N);
+      }
       break;
     }
     case PI_DUMP_XMEANS: {

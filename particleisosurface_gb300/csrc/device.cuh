@@ -106,6 +106,38 @@ __device__ __forceinline__ void amul(const float4& a, const float4& b, float dx,
   u2 = fmaf(a.z, dx, fmaf(b.x, dy, b.y * dz));
 }
 
+// The kernel terms of the candidates [s, e) at q, added to acc in candidate
+// order.  32 candidates at a time: first the cheap |d|^2 < R^2 test of each
+// into a bit mask, then the kernel terms of the set bits in candidate order,
+// so that a warp runs the costly part as often as its busiest lane needs it
+// rather than once per candidate any lane needs.
+__device__ __forceinline__ void field_row(const PartView& P, int s, int e, float qx, float qy, float qz,
+                                          Kahan& acc) {
+  for (int j0 = s; j0 < e; j0 += 32) {
+    const int cnt = min(32, e - j0);
+    unsigned m = 0u;
+    for (int k = 0; k < cnt; ++k) {
+      const float4 x = __ldg(P.xm + j0 + k);
+      const float dx = qx - x.x, dyy = qy - x.y, dzz = qz - x.z;
+      const float e2 = fmaf(dx, dx, fmaf(dyy, dyy, dzz * dzz));
+      m |= (e2 < x.w ? 1u : 0u) << k;
+    }
+    while (m) {
+      const int j = j0 + __ffs(m) - 1;
+      m &= m - 1u;
+      const float4 x = __ldg(P.xm + j);
+      const float dx = qx - x.x, dyy = qy - x.y, dzz = qz - x.z;
+      const float4 a = __ldg(P.ga + j);
+      const float4 b = __ldg(P.gb + j);
+      const float4 lo = __ldg(P.xlo + j);
+      float u0, u1, u2;
+      amul(a, b, dx - lo.x, dyy - lo.y, dzz - lo.z, u0, u1, u2);
+      const float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
+      if (s2 < 4.0f) acc.add(b.z * bspline_s2(s2));
+    }
+  }
+}
+
 // Sum over the 27-cell candidates of particle kernel values at q: the
 // sum in Evaluator::SingleEval (src/evaluator.cpp:60-87) without the
 // iso - sum step.  Compensated (Kahan) FP32 accumulation.
@@ -120,34 +152,66 @@ __device__ __forceinline__ float field_sum(const GridView& g, const PartView& P,
       int s, e;
       if (!nb_row(g, cx, cy + dy, cz + dz, &s, &e)) continue;
       pairs += e - s;
-      // 32 candidates at a time: first the cheap |d|^2 < R^2 test of each
-      // into a bit mask, then the kernel terms of the set bits in candidate
-      // order, so that a warp runs the costly part as often as its busiest
-      // lane needs it rather than once per candidate any lane needs
-      for (int j0 = s; j0 < e; j0 += 32) {
-        const int cnt = min(32, e - j0);
-        unsigned m = 0u;
-        for (int k = 0; k < cnt; ++k) {
-          const float4 x = __ldg(P.xm + j0 + k);
-          const float dx = qx - x.x, dyy = qy - x.y, dzz = qz - x.z;
-          const float e2 = fmaf(dx, dx, fmaf(dyy, dyy, dzz * dzz));
-          m |= (e2 < x.w ? 1u : 0u) << k;
-        }
-        while (m) {
-          const int j = j0 + __ffs(m) - 1;
-          m &= m - 1u;
-          const float4 x = __ldg(P.xm + j);
-          const float dx = qx - x.x, dyy = qy - x.y, dzz = qz - x.z;
-          const float4 a = __ldg(P.ga + j);
-          const float4 b = __ldg(P.gb + j);
-          const float4 lo = __ldg(P.xlo + j);
-          float u0, u1, u2;
-          amul(a, b, dx - lo.x, dyy - lo.y, dzz - lo.z, u0, u1, u2);
-          const float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
-          if (s2 < 4.0f) acc.add(b.z * bspline_s2(s2));
-        }
-      }
+      field_row(P, s, e, qx, qy, qz, acc);
     }
+  if (npairs) *npairs += pairs;
+  return acc.s;
+}
+
+// ---------------------------------------------------------------------------
+// Variable radius: the particles binned by radius (MultiLevelSearcher,
+// src/multi_level_reseacher.cpp:6-77), one hash grid per non-empty bin with
+// the cell size of the bin's largest radius times 4.  Particles are sorted by
+// (bin, cell key + 1, particle); off[] holds every bin's cell offsets one
+// bin after the other (cellNum + 1 entries per bin, offBase its first), with
+// bin b's entries counted from the bin's first sorted position and the
+// reference's shift by the bin's key -1 particles kept.  A point's candidate
+// list is the bins' 27-cell lists in bin order (GetNeighbors).
+// ---------------------------------------------------------------------------
+constexpr int kMaxBins = 32;
+
+struct BinGrid {
+  float b0, b2, b4, cell;
+  int nx, ny, nz;
+  int offBase;
+};
+
+struct MultiGridView {
+  int nb;
+  const int* off;
+  BinGrid g[kMaxBins];
+};
+
+__device__ __forceinline__ bool bin_row(const BinGrid& g, const int* off, int cx, int y, int z, int* s, int* e) {
+  if (z < 0 || z >= g.nz || y < 0 || y >= g.ny) return false;
+  const int x0 = cx - 1 < 0 ? 0 : cx - 1;
+  const int x1 = cx + 1 > g.nx - 1 ? g.nx - 1 : cx + 1;
+  if (x0 > x1) return false;
+  const long long base = (long long)g.offBase + ((long long)z * g.ny + y) * g.nx;
+  *s = __ldg(off + base + x0);
+  *e = __ldg(off + base + x1 + 1);
+  return *s < *e;
+}
+
+// SingleEval's sum with the variable-radius candidate list; the per-particle
+// records already hold each particle's A = G / (2 r_j), det * Sigma_j and
+// support radius.
+__device__ __forceinline__ float field_sum_vr(const MultiGridView& m, const PartView& P, float qx, float qy,
+                                              float qz, long long* npairs) {
+  Kahan acc;
+  long long pairs = 0;
+  for (int b = 0; b < m.nb; ++b) {
+    const BinGrid g = m.g[b];
+    const int cx = cell_coord(qx, g.b0, g.cell, g.nx), cy = cell_coord(qy, g.b2, g.cell, g.ny),
+              cz = cell_coord(qz, g.b4, g.cell, g.nz);
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy) {
+        int s, e;
+        if (!bin_row(g, m.off, cx, cy + dy, cz + dz, &s, &e)) continue;
+        pairs += e - s;
+        field_row(P, s, e, qx, qy, qz, acc);
+      }
+  }
   if (npairs) *npairs += pairs;
   return acc.s;
 }

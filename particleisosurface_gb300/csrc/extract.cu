@@ -421,10 +421,11 @@ __global__ void k_tri_slots(long long nu, const int* __restrict__ cells, const i
 }
 
 struct BisectArgs {
-  GridView g;
+  GridView g;  // the hash grid (constant radius); with a variable radius the grid the vertices are bucketed by
   PartView P;
   float iso;
-  float rr;  // r / 2
+  float rr;  // r / 2 (variable radius: the searcher's minimum radius / 2)
+  const MultiGridView* mg;  // variable radius: the bins' grids, else null
 };
 
 // Vertices listed by the hash cell of their first bisection midpoint (count
@@ -470,6 +471,7 @@ __global__ void k_vcell_place(long long nv, const int* __restrict__ key, const i
   list[off[k] + b + __popc(peers & ((1u << lane) - 1u))] = (int)v;
 }
 
+template <bool VR>
 __global__ void k_bisect(BisectArgs a, long long nv, const int* __restrict__ order, const int* __restrict__ rep,
                          const int* __restrict__ slotA,
                          const int* __restrict__ slotB, const float4* __restrict__ nd_v,
@@ -490,7 +492,7 @@ __global__ void k_bisect(BisectArgs a, long long nv, const int* __restrict__ ord
     m.x = __fmul_rn(__fadd_rn(p.x, q.x), 0.5f);
     m.y = __fmul_rn(__fadd_rn(p.y, q.y), 0.5f);
     m.z = __fmul_rn(__fadd_rn(p.z, q.z), 0.5f);
-    m.w = a.iso - field_sum(a.g, a.P, m.x, m.y, m.z, &pairs);
+    m.w = a.iso - (VR ? field_sum_vr(*a.mg, a.P, m.x, m.y, m.z, &pairs) : field_sum(a.g, a.P, m.x, m.y, m.z, &pairs));
     if ((m.w > 0.f) == (p.w > 0.f))
       p = m;
     else
@@ -729,10 +731,20 @@ void stage_extract(pi_frame* f) {
   f->mk.alloc(c, s, nv * 2 > 0 ? nv * 2 : 2);
   const GridHost& gh = f->g;
   BisectArgs ba{GridView{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p},
-                PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p}, f->iso, f->P.radius / 2};
+                PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p}, f->iso, f->P.radius / 2, nullptr};
+  if (f->varR) {
+    // bucket the vertices by a grid of cells 4 * maxR over the root box;
+    // bisect down to half the searcher's minimum radius
+    // (src/visitorextract.cpp:54)
+    const float bcell = f->vrMaxR * 4.0f;
+    const int bn = std::max(1, (int)std::ceil(2.0f * f->rootH / bcell));
+    ba.g = GridView{f->rootC[0] - f->rootH, f->rootC[1] - f->rootH, f->rootC[2] - f->rootH, bcell, bn, bn, bn, nullptr};
+    ba.rr = f->vrMinR / 2;
+    ba.mg = f->mgv.p;
+  }
   {
-    const int ekx = gh.nx + 4, eky = gh.ny + 4;
-    const long long nc = (long long)ekx * eky * (gh.nz + 4);
+    const int ekx = ba.g.nx + 4, eky = ba.g.ny + 4;
+    const long long nc = (long long)ekx * eky * (ba.g.nz + 4);
     DBuf<int> vcnt, vfill, vkey, vorder;
     vcnt.alloc(c, s, nc + 1);
     vfill.alloc(c, s, nc);
@@ -746,8 +758,12 @@ void stage_extract(pi_frame* f) {
     exclusive_scan_i32(vcnt.p, vcnt.p, nc + 1, nullptr, tmp.p, s);
     PI_LAUNCH(k_vcell_place, div_up(nv, 256), 256, 0, s, nv, vkey.p, vcnt.p, vfill.p, vorder.p);
     prof_begin(c, s, PG_BISECT);
-    PI_LAUNCH(k_bisect, div_up(nv, 128), 128, 0, s, ba, nv, vorder.p, rep.p, slotA.p, slotB.p, f->nd_v.p,
-              f->nd_id.p, f->mv.p, f->mk.p, f->dcount.p);
+    if (f->varR)
+      PI_LAUNCH(k_bisect<true>, div_up(nv, 128), 128, 0, s, ba, nv, vorder.p, rep.p, slotA.p, slotB.p, f->nd_v.p,
+                f->nd_id.p, f->mv.p, f->mk.p, f->dcount.p);
+    else
+      PI_LAUNCH(k_bisect<false>, div_up(nv, 128), 128, 0, s, ba, nv, vorder.p, rep.p, slotA.p, slotB.p, f->nd_v.p,
+                f->nd_id.p, f->mv.p, f->mk.p, f->dcount.p);
     prof_end(c, s, PG_BISECT);
   }
   counters_snapshot(f, kPinExtract);

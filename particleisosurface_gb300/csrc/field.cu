@@ -99,13 +99,117 @@ static float grad_scale(pi_frame* f) {
   return (float)(-6.0 * h * h * h * h * h);
 }
 
+// ---- variable radius: the bins' candidate lists, per-particle scales ----
+
+// Gradient-form sum with each term scaled by its particle's -6 h_j^5 (gb.w).
+__device__ __forceinline__ void grad_sum_vr(const MultiGridView& m, const PartView& P, float qx, float qy, float qz,
+                                            float& gx, float& gy, float& gz) {
+  Kahan ax, ay, az;
+  for (int b = 0; b < m.nb; ++b) {
+    const BinGrid g = m.g[b];
+    const int cx = cell_coord(qx, g.b0, g.cell, g.nx), cy = cell_coord(qy, g.b2, g.cell, g.ny),
+              cz = cell_coord(qz, g.b4, g.cell, g.nz);
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy) {
+        int s, e;
+        if (!bin_row(g, m.off, cx, cy + dy, cz + dz, &s, &e)) continue;
+        for (int j = s; j < e; ++j) {
+          const float4 x = __ldg(P.xm + j);
+          const float dx = qx - x.x, dyy = qy - x.y, dzz = qz - x.z;
+          if (!(fmaf(dx, dx, fmaf(dyy, dyy, dzz * dzz)) < 0.25f * x.w)) continue;
+          const float4 a = __ldg(P.ga + j);
+          const float4 bb = __ldg(P.gb + j);
+          const float4 lo = __ldg(P.xlo + j);
+          float u0, u1, u2;
+          amul(a, bb, dx - lo.x, dyy - lo.y, dzz - lo.z, u0, u1, u2);
+          const float s2 = fmaf(u0, u0, fmaf(u1, u1, u2 * u2));
+          if (s2 < 1.0f) {
+            const float om = 1.0f - s2;
+            const float fct = bb.z * om * om * bb.w;
+            ax.add(u0 * fct);
+            ay.add(u1 * fct);
+            az.add(u2 * fct);
+          }
+        }
+      }
+  }
+  gx = ax.s;
+  gy = ay.s;
+  gz = az.s;
+}
+
+__global__ void __launch_bounds__(128) k_vr_normals(const MultiGridView* __restrict__ mg, PartView P, long long n,
+                                                    float4* __restrict__ nrm) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const float4 p = P.pos[t];
+  float gx, gy, gz;
+  grad_sum_vr(*mg, P, p.x, p.y, p.z, gx, gy, gz);
+  nrm[t] = make_float4(gx, gy, gz, sqrtf(gx * gx + gy * gy + gz * gz));
+}
+
+__global__ void k_vr_eval_points(const MultiGridView* __restrict__ mg, PartView P, const float* __restrict__ pts,
+                                 long long m, float iso, float* __restrict__ val, float* __restrict__ grad) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const float qx = pts[3 * i], qy = pts[3 * i + 1], qz = pts[3 * i + 2];
+  val[i] = iso - field_sum_vr(*mg, P, qx, qy, qz, nullptr);
+  if (grad) grad_sum_vr(*mg, P, qx, qy, qz, grad[3 * i], grad[3 * i + 1], grad[3 * i + 2]);
+}
+
+__global__ void k_vr_nb_count(const MultiGridView* __restrict__ mg, const float* __restrict__ pts, long long m,
+                              int* __restrict__ cnt) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const MultiGridView& v = *mg;
+  int c = 0;
+  for (int b = 0; b < v.nb; ++b) {
+    const BinGrid g = v.g[b];
+    const int cx = cell_coord(pts[3 * i], g.b0, g.cell, g.nx), cy = cell_coord(pts[3 * i + 1], g.b2, g.cell, g.ny),
+              cz = cell_coord(pts[3 * i + 2], g.b4, g.cell, g.nz);
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy) {
+        int s, e;
+        if (bin_row(g, v.off, cx, cy + dy, cz + dz, &s, &e)) c += e - s;
+      }
+  }
+  cnt[i] = c;
+}
+
+__global__ void k_vr_nb_fill(const MultiGridView* __restrict__ mg, const float* __restrict__ pts, long long m,
+                             const int* __restrict__ off, const uint32_t* __restrict__ sidx, int* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const MultiGridView& v = *mg;
+  int o = off[i];
+  for (int b = 0; b < v.nb; ++b) {
+    const BinGrid g = v.g[b];
+    const int cx = cell_coord(pts[3 * i], g.b0, g.cell, g.nx), cy = cell_coord(pts[3 * i + 1], g.b2, g.cell, g.ny),
+              cz = cell_coord(pts[3 * i + 2], g.b4, g.cell, g.nz);
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy) {
+        int s, e;
+        if (!bin_row(g, v.off, cx, cy + dy, cz + dz, &s, &e)) continue;
+        for (int j = s; j < e; ++j) out[o++] = (int)sidx[j];
+      }
+  }
+}
+
 void stage_normals(pi_frame* f) {
   cudaStream_t s = f->ctx->stream;
+  if (f->varR) {
+    PI_LAUNCH(k_vr_normals, div_up(f->N, 128), 128, 0, s, f->mgv.p, pview(f), f->N, f->nrm.p);
+    return;
+  }
   PI_LAUNCH(k_normals, div_up(f->N, 128), 128, 0, s, gview(f), pview(f), f->N, grad_scale(f), f->nrm.p);
 }
 
 void eval_points(pi_frame* f, const float* d_pts, long long m, float* d_val, float* d_grad) {
   cudaStream_t s = f->ctx->stream;
+  if (f->varR) {
+    PI_LAUNCH(k_vr_eval_points, div_up(m, 128), 128, 0, s, f->mgv.p, pview(f), d_pts, m, f->iso, d_val, d_grad);
+    return;
+  }
   PI_LAUNCH(k_eval_points, div_up(m, 128), 128, 0, s, gview(f), pview(f), d_pts, m, f->iso, grad_scale(f),
             d_val, d_grad);
 }
@@ -150,7 +254,10 @@ long long neighbors(pi_frame* f, const float* h_pts, long long m, long long* h_o
   PI_CUDA(cudaMemcpyAsync(pts.p, h_pts, sizeof(float) * 3 * m, cudaMemcpyHostToDevice, s));
   GridView g = gview(f);
   PI_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int) * (m + 1), s));
-  PI_LAUNCH(k_nb_count, div_up(m, 128), 128, 0, s, g, pts.p, m, cnt.p);
+  if (f->varR)
+    PI_LAUNCH(k_vr_nb_count, div_up(m, 128), 128, 0, s, f->mgv.p, pts.p, m, cnt.p);
+  else
+    PI_LAUNCH(k_nb_count, div_up(m, 128), 128, 0, s, g, pts.p, m, cnt.p);
   int total = 0;
   exclusive_scan_i32(cnt.p, cnt.p, m + 1, nullptr, tmp.p, s);
   PI_CUDA(cudaMemcpyAsync(&total, cnt.p + m, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -161,7 +268,10 @@ long long neighbors(pi_frame* f, const float* h_pts, long long m, long long* h_o
   if (total > cap) return total;
   DBuf<int> out;
   out.alloc(f->ctx, s, total > 0 ? total : 1);
-  PI_LAUNCH(k_nb_fill, div_up(m, 128), 128, 0, s, g, pts.p, m, cnt.p, f->sidx.p, out.p);
+  if (f->varR)
+    PI_LAUNCH(k_vr_nb_fill, div_up(m, 128), 128, 0, s, f->mgv.p, pts.p, m, cnt.p, f->sidx.p, out.p);
+  else
+    PI_LAUNCH(k_nb_fill, div_up(m, 128), 128, 0, s, g, pts.p, m, cnt.p, f->sidx.p, out.p);
   PI_CUDA(cudaMemcpyAsync(h_idx, out.p, sizeof(int) * total, cudaMemcpyDeviceToHost, s));
   PI_CUDA(cudaStreamSynchronize(s));
   return total;

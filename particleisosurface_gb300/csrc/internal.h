@@ -8,6 +8,7 @@
 
 #include "../../include/pisurf.h"
 #include "common.cuh"
+#include "device.cuh"
 
 struct pi_ctx;
 
@@ -32,6 +33,20 @@ struct DBuf {
   void release();
   ~DBuf() { release(); }
   size_t bytes() const { return n * sizeof(T); }
+};
+
+// One radius bin's hash grid (variable radius): the HashGrid of the bin's
+// particles (src/hash_grid.cpp:36-69).
+struct BinHost {
+  float bounding[6];
+  float cell;
+  int nx, ny, nz;
+  long long cellNum;
+  int offBase;         // first entry of the bin in the concatenated offsets
+  long long start;     // first sorted position of the bin's particles
+  long long count;
+  int radius_id;       // the particle whose radius sets the cell size
+  int bin;             // index of the bin among all radius bins
 };
 
 struct GridHost {
@@ -104,6 +119,20 @@ struct pi_frame {
   pisurf::DBuf<float> gfull;     // N*9, sorted order (dumps)
   pisurf::DBuf<float> det;       // N, sorted order (dumps)
   pisurf::DBuf<int8_t> f64flag;  // N, sorted order
+  // variable radius (pi_frame_upload_radii): host and device radii, the grid
+  // index of each particle, the bins' grids (host and a device view), the
+  // searcher's min / max / average radius and the per-node min radius
+  bool varR = false;
+  std::vector<float> hrad;
+  pisurf::DBuf<float> rad;
+  // per-particle kernel constants (Influnce2, Sigma, nI = 4 r, 1 / nI^3) with
+  // the reference's float / double semantics, original and sorted order
+  pisurf::DBuf<float4> vrc, vrcs;
+  pisurf::DBuf<int> pbin;
+  std::vector<pisurf::BinHost> bins;
+  pisurf::DBuf<pisurf::MultiGridView> mgv;
+  float vrMinR = 0, vrMaxR = 0, vrAvgR = 0;
+  pisurf::DBuf<float> nd_minr;
   // FP64 oracle state (fp64.cu), sorted order: centres, G, det; computed on
   // demand and invalid once the hash grid changes
   pisurf::DBuf<double> x64, g64, det64;
@@ -187,6 +216,14 @@ void resolve_pending(pi_frame* f);
 // std::length_error, before any int conversion could overflow, when an axis
 // or the product exceeds max_cells.
 long long grid_cell_counts(const float bounding[6], float cell, long long max_cells, int nn[3]);
+
+// Variable radius (varr.cu): radii upload, the bins' hash grids, the root
+// box and scalars (resizeRootBoxVarR, CalculateMaxScalarVarR,
+// RecommendIsoValueVarR); the anisotropy pass (aniso.cu).
+void stage_upload_radii(pi_frame* f, const float* radii, long long n);
+void stage_hashgrid_vr(pi_frame* f);
+void host_root_and_scalars_vr(pi_frame* f);
+void stage_aniso_vr(pi_frame* f);
 
 void stage_upload_host(pi_frame* f, const float* xyz, long long n);
 void stage_upload_device(pi_frame* f, const float* d_xyz, long long n);

@@ -448,7 +448,7 @@ __global__ void __launch_bounds__(64, 24) k_classify(LevelArgs a, const float* _
                            const float4* __restrict__ nd_c,
                            float4* __restrict__ nd_v, int8_t* __restrict__ nd_type, int8_t* __restrict__ nd_sc,
                            float* __restrict__ nd_curv, float* __restrict__ nd_samp, int qef, int curv_known,
-                           unsigned long long* __restrict__ counters) {
+                           unsigned long long* __restrict__ counters, const float* __restrict__ nd_minr) {
   const long long node = a.lb + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (node >= a.le) return;
@@ -467,7 +467,10 @@ __global__ void __launch_bounds__(64, 24) k_classify(LevelArgs a, const float* _
   const float vc = __shfl_sync(0xffffffffu, val, 27);
   if (qef && lane < 27) nd_samp[node * 27 + lane] = val;
   const float cellsize = 2.0f * c.w;
-  const bool leaf_by_size = (double)(cellsize - a.radius) < 1e-8;
+  // leaf by size: the node is no larger than the radius (variable radius:
+  // the smallest radius of the particles reaching it, src/surface_
+  // reconstructor.cpp:156,203-208,247)
+  const bool leaf_by_size = (double)(cellsize - (nd_minr ? nd_minr[node] : a.radius)) < 1e-8;
   int8_t type = T_LEAF;
   float curv = -1.0f;
   if (!leaf_by_size && signchange && curv_known) {
@@ -954,7 +957,8 @@ static void ensure_nodes(pi_frame* f, long long need) {
   // (pi_reconstruct reuses its frame across parameters) may hold node arrays
   // large enough and no samples yet
   const bool samp_ok = !f->P.qef || (long long)f->nd_samp.n >= need * 27;
-  if ((long long)f->nd_c.n >= need && samp_ok) return;
+  const bool minr_ok = !f->varR || (long long)f->nd_minr.n >= need;
+  if ((long long)f->nd_c.n >= need && samp_ok && minr_ok) return;
   long long cap = std::max<long long>(need, (long long)(f->nd_c.n * 3 / 2) + 1024);
   pi_ctx* c = f->ctx;
   cudaStream_t s = c->stream;
@@ -970,12 +974,232 @@ static void ensure_nodes(pi_frame* f, long long need) {
   f->nd_curv.grow(c, s, cap, keep);
   f->nd_org.grow(c, s, cap, keep);
   if (f->P.qef) f->nd_samp.grow(c, s, cap * 27, keep * 27);
+  if (f->varR) f->nd_minr.grow(c, s, cap, keep);
+}
+
+// ---------------------------------------------------------------------------
+// Variable radius.  checkEmptyAndCalcCurv with per-particle radii
+// (src/surface_reconstructor.cpp:152-222): a particle reaches a node when it
+// lies strictly inside the node box grown by its own radius * smooth_factor;
+// the node is empty when none does, else its curvature sums run over those
+// particles and min_radius is their smallest radius, which makes the node a
+// leaf by size when cellsize - min_radius < 1e-8 (:247).  One warp per node
+// over the cells of every bin's grid that the box grown by the largest
+// radius touches (the reference's GetInBoxParticles, box +- 1 cell, is a
+// superset of these).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(64) k_vr_empty(const MultiGridView* __restrict__ mg, LevelArgs a,
+                                                 float emax, const float4* __restrict__ nd_c,
+                                                 float4* __restrict__ nd_v, int8_t* __restrict__ nd_type,
+                                                 float* __restrict__ nd_curv, float* __restrict__ nd_minr) {
+  const long long node = a.lb + (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (node >= a.le) return;
+  const MultiGridView& m = *mg;
+  const float4 c = nd_c[node];
+  const float h = c.w;
+  const float b1x = __fsub_rn(c.x, h), b1y = __fsub_rn(c.y, h), b1z = __fsub_rn(c.z, h);
+  const float b2x = __fadd_rn(c.x, h), b2y = __fadd_rn(c.y, h), b2z = __fadd_rn(c.z, h);
+  bool found = false;
+  float minr = 3.402823466e38f;
+  Kahan sx, sy, sz, ar;
+  for (int b = 0; b < m.nb; ++b) {
+    const BinGrid g = m.g[b];
+    const int x0 = max(cell_coord(__fsub_rn(b1x, emax), g.b0, g.cell, g.nx), 0);
+    const int y0 = max(cell_coord(__fsub_rn(b1y, emax), g.b2, g.cell, g.ny), 0);
+    const int z0 = max(cell_coord(__fsub_rn(b1z, emax), g.b4, g.cell, g.nz), 0);
+    const int x1 = min(cell_coord(__fadd_rn(b2x, emax), g.b0, g.cell, g.nx), g.nx - 1);
+    const int y1 = min(cell_coord(__fadd_rn(b2y, emax), g.b2, g.cell, g.ny), g.ny - 1);
+    const int z1 = min(cell_coord(__fadd_rn(b2z, emax), g.b4, g.cell, g.nz), g.nz - 1);
+    if (x0 > x1 || y0 > y1 || z0 > z1) continue;
+    const int nyb = y1 - y0 + 1;
+    const int rows = (z1 - z0 + 1) * nyb;
+    for (int r = lane; r < rows; r += 32) {
+      const int z = z0 + r / nyb, y = y0 + r % nyb;
+      const long long base = (long long)g.offBase + ((long long)z * g.ny + y) * g.nx;
+      const int s = __ldg(m.off + base + x0), e = __ldg(m.off + base + x1 + 1);
+      for (int j = s; j < e; ++j) {
+        const float4 p = __ldg(a.pos + j);
+        const float ej = p.w * a.expand;  // r_j * smooth_factor
+        if (p.x > __fsub_rn(b1x, ej) && p.x < __fadd_rn(b2x, ej) && p.y > __fsub_rn(b1y, ej) &&
+            p.y < __fadd_rn(b2y, ej) && p.z > __fsub_rn(b1z, ej) && p.z < __fadd_rn(b2z, ej)) {
+          found = true;
+          minr = fminf(minr, p.w);
+          const float4 nv = __ldg(a.nrm + j);
+          sx.add(nv.x);
+          sy.add(nv.y);
+          sz.add(nv.z);
+          ar.add(nv.w);
+        }
+      }
+    }
+  }
+  found = __any_sync(0xffffffffu, found);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) minr = fminf(minr, __shfl_xor_sync(0xffffffffu, minr, o));
+  const float nx = warp_sum(sx.s - sx.c), ny = warp_sum(sy.s - sy.c), nz = warp_sum(sz.s - sz.c);
+  const float area = warp_sum(ar.s - ar.c);
+  if (lane == 0) {
+    if (!found) {
+      nd_type[node] = T_EMPTY;
+      nd_curv[node] = 1.0f;
+      float4 v = nd_v[node];
+      v.w = a.iso;
+      nd_v[node] = v;
+    } else {
+      // above D_min a node is INTERNAL unless it is a leaf by size already
+      // (every particle reaching it is at least its size; afterSampleEval
+      // tests the size first, :247): then it waits for its value
+      const bool leaf_by_size = (double)(2.0f * h - minr) < 1e-8;
+      nd_type[node] = (a.big && !leaf_by_size) ? T_INTERNAL : T_UNCERTAIN;
+      nd_curv[node] = (area == 0.f) ? 1.0f : sqrtf(nx * nx + ny * ny + nz * nz) / area;
+      nd_minr[node] = minr;
+    }
+  }
+}
+
+// Leaves by size above D_min (variable radius only): no GridEval there, the
+// value is SingleEval at the node position (src/surface_reconstructor.cpp:
+// 245-253).
+__global__ void k_vr_big_leaf(const MultiGridView* __restrict__ mg, LevelArgs a, float4* __restrict__ nd_v,
+                              int8_t* __restrict__ nd_type, unsigned long long* __restrict__ counters) {
+  const long long node = a.lb + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (node >= a.le || nd_type[node] != T_UNCERTAIN) return;
+  float4 v = nd_v[node];
+  v.w = a.iso - field_sum_vr(*mg, a.P, v.x, v.y, v.z, nullptr);
+  nd_v[node] = v;
+  nd_type[node] = T_LEAF;
+  stripe_add(counters, C_REF_EVALS, 1ull);
+  stripe_add(counters, C_DONE_THREAD, 1ull);
+}
+
+// Field at the distinct samples of a level, one thread per sample in bucket
+// order, over the bins' candidate lists.
+__global__ void __launch_bounds__(256, 4) k_vr_q_eval_thread(const MultiGridView* __restrict__ mg, QArgs a,
+                                                             const int* __restrict__ list,
+                                                             const int* __restrict__ count_ptr,
+                                                             const float4* __restrict__ nd_c,
+                                                             const float4* __restrict__ nd_v, float* __restrict__ qval,
+                                                             unsigned long long* __restrict__ counters) {
+  const int n = *count_ptr;
+  long long pairs = 0, done = 0;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int q = list[t];
+    const long long node = a.lb + q / kQ;
+    float qx, qy, qz;
+    sample_point(nd_c[node], nd_v[node], q % kQ, qx, qy, qz);
+    qval[q] = a.iso - field_sum_vr(*mg, a.P, qx, qy, qz, &pairs);
+    ++done;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+    done += __shfl_xor_sync(0xffffffffu, done, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    stripe_add(counters, C_SAMPLE_PAIRS, (unsigned long long)pairs);
+    stripe_add(counters, C_PAIRS_THREAD, (unsigned long long)pairs);
+    stripe_add(counters, C_DONE_THREAD, (unsigned long long)done);
+  }
+}
+
+// genIsoOurs state 0 with per-particle radii: every level runs the
+// emptiness scan above, then (depth >= D_min) the sampling, one thread per
+// distinct sample, and the classification with each node's min_radius.
+static void stage_octree_vr(pi_frame* f) {
+  pi_ctx* ctx = f->ctx;
+  cudaStream_t s = ctx->stream;
+  f->nNodes = 0;
+  f->levelBegin.clear();
+  ensure_nodes(f, 1 << 16);
+  if (!f->ev[kLevelEvent]) PI_CUDA(cudaEventCreateWithFlags(&f->ev[kLevelEvent], cudaEventDisableTiming));
+  PI_LAUNCH(k_root, 1, 1, 0, s, f->rootC[0], f->rootC[1], f->rootC[2], f->rootH, 1 << f->dmax, f->nd_c.p,
+            f->nd_v.p, f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p,
+            f->nd_curv.p, f->nd_org.p);
+  f->nNodes = 1;
+  // sample buckets: a grid of cells 4 * maxR over the root box (it holds
+  // every sample), whole cells
+  const float bcell = f->vrMaxR * 4.0f;
+  const int bn = std::max(1, (int)std::ceil(2.0f * f->rootH / bcell));
+  GridView bg{f->rootC[0] - f->rootH, f->rootC[1] - f->rootH, f->rootC[2] - f->rootH, bcell, bn, bn, bn, nullptr};
+  PartView P{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p};
+  const int ekx = bn + 4, eky = bn + 4;
+  const long long nb = (long long)ekx * eky * (bn + 4);
+  counters_reset(f);
+  DBuf<int> flag, qcnt, qkey, rep, order, ucnt, ucum;
+  DBuf<unsigned> hslot;
+  DBuf<float> qval;
+  qcnt.alloc(ctx, s, nb + 2);
+  ucnt.alloc(ctx, s, nb + 1);
+  ucum.alloc(ctx, s, nb + 1);
+  long long lb = 0, le = 1;
+  for (int depth = 0; le > lb; ++depth) {
+    f->levelBegin.push_back(lb);
+    const long long nl = le - lb;
+    LevelArgs la{bg, f->pos.p, f->nrm.p, f->P.smooth_factor, f->iso, f->vrMinR, lb, le, depth < f->dmin ? 1 : 0, P};
+    PI_LAUNCH(k_vr_empty, div_up(nl, 2), 64, 0, s, f->mgv.p, la, f->vrMaxR * f->P.smooth_factor, f->nd_c.p,
+              f->nd_v.p, f->nd_type.p, f->nd_curv.p, f->nd_minr.p);
+    if (depth < f->dmin)
+      PI_LAUNCH(k_vr_big_leaf, div_up(nl, 128), 128, 0, s, f->mgv.p, la, f->nd_v.p, f->nd_type.p, f->dcount.p);
+    if (depth >= f->dmin) {
+      const long long qn = nl * kQ;
+      if (f->tmp.n < scan_tmp_ints(nb + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(nb + 1));
+      qkey.alloc(ctx, s, qn);
+      rep.alloc(ctx, s, qn);
+      hslot.alloc(ctx, s, 2 * qn);
+      qval.alloc(ctx, s, qn);
+      order.alloc(ctx, s, qn);
+      PI_CUDA(cudaMemsetAsync(qcnt.p, 0, sizeof(int) * (nb + 2), s));
+      PI_CUDA(cudaMemsetAsync(ucnt.p, 0, sizeof(int) * (nb + 1), s));
+      PI_CUDA(cudaMemsetAsync(hslot.p, 0, sizeof(unsigned) * 2 * qn, s));
+      QArgs qa{bg, P, f->iso, lb, le, ekx, eky, 0};
+      PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
+      exclusive_scan_i32(qcnt.p, qcnt.p, nb + 1, nullptr, f->tmp.p, s);
+      PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
+                ucnt.p, rep.p, order.p);
+      int* list = reinterpret_cast<int*>(hslot.p);
+      exclusive_scan_i32(ucnt.p, ucum.p, nb + 1, nullptr, f->tmp.p, s);
+      PI_LAUNCH(k_q_compact, div_up(nb, 256), 256, 0, s, nb, qcnt.p, ucnt.p, ucum.p, order.p, list);
+      prof_begin(ctx, s, PG_THREAD);
+      PI_LAUNCH(k_vr_q_eval_thread, (int)std::min<long long>((long long)ctx->smCount * 8, div_up(qn, 256)), 256, 0,
+                s, f->mgv.p, qa, list, ucum.p + nb, f->nd_c.p, f->nd_v.p, qval.p, f->dcount.p);
+      prof_end(ctx, s, PG_THREAD);
+      const int wpb = 2;
+      PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p, f->nd_type.p,
+                f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, 0, 1, f->dcount.p, (const float*)f->nd_minr.p);
+    }
+    flag.alloc(ctx, s, nl + 1);
+    if (f->tmp.n < scan_tmp_ints(nl + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(nl + 1));
+    PI_LAUNCH(k_internal_flag, div_up(nl, 256), 256, 0, s, f->nd_type.p, lb, le, flag.p);
+    PI_CUDA(cudaMemsetAsync(flag.p + nl, 0, sizeof(int), s));
+    exclusive_scan_i32(flag.p, flag.p, nl + 1, nullptr, f->tmp.p, s);
+    int* const nint_h = reinterpret_cast<int*>(ctx->hpin + kPinSlots * kCounterWords + 1);
+    PI_CUDA(cudaMemcpyAsync(nint_h, flag.p + nl, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PI_CUDA(cudaEventRecord(f->ev[kLevelEvent], s));
+    f->nNodes = le;
+    ensure_nodes(f, le + 8 * nl);
+    PI_LAUNCH(k_spawn, div_up(nl, 256), 256, 0, s, lb, le, le, flag.p, f->nd_type.p, depth + 1, f->nd_c.p, f->nd_v.p,
+              f->nd_id.p, f->nd_parent.p, f->nd_child.p, f->nd_type.p, f->nd_depth.p, f->nd_sc.p, f->nd_curv.p,
+              f->nd_org.p);
+    PI_CUDA(cudaEventSynchronize(f->ev[kLevelEvent]));
+    const int nint = *nint_h;
+    const long long newn = 8LL * nint;
+    f->nNodes = le + newn;
+    if (nint == 0 || depth >= f->dmax) break;
+    lb = le;
+    le = le + newn;
+  }
+  counters_snapshot(f, kPinOctree);
 }
 
 void stage_octree(pi_frame* f) {
   pi_ctx* ctx = f->ctx;
   cudaStream_t s = ctx->stream;
   if (f->dmax > 20) throw std::length_error("octree depth above 20");
+  if (f->varR) {
+    stage_octree_vr(f);
+    return;
+  }
   f->nNodes = 0;
   f->levelBegin.clear();
   ensure_nodes(f, 1 << 16);
@@ -1099,7 +1323,8 @@ void stage_octree(pi_frame* f) {
                   s, qa, list, ucum.p + nb, f->nd_c.p, f->nd_v.p, qval.p, f->dcount.p);
       prof_end(ctx, s, pg);
       PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p, f->nd_type.p,
-                f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p);
+                f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p,
+                (const float*)nullptr);
       if (f->P.qef) qef_level(f, lb, le, depth, qkey.p);  // the sample keys are spent (qn >= nl + 1)
     }
     flag.alloc(ctx, s, nl + 1);

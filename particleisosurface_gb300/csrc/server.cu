@@ -14,8 +14,8 @@
 // with a budget, the worker's context is capped at that reservation, so a
 // frame cannot take more than it was admitted with: a frame that needs more
 // fails inside the worker with PI_ERR_NOMEM and goes back to the head of the
-// queue with its reservation doubled (until it would exceed the whole
-// budget; then the request fails with PI_ERR_NOMEM).  When the head request
+// queue with its reservation doubled, up to the whole budget (a frame that
+// needs more than the whole budget fails with PI_ERR_NOMEM).  When the head request
 // does not fit, up to kLookahead requests behind it may pass it if they fit,
 // but no request is passed more than kMaxBypass times, so a large request
 // cannot starve.
@@ -53,9 +53,11 @@ static double now_ms() {
 }
 
 // Device bytes of one frame, per particle plus a fixed part (hash grid and
-// per-particle arrays ~160 B, octree nodes and per-level sample buffers and
-// extraction sort buffers ~2 KB at the configurations' surface densities).
-constexpr size_t kEstPerParticle = 2304, kEstFixed = 64ull << 20;
+// per-particle arrays ~190 B, octree nodes, per-level sample buffers and
+// extraction tables ~2-3 KB at the configurations' surface densities; the
+// fixed part covers the per-cell bucket tables and the corner bitmap of
+// small frames).
+constexpr size_t kEstPerParticle = 3072, kEstFixed = 128ull << 20;
 
 constexpr int kLookahead = 16;  // queued requests that may pass a blocked head
 constexpr int kMaxBypass = 8;   // times one request may be passed
@@ -215,9 +217,10 @@ static void worker_main(pi_server* s, int slot) {
     std::string err = rc0 ? std::string(pi_last_error()) : std::string();
     size_t held = 0;
     if (!rc) {
-      // a budget caps the context at the request's reservation; a resident
-      // frame holding more than that is given back first
-      ctx->budget = s->budget ? r->est : 0;
+      // a budget caps the context at the request's reservation (at most the
+      // whole budget); a resident frame holding more than that is given back
+      // first
+      ctx->budget = s->budget ? std::min(r->est, s->budget) : 0;
       if (kept && s->budget && (size_t)ctx->used.load() > r->est) {
         pi_frame_destroy(kept);
         kept = nullptr;
@@ -260,10 +263,10 @@ static void worker_main(pi_server* s, int slot) {
       s->reserved -= r->est;
       s->in_flight--;
       s->busy[slot] = 0;
-      if (rc == PI_ERR_NOMEM && s->budget && r->est * 2 <= s->budget) {
+      if (rc == PI_ERR_NOMEM && s->budget && r->est < s->budget) {
         // the frame needs more than its reservation: back to the head with
-        // twice as much
-        r->est *= 2;
+        // twice as much, at most the whole budget
+        r->est = std::min(r->est * 2, s->budget);
         r->retries++;
         s->retries++;
         s->queue.push_front(r);

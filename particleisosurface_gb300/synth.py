@@ -298,6 +298,29 @@ def sheets_and_filaments(n=500_000, radius=0.01, seed=4) -> Frame:
     return Frame(pts, radius, scale, seed, "sheets_filaments_%d" % n)
 
 
+@dataclasses.dataclass
+class VarFrame(Frame):
+    radii: np.ndarray = None  # (n,) float32 per-particle radii
+
+
+def two_radius_frame(n=20000, seed=6, r_small=0.01, r_large=0.02, jitter=0.2) -> VarFrame:
+    """Variable-radius frame: a jittered-lattice slab of small particles
+    (radius r_small, spacing 2 r_small) under a jittered-lattice sphere of
+    large particles (radius r_large, spacing 2 r_large), each half of the
+    particles; the geometry is scaled about the origin until each part holds
+    its count, as the other generators do."""
+    rng = np.random.default_rng(seed)
+    n_small = n // 2
+    n_large = n - n_small
+    slab = lambda s: _lattice_box(np.array([0.0, 0.0, 0.0]), np.array([0.6, 0.15, 0.6]) * s, 2 * r_small)
+    pts_s, s1 = _scaled_lattice(slab, n_small, rng)
+    sph = lambda s: _lattice_sphere(np.array([0.3, 0.45, 0.3]) * s1, 0.18 * s, 2 * r_large)
+    pts_l, _ = _scaled_lattice(sph, n_large, rng)
+    pts = np.concatenate([_jitter(pts_s, jitter * r_small, rng), _jitter(pts_l, jitter * r_large, rng)])
+    radii = np.concatenate([np.full(len(pts_s), r_small, np.float32), np.full(len(pts_l), r_large, np.float32)])
+    return VarFrame(pts, r_small, s1, seed, "two_radius_%d" % n, radii)
+
+
 def advect(xyz, w, g, t, dt, steps=1, scale=1.0):
     """Swirl plus gravity u = (-w (y - 0.5), w (x - 0.5), -g t) in the unit box
     scaled by `scale` (the geometry rule scales the domain with the particle

@@ -214,3 +214,61 @@ def test_uniform_grid_lattice_and_values():
     pts = np.array([[coord(0, x), coord(1, y), coord(2, z)] for z, y, x in idx], np.float32)
     ev = o.eval(pts)
     np.testing.assert_array_equal(np.array([vals[k] for k in idx]), ev)
+
+
+def test_variable_radius_with_equal_radii_matches_constant_radius():
+    """The variable-radius path (MultiLevelSearcher, per-particle kernel
+    constants) with every radius equal: a single radius bin whose grid is the
+    constant-radius grid, so keys, cell order, smoothed centres, G and the
+    field are the constant-radius path's bit for bit (src/evaluator.cpp:16-37
+    compute the same float constants either way)."""
+    fr = synth.small_blob(n=1500, seed=5)
+    c = O.OracleFrame(fr.xyz, fr.radius)
+    v = O.OracleFrame(fr.xyz, np.full(fr.n, fr.radius, np.float32))
+    for s in (1, 2):
+        c.stage(s)
+        v.stage(s)
+    bins = v.bins()
+    assert len(bins) == 1
+    gi = c.grid_info()
+    np.testing.assert_array_equal(bins[0]["bounding"], gi["bounding"])
+    assert bins[0]["cell_num"] == gi["cell_num"]
+    np.testing.assert_array_equal(bins[0]["keys"], c.keys())
+    np.testing.assert_array_equal(bins[0]["index_list"], c.index_list())
+    for a, b in zip(c.aniso(), v.aniso()):
+        np.testing.assert_array_equal(a, b)
+    rng = np.random.default_rng(1)
+    pts = (fr.xyz[rng.choice(fr.n, 300)] + rng.normal(0, fr.radius, (300, 3))).astype(np.float32)
+    off_c, idx_c = c.neighbors(pts)
+    off_v, idx_v = v.neighbors(pts)
+    np.testing.assert_array_equal(off_c, off_v)
+    np.testing.assert_array_equal(idx_c, idx_v)
+    # the searcher's radii: min * 0.99, max * 1.01
+    sr = v.searcher_radii()
+    assert sr["min"] == np.float32(np.float32(fr.radius) * 0.99) or abs(sr["min"] / fr.radius - 0.99) < 1e-6
+
+
+def test_variable_radius_bins_and_frame():
+    """Two radii, r and 2r: the searcher bins them (bin width about min / 2),
+    each bin's grid has the cell size of its largest radius times 4, the
+    neighbour list of a point is the bins' 27-cell lists in bin order, and a
+    whole frame reconstructs (leaves at the depth of the smallest radius
+    inside them)."""
+    fr = synth.two_radius_frame(n=4000, seed=6)
+    o = O.OracleFrame(fr.xyz, fr.radii)
+    o.run()
+    bins = o.bins()
+    assert len(bins) == 2
+    radii = fr.radii
+    for b in bins:
+        assert b["cell_size"] == np.float32(radii[b["radius_id"]] * np.float32(4.0))
+        assert np.all(radii[b["particles"]] <= radii[b["radius_id"]])
+        # IndexList is the bin's particles ordered by (key, particle)
+        order = np.lexsort((b["particles"], b["keys"]))
+        np.testing.assert_array_equal(b["index_list"], b["particles"][order])
+    assert sum(len(b["particles"]) for b in bins) == fr.n
+    v, t, k = o.mesh()
+    assert len(v) > 100 and len(t) > 100
+    nodes = o.nodes()
+    leaves = nodes["type"] == 2
+    assert leaves.any()
