@@ -267,6 +267,12 @@ static void need(const pi_frame* f, int stage) {
   if (f->stage < stage) throw StateError("stage called before the stages it depends on");
 }
 
+// The uniform grid, the box query and the FP64 oracle are built for one
+// hash grid (a constant radius).
+static void const_radius_only(const pi_frame* f) {
+  if (f->varR) throw StateError("not available with per-particle radii");
+}
+
 // An NVTX range per stage (names as the reference's printf stage titles), so
 // a timeline tool shows the stages; free when no tool is attached.
 struct NvtxRange {
@@ -797,6 +803,7 @@ int pi_fp64_aniso(pi_frame* f, double* xmeans3, double* g9, double* det) {
   PI_API_BEGIN
   PI_CHECK(f, "frame is null");
   need(f, 2);
+  const_radius_only(f);
   set_device(f->ctx);
   fp64_aniso_get(f, xmeans3, g9, det);
   PI_API_END
@@ -806,6 +813,7 @@ int pi_fp64_eval_field(pi_frame* f, const float* pts, int64_t m, double* scalar,
   PI_API_BEGIN
   PI_CHECK(f && pts && scalar && m > 0, "bad arguments");
   need(f, 2);
+  const_radius_only(f);
   set_device(f->ctx);
   cudaStream_t s = f->ctx->stream;
   DBuf<float> dp;
@@ -850,6 +858,7 @@ int pi_grid_dims(pi_frame* f, int32_t* dims3, float* box6, int64_t* npoints) {
   PI_API_BEGIN
   PI_CHECK(f && dims3, "bad arguments");
   need(f, 2);
+  const_radius_only(f);
   float box[6];
   int steps[3], dims[3];
   uniform_grid_host(f, box, steps, dims);
@@ -864,6 +873,7 @@ int pi_grid_sample_device(pi_frame* f, float* d_values, int64_t cap) {
   PI_API_BEGIN
   PI_CHECK(f && d_values, "bad arguments");
   need(f, 4);
+  const_radius_only(f);
   set_device(f->ctx);
   const long long total = grid_sample(f, d_values, cap);
   if (total > cap) throw std::length_error("value buffer too small for the lattice");
@@ -874,6 +884,7 @@ int pi_grid_sample(pi_frame* f, float* values, int64_t cap) {
   PI_API_BEGIN
   PI_CHECK(f && values, "bad arguments");
   need(f, 4);
+  const_radius_only(f);
   set_device(f->ctx);
   cudaStream_t s = f->ctx->stream;
   const long long total = grid_sample(f, nullptr, 0);
@@ -890,6 +901,7 @@ int pi_grid_write_vti(pi_frame* f, const char* path) {
   PI_API_BEGIN
   PI_CHECK(f && path, "bad arguments");
   need(f, 4);
+  const_radius_only(f);
   set_device(f->ctx);
   float box[6];
   int steps[3], dims[3];
@@ -991,6 +1003,7 @@ int pi_hashgrid_in_box(pi_frame* f, const float* b1, const float* b2, int32_t* i
   PI_API_BEGIN
   PI_CHECK(f && b1 && b2 && total, "bad arguments");
   need(f, 2);
+  const_radius_only(f);
   set_device(f->ctx);
   long long t = in_box(f, b1, b2, idx, idx ? cap : 0);
   *total = t;
