@@ -25,6 +25,9 @@
 //   writeObjFile        src/main.cpp:54-67
 //   writePlyFile, loadParticlesFromCSV  src/main.cpp:69-114, 215-275
 //   UniformGrid         include/marching.h:18-70 (dense-grid mode)
+//   MultiLevelSearcher  include/multi_level_researcher.h:8-40 (per-particle radii)
+//   IS_CONST_RADIUS     include/iso_common.h:6, defined by the host program
+//                       (src/main.cpp:32) unless PISURF_NO_GLOBAL_NAMES is set
 #ifndef PISURF_HPP
 #define PISURF_HPP
 
@@ -38,6 +41,13 @@
 #include <vector>
 
 #include "pisurf.h"
+
+#ifndef PISURF_NO_GLOBAL_NAMES
+// The reference's run-mode switch: true for one radius, false for the
+// per-particle radii passed to SurfReconstructor.  The host program defines
+// it, as the reference's main does.
+extern bool IS_CONST_RADIUS;
+#endif
 
 namespace pisurf {
 
@@ -197,7 +207,53 @@ struct Frame {
   }
 };
 
+inline bool const_radius_mode() {
+#ifndef PISURF_NO_GLOBAL_NAMES
+  return ::IS_CONST_RADIUS;
+#else
+  return true;
+#endif
+}
 }  // namespace detail
+
+// MultiLevelSearcher (src/multi_level_reseacher.cpp): the radius bins of a
+// frame with per-particle radii, one hash grid per non-empty bin, built by
+// SurfReconstructor::Run.  GetNeighbors runs on the GPU.
+class MultiLevelSearcher {
+ public:
+  explicit MultiLevelSearcher(std::shared_ptr<detail::Frame> f) : frame_(std::move(f)) {
+    const pi_frame_info fi = frame_->info();
+    minRadius_ = fi.radius_min;
+    maxRadius_ = fi.radius_max;
+    particlesNum_ = (unsigned int)fi.num_particles;
+    grids_ = fi.num_grids;
+  }
+  float getMaxRadius() const { return maxRadius_; }
+  float getMinRadius() const { return minRadius_; }
+  float getParticlesNum() const { return (float)particlesNum_; }
+  // the number of hash grids (getSearchers()->size() in the reference)
+  int getSearchersNum() const { return grids_; }
+  // GetNeighbors (src/multi_level_reseacher.cpp:79-92): the bins' 27-cell
+  // candidate lists, in bin order.
+  void GetNeighbors(const Vector3f& pos, std::vector<int>& neighbors) {
+    const float p[3] = {pos[0], pos[1], pos[2]};
+    int64_t off[2] = {0, 0}, total = 0;
+    neighbors.assign(1024, 0);
+    int rc = pi_hashgrid_neighbors(frame_->h, p, 1, off, neighbors.data(), (int64_t)neighbors.size(), &total);
+    if (rc == PI_ERR_LIMIT) {
+      neighbors.assign((size_t)total, 0);
+      rc = pi_hashgrid_neighbors(frame_->h, p, 1, off, neighbors.data(), total, &total);
+    }
+    check(rc);
+    neighbors.resize((size_t)total);
+  }
+
+ private:
+  std::shared_ptr<detail::Frame> frame_;
+  float minRadius_ = 0.f, maxRadius_ = 0.f;
+  unsigned int particlesNum_ = 0;
+  int grids_ = 0;
+};
 
 // HashGrid, constant radius (src/hash_grid.cpp).  Built by
 // SurfReconstructor::Run; the queries run on the GPU.
@@ -395,14 +451,16 @@ struct TNode {
   bool is_leaf() const { return type == LEAF || type == EMPTY; }
 };
 
-// SurfReconstructor (src/surface_reconstructor.cpp), constant radius.
+// SurfReconstructor (src/surface_reconstructor.cpp).  Run reads
+// IS_CONST_RADIUS as the reference does: when it is false the frame takes the
+// per-particle radii (radiuses, one per particle) and the radius argument is
+// not used.
 class SurfReconstructor {
  public:
   SurfReconstructor() = default;
   SurfReconstructor(std::vector<Vector3f>& particles, std::vector<float>& radiuses, Mesh* mesh, float radius,
                     int device = 0)
-      : mesh_(mesh), radius_(radius), device_(device) {
-    (void)radiuses;  // constant-radius path: the per-particle radii are not read
+      : mesh_(mesh), radius_(radius), device_(device), radii_(radiuses) {
     xyz_.resize(particles.size() * 3);
     for (size_t i = 0; i < particles.size(); ++i)
       for (int c = 0; c < 3; ++c) xyz_[3 * i + c] = particles[i][c];
@@ -417,11 +475,19 @@ class SurfReconstructor {
     p.smooth_factor = smooth_factor;
     p.iso_factor = iso_factor;
     p.qef = qef_ ? 1 : 0;
+    const bool var_r = !detail::const_radius_mode();
+    if (var_r && !radii_.empty()) {
+      float lo = radii_[0];
+      for (float r : radii_) lo = r < lo ? r : lo;
+      p.radius = lo;  // not used by the variable-radius path; any valid radius
+    }
     frame_ = std::make_shared<detail::Frame>(detail::Context::get(device_), p);
     check(pi_frame_upload(frame_->h, xyz_.data(), (int64_t)(xyz_.size() / 3)));
+    if (var_r) check(pi_frame_upload_radii(frame_->h, radii_.data(), (int64_t)radii_.size()));
     check(pi_run(frame_->h));
     info_ = frame_->info();
-    hashgrid_ = std::make_shared<HashGrid>(frame_);
+    searcher_ = var_r ? std::make_shared<MultiLevelSearcher>(frame_) : nullptr;
+    hashgrid_ = var_r ? nullptr : std::make_shared<HashGrid>(frame_);
     evaluator_ = std::make_shared<Evaluator>(frame_, smooth_factor, iso_factor);
     root_.reset();
     if (mesh_) {
@@ -455,6 +521,7 @@ class SurfReconstructor {
   int getDepthMax() const { return info_.depth_max; }
   int getDepthMin() const { return info_.depth_min; }
   std::shared_ptr<HashGrid> getHashGrid() const { return hashgrid_; }
+  std::shared_ptr<MultiLevelSearcher> getSearcher() const { return searcher_; }
   std::shared_ptr<Evaluator> getEvaluator() const { return evaluator_; }
   int getGlobalParticlesNum() const { return (int)(xyz_.size() / 3); }
   float getConstRadius() const { return radius_; }
@@ -490,11 +557,13 @@ class SurfReconstructor {
   Mesh* mesh_ = nullptr;
   float radius_ = 0.f;
   int device_ = 0;
+  std::vector<float> radii_;
   bool qef_ = false;
   int state_ = 0;
   pi_frame_info info_{};
   std::shared_ptr<detail::Frame> frame_;
   std::shared_ptr<HashGrid> hashgrid_;
+  std::shared_ptr<MultiLevelSearcher> searcher_;
   std::shared_ptr<Evaluator> evaluator_;
   std::shared_ptr<TNode> root_;
 };
@@ -555,6 +624,7 @@ using pisurf::UniformGrid;
 using pisurf::Evaluator;
 using pisurf::HashGrid;
 using pisurf::Mesh;
+using pisurf::MultiLevelSearcher;
 using pisurf::SurfReconstructor;
 using pisurf::TNode;
 using pisurf::Triangle;

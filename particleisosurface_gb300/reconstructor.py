@@ -9,7 +9,10 @@ Everything runs in the CUDA library through the C ABI (include/pisurf.h);
 the facade only moves arrays.  Reference interfaces mirrored:
 SurfReconstructor (include/surface_reconstructor.h:71-92), Evaluator
 (include/evaluator.h:76-95), HashGrid (include/hash_grid.h:16-38),
-Mesh (include/global.h:86-115).
+MultiLevelSearcher (include/multi_level_researcher.h:8-40), Mesh
+(include/global.h:86-115), and the run-mode switch IS_CONST_RADIUS
+(include/iso_common.h:6): set it to False, as the reference's main does for
+per-particle radii, and SurfReconstructor.Run uses `radiuses`.
 """
 from __future__ import annotations
 
@@ -18,6 +21,8 @@ import numpy as np
 from . import _native as N
 
 _default_ctx = None
+
+IS_CONST_RADIUS = True
 
 
 def default_context():
@@ -131,20 +136,57 @@ class Evaluator:
         return self._f.dump(N.DUMP_NORMALS)
 
 
+class MultiLevelSearcher:
+    """The radius bins of a frame with per-particle radii
+    (src/multi_level_reseacher.cpp): one hash grid per non-empty bin."""
+
+    def __init__(self, frame):
+        self._f = frame
+        info = frame.info()
+        self._min, self._max, self._n = info["radius_min"], info["radius_max"], info["num_particles"]
+        self._grids = [frame.grid(k) for k in range(info["num_grids"])]
+
+    def getMinRadius(self):
+        return self._min
+
+    def getMaxRadius(self):
+        return self._max
+
+    def getParticlesNum(self):
+        return self._n
+
+    def getSearchers(self):
+        """One record per bin grid: bounding, dims, cell_size, count, radius_id."""
+        return self._grids
+
+    def GetNeighbors(self, pos):
+        """GetNeighbors (src/multi_level_reseacher.cpp:79-92)."""
+        off, idx = self._f.neighbors(np.asarray(pos, np.float32).reshape(1, 3))
+        return idx.tolist()
+
+
 class SurfReconstructor:
     def __init__(self, particles, radiuses, mesh: Mesh, radius: float, ctx: N.Context | None = None,
                  qef: bool = False):
         self._particles = np.ascontiguousarray(np.asarray(particles, np.float32).reshape(-1, 3))
+        self._radiuses = np.ascontiguousarray(np.asarray(radiuses, np.float32).reshape(-1))
         self._radius = float(radius)
         self._mesh = mesh
         self._ctx = ctx or default_context()
         self._qef = qef
         self._frame = None
+        self._var_r = False
 
     def Run(self, iso_factor=1.9, smooth_factor=2.0):
         self._mesh.reset()
-        params = N.default_params(self._radius, smooth_factor=smooth_factor, iso_factor=iso_factor, qef=self._qef)
-        self._frame = N.Frame(self._ctx, params).upload(self._particles).run()
+        var_r = not IS_CONST_RADIUS
+        radius = float(self._radiuses.min()) if var_r and self._radiuses.size else self._radius
+        params = N.default_params(radius, smooth_factor=smooth_factor, iso_factor=iso_factor, qef=self._qef)
+        f = N.Frame(self._ctx, params).upload(self._particles)
+        if var_r:
+            f.upload_radii(self._radiuses)
+        self._var_r = var_r
+        self._frame = f.run()
         v, t, k = self._frame.mesh(keys=True)
         self._mesh.vertices = v
         self._mesh.tris = t + 1
@@ -172,7 +214,10 @@ class SurfReconstructor:
         return self._particles
 
     def getHashGrid(self):
-        return HashGrid(self._frame)
+        return None if self._var_r else HashGrid(self._frame)
+
+    def getSearcher(self):
+        return MultiLevelSearcher(self._frame) if self._var_r else None
 
     def getEvaluator(self):
         return Evaluator(self._frame)

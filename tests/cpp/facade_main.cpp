@@ -1,8 +1,9 @@
 // Host program written against the reference's C++ API (the calls of
 // runOurs, src/main.cpp:330-405), compiled against include/pisurf.hpp.
-//   facade_main <xyz float32 file | particles .csv> <n> <radius> <out.obj>
+//   facade_main <xyz float32 file | particles .csv> <n> <radius> <out.obj> [radii float32 file]
 // (also writes <out.obj>.ply, and <out.obj's directory>/grid.vti through
-// UniformGrid)
+// UniformGrid).  With a radii file the program runs as the reference does
+// with IS_CONST_RADIUS false: per-particle radii and MultiLevelSearcher.
 // Prints one JSON line; exits 3 when no CUDA device is usable (the library
 // has no CPU fallback).
 #include <cstdio>
@@ -12,9 +13,36 @@
 
 #include "pisurf.hpp"
 
+bool IS_CONST_RADIUS = true;
+
+// Variable-radius run: the mesh, the searcher's radii and one neighbour query.
+static int run_var_radius(std::vector<pisurf::Vector3f>& particles, std::vector<float>& radiuses, float radius,
+                          const char* out_obj) {
+  IS_CONST_RADIUS = false;
+  Mesh mesh;
+  try {
+    SurfReconstructor constructor(particles, radiuses, &mesh, radius);
+    constructor.Run(1.9f, 2.0f);
+    writeObjFile(mesh, out_obj);
+    std::shared_ptr<MultiLevelSearcher> searcher = constructor.getSearcher();
+    std::vector<int> nb;
+    searcher->GetNeighbors(particles[0], nb);
+    std::printf(
+        "{\"vertices\": %u, \"triangles\": %u, \"depth_max\": %d, \"depth_min\": %d, \"min_radius\": %.9g, "
+        "\"max_radius\": %.9g, \"grids\": %d, \"neighbors0\": %zu, \"has_hash_grid\": %d}\n",
+        mesh.verticesNum, mesh.trianglesNum, constructor.getDepthMax(), constructor.getDepthMin(),
+        searcher->getMinRadius(), searcher->getMaxRadius(), searcher->getSearchersNum(), nb.size(),
+        constructor.getHashGrid() ? 1 : 0);
+  } catch (const pisurf::Error& e) {
+    std::printf("{\"error\": %d, \"message\": \"%s\"}\n", e.code(), e.what());
+    return e.code() == PI_ERR_CUDA ? 3 : 1;
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
-  if (argc != 5) {
-    std::fprintf(stderr, "usage: %s xyz.f32 n radius out.obj\n", argv[0]);
+  if (argc != 5 && argc != 6) {
+    std::fprintf(stderr, "usage: %s xyz.f32 n radius out.obj [radii.f32]\n", argv[0]);
     return 2;
   }
   const long n = std::atol(argv[2]);
@@ -39,6 +67,16 @@ int main(int argc, char** argv) {
     }
     particles.resize((size_t)n);
     for (long i = 0; i < n; ++i) particles[i] = pisurf::Vector3f(raw[3 * i], raw[3 * i + 1], raw[3 * i + 2]);
+  }
+  if (argc == 6) {
+    radiuses.resize(particles.size());
+    std::ifstream rin(argv[5], std::ios::binary);
+    rin.read(reinterpret_cast<char*>(radiuses.data()), (std::streamsize)(radiuses.size() * sizeof(float)));
+    if (!rin) {
+      std::fprintf(stderr, "cannot read %s\n", argv[5]);
+      return 2;
+    }
+    return run_var_radius(particles, radiuses, radius, argv[4]);
   }
   radiuses.assign(particles.size(), radius);
 

@@ -63,3 +63,31 @@ def test_facade_obj_identical_to_library_writer(tmp_path):
     assert out["neighbors0"] == len(idx)
     assert out["key0"] == int(o.keys()[0])
     assert abs(out["scalar0"] - float(o.eval(fr.xyz[:1])[0])) <= 3e-5 * sc["max_scalar"]
+
+
+def test_facade_variable_radius_equals_library(tmp_path):
+    """IS_CONST_RADIUS false in the host program: SurfReconstructor takes the
+    per-particle radii (pi_frame_upload_radii), the mesh equals the
+    library's, and getSearcher() reports the searcher's radii and bins."""
+    exe = facade.build()
+    fr = synth.two_radius_frame(n=4000, seed=6)
+    src, rad = tmp_path / "xyz.f32", tmp_path / "r.f32"
+    fr.xyz.astype(np.float32).tofile(src)
+    fr.radii.astype(np.float32).tofile(rad)
+    r = subprocess.run([exe, str(src), str(fr.n), "0.5", str(tmp_path / "facade.obj"), str(rad)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    ctx = N.Context(0)
+    f = N.Frame(ctx, N.default_params(float(fr.radii.min()))).upload(fr.xyz).upload_radii(fr.radii).run()
+    f.write_obj(str(tmp_path / "lib.obj"))
+    assert (tmp_path / "facade.obj").read_bytes() == (tmp_path / "lib.obj").read_bytes()
+    info = f.info()
+    assert out["grids"] == info["num_grids"] >= 2 and out["has_hash_grid"] == 0
+    assert out["min_radius"] == pytest.approx(info["radius_min"], rel=1e-7)
+    assert out["max_radius"] == pytest.approx(info["radius_max"], rel=1e-7)
+    assert out["depth_max"] == info["depth_max"] and out["vertices"] == info["num_vertices"]
+    off, idx = f.neighbors(fr.xyz[:1])
+    assert out["neighbors0"] == len(idx)
+    f.close()
+    ctx.close()

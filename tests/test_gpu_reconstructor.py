@@ -95,3 +95,31 @@ def test_uniform_grid_facade(ctx, tmp_path):
     np.testing.assert_array_equal(vals, f.grid_sample().ravel())
     assert (tmp_path / "grid.vti").stat().st_size > 4 * npts
     f.close()
+
+
+def test_surf_reconstructor_variable_radius(ctx):
+    """IS_CONST_RADIUS = False: Run takes the per-particle radii, the mesh is
+    pi_run's with pi_frame_upload_radii, and getSearcher() describes the
+    radius bins; the radius argument is not used."""
+    fr = synth.two_radius_frame(n=4000, seed=6)
+    mesh = R.Mesh()
+    rec = R.SurfReconstructor(fr.xyz, fr.radii, mesh, 123.0, ctx=ctx)
+    R.IS_CONST_RADIUS = False
+    try:
+        rec.Run(1.9, 2.0)
+    finally:
+        R.IS_CONST_RADIUS = True
+    g = N.Frame(ctx, N.default_params(float(fr.radii.min()))).upload(fr.xyz).upload_radii(fr.radii).run()
+    v, t, k = g.mesh(keys=True)
+    np.testing.assert_array_equal(mesh.vertices, v)
+    np.testing.assert_array_equal(mesh.tris, t + 1)
+    assert rec.getHashGrid() is None
+    s = rec.getSearcher()
+    info = g.info()
+    assert s.getMinRadius() == info["radius_min"] and s.getMaxRadius() == info["radius_max"]
+    assert len(s.getSearchers()) == info["num_grids"] >= 2
+    assert sum(b["count"] for b in s.getSearchers()) == fr.n
+    p = fr.xyz[17]
+    off, idx = g.neighbors(p.reshape(1, 3))
+    assert s.GetNeighbors(p) == idx.tolist()
+    g.close()
