@@ -45,7 +45,18 @@ typedef struct pi_params {
   int32_t qef;         /* 0: leaf value at the cell centre (reference default);
                           1: per-leaf QEF vertex (TNode::NodeCalcNode switched on) */
   int32_t max_depth;   /* 0: no cap; otherwise PI_ERR_LIMIT if D_max exceeds it */
-  int32_t reserved[7];
+  int32_t splash;      /* 0: no splash particle (the reference as it ships);
+                          1: splash particles (GlobalSplash with the marking of
+                          src/evaluator.cpp:675,690 switched on, GEN_SPLASH):
+                          a particle with <= 2 candidates or <= 2 neighbours
+                          within 4r is a splash particle; it keeps the identity
+                          G, takes no part in field sums, normals or node
+                          emptiness, has a zero normal, and is appended to the
+                          mesh as an icosahedron of radius r (12 vertices, 20
+                          triangles, Mesh::AppendSplash_ConstR,
+                          src/global.cpp:65-115) after the surface, in particle
+                          order.  Constant radius only. */
+  int32_t reserved[6];
 } pi_params;
 
 /* Per-frame results of the non-mesh stages (pi_frame_info). */
@@ -82,6 +93,7 @@ typedef struct pi_frame_info {
   int32_t num_grids;        /* hash grids: 1, or the non-empty radius bins (per-particle radii) */
   float radius_min, radius_max; /* the radius, or the searcher's min / max radius
                                    (smallest * 0.99, largest * 1.01) */
+  int64_t num_splash;       /* splash particles (pi_params.splash) */
 } pi_frame_info;
 
 /* Parity dumps (pi_stage_dump).  Arrays are in original particle order unless
@@ -97,6 +109,7 @@ typedef struct pi_frame_info {
 #define PI_DUMP_FP64_FLAGS 9  /* int8[N] 1 where the eigen step ran in FP64 */
 #define PI_DUMP_QEF_SAMPLES 10 /* float[num_nodes*27] GridEval sample values (qef mode) */
 #define PI_DUMP_GRID_OF 11    /* int32[N]  hash grid (radius bin) of each particle */
+#define PI_DUMP_SPLASH 12     /* int8[N]   1 for a splash particle (Evaluator::GlobalSplash) */
 
 typedef struct pi_node {
   uint64_t id;      /* TNode::id */

@@ -507,7 +507,8 @@ static void inv4(const R a[4][4], R out[4][4]) {
 // ---------------------------------------------------------------------------
 // Evaluator, constant radius, anisotropic B-spline
 // (src/evaluator.cpp, globals of src/main.cpp:29-52: USE_ANI=1, USE_POLY6=0,
-// CALC_P_NORMAL=1, no splash particle)
+// CALC_P_NORMAL=1; splash particles only with PIO_SPLASH, which switches on
+// the GlobalSplash marking commented out at :675,690)
 // ---------------------------------------------------------------------------
 template <class R>
 struct Evaluator {
@@ -534,6 +535,10 @@ struct Evaluator {
   std::vector<V3<R>> xMeans, Normals;
   std::vector<M3<R>> Gs;
   std::vector<R> Dets;
+  bool splash_on = false;
+  std::vector<char> GlobalSplash;
+  // src/evaluator.cpp:254-261
+  bool CheckSplash(int j) const { return splash_on && GlobalSplash[j]; }
   std::atomic<long long> nEvals{0}, nPairs{0};
 
   // src/evaluator.cpp:5-58 (constant-radius branch).  Influnce2 and Sigma use
@@ -568,6 +573,7 @@ struct Evaluator {
       }
     }
     Normals.assign(N, V3<R>{{0, 0, 0}});
+    GlobalSplash.assign(N, 0);
     xMeans.resize(N);
     Gs.resize(N);
     Dets.resize(N);
@@ -630,6 +636,7 @@ struct Evaluator {
     neighbors(p, nb);
     V3<R> q{{(R)p[0], (R)p[1], (R)p[2]}};
     for (int j : nb) {
+      if (CheckSplash(j)) continue;
       V3<R> diff{{q[0] - xMeans[j][0], q[1] - xMeans[j][1], q[2] - xMeans[j][2]}};
       scalar += AnisotropicInterpolate(j, diff);
     }
@@ -648,6 +655,7 @@ struct Evaluator {
     neighbors(p, nb);
     V3<R> q{{(R)p[0], (R)p[1], (R)p[2]}};
     for (int j : nb) {
+      if (CheckSplash(j)) continue;
       V3<R> diff{{q[0] - xMeans[j][0], q[1] - xMeans[j][1], q[2] - xMeans[j][2]}};
       scalar += AnisotropicInterpolate(j, diff);
       V3<R> g = AnisotropicInterpolateGrad(j, diff);
@@ -743,6 +751,17 @@ struct Evaluator {
         G(i, j) = sum3<R>(vs(i, 0) * u(j, 0), vs(i, 1) * u(j, 1), vs(i, 2) * u(j, 2)) * scale;
   }
 
+  // the pass-1 branches for <= 2 candidates or neighbours
+  // (src/evaluator.cpp:670-697): identity G; a splash particle with the
+  // marking switched on, whose G pass 2 then leaves alone
+  void splash_mark(int p) {
+    if (!splash_on) return;
+    GlobalSplash[p] = 1;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) Gs[p](i, j) = (i == j) ? R(1) : R(0);
+    Dets[p] = det3<R>(Gs[p]);
+  }
+
   // src/evaluator.cpp:656-749
   void compute_Gs_xMeans() {
 #pragma omp parallel for
@@ -753,13 +772,16 @@ struct Evaluator {
       neighbors((*P)[p].data(), temp);
       if (temp.size() <= 2) {
         xMeans[p] = pos(p);
+        splash_mark(p);
         continue;
       }
       compute_xMeans(p, temp, nn, xMean);
       xMeans[p] = xMean;
+      if (nn <= 2) splash_mark(p);
     }
 #pragma omp parallel for
     for (int p = 0; p < N; p++) {
+      if (CheckSplash(p)) continue;
       std::vector<int> temp;
       M3<R> G;
       neighbors((*P)[p].data(), temp);
@@ -818,7 +840,7 @@ struct Evaluator {
 #pragma omp parallel for
     for (int p = 0; p < N; p++) {
       R s = 0;
-      SingleEvalWithGrad((*P)[p].data(), s, Normals[p]);
+      if (!CheckSplash(p)) SingleEvalWithGrad((*P)[p].data(), s, Normals[p]);
     }
   }
 };
@@ -986,6 +1008,7 @@ struct Frame : FrameBase {
     if (!empty) {
       bool all_splash = true;
       for (const int& in : insides) {
+        if (ev.CheckSplash(in)) continue;
         const float e = (varR ? radii[in] : radius) * ev._SMOOTH_FACTOR;
         const F3& p = P[in];
         if (p[0] > (box1[0] - e) && p[0] < (box2[0] + e) && p[1] > (box1[1] - e) &&
@@ -1450,6 +1473,49 @@ struct Frame : FrameBase {
     }
   }
 
+  // Mesh::BuildIcosaTable (src/global.cpp:65-92), in float
+  static void icosa_table(float T[12][3]) {
+    const float PI = 3.1415926f;
+    const float H_ANGLE = PI / 180 * 72;
+    const float V_ANGLE = std::atan(1.0f / 2);
+    float hAngle1 = -PI / 2 - H_ANGLE / 2, hAngle2 = -PI / 2;
+    T[0][0] = 0, T[0][1] = 0, T[0][2] = 1;
+    for (int i = 1; i <= 5; i++) {
+      const float z = std::sin(V_ANGLE), xy = std::cos(V_ANGLE);
+      T[i][0] = xy * std::cos(hAngle1), T[i][1] = xy * std::sin(hAngle1), T[i][2] = z;
+      T[i + 5][0] = xy * std::cos(hAngle2), T[i + 5][1] = xy * std::sin(hAngle2), T[i + 5][2] = -z;
+      hAngle1 += H_ANGLE;
+      hAngle2 += H_ANGLE;
+    }
+    T[11][0] = 0, T[11][1] = 0, T[11][2] = -1;
+  }
+
+  // GEN_SPLASH (src/surface_reconstructor.cpp:299-320) with
+  // Mesh::AppendSplash_ConstR / AppendSplash_VarR (src/global.cpp:94-138):
+  // 12 vertices and 20 triangles per splash particle, particle order; vertex
+  // keys (12 p + i, ~0)
+  void append_splash() {
+    float T[12][3];
+    icosa_table(T);
+    for (int p = 0; p < ev.N; p++) {
+      if (!ev.CheckSplash(p)) continue;
+      int idx[12];
+      const float rr = varR ? radii[p] : radius;
+      for (int i = 0; i < 12; i++) {
+        const F3& q = P[p];
+        mverts.push_back({q[0] + T[i][0] * rr, q[1] + T[i][1] * rr, q[2] + T[i][2] * rr});
+        mvkeys.push_back({12ull * (unsigned long long)p + (unsigned long long)i, ~0ull});
+        idx[i] = (int)mverts.size();
+      }
+      for (int i = 0; i < 5; i++) {
+        mtris.push_back({idx[0], idx[1 + i], idx[(1 + i) % 5 + 1]});
+        mtris.push_back({idx[1 + i], idx[(1 + i) % 5 + 1], idx[6 + i]});
+        mtris.push_back({idx[(1 + i) % 5 + 1], idx[6 + i], idx[(1 + i) % 5 + 6]});
+        mtris.push_back({idx[6 + i], idx[(1 + i) % 5 + 6], idx[11]});
+      }
+    }
+  }
+
   int stage(int s) override {
     if (s != stage_done + 1) return -2;
     double t0 = now_s();
@@ -1467,6 +1533,7 @@ struct Frame : FrameBase {
           ev.GlobalRadius = &radii;
         }
         ev.init(&grid, &P, radius);
+        ev.splash_on = (flags & PIO_SPLASH) != 0;
         ev._SMOOTH_FACTOR = smooth_factor;
         ev.compute_Gs_xMeans();
         break;
@@ -1493,6 +1560,7 @@ struct Frame : FrameBase {
         nDual = (long long)dual_grids.size();
         calc_vertices();
         generate_mesh();
+        if (ev.splash_on) append_splash();
         break;
       }
       default:
@@ -1670,6 +1738,13 @@ int pio_get_aniso(const pio_frame* h, double* xm, double* g9, double* det) {
         for (int b = 0; b < 3; ++b) g9[9 * i + 3 * a + b] = (double)f.ev.Gs[i](a, b);
       det[i] = (double)f.ev.Dets[i];
     }
+    return 0;
+  });
+}
+int pio_get_splash(const pio_frame* h, int8_t* out) {
+  if (h->f->stage_done < 2) return -1;
+  return withc(h, [&](const auto& f) {
+    for (int i = 0; i < f.ev.N; ++i) out[i] = f.ev.CheckSplash(i) ? 1 : 0;
     return 0;
   });
 }

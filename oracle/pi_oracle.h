@@ -34,9 +34,13 @@ extern "C" {
 #define PIO_QEF 2       /* call NodeCalcNode on leaves (the two commented-out calls
                            at src/surface_reconstructor.cpp:258,270 switched on) */
 #define PIO_FP64 4      /* evaluator arithmetic in double (the FP64 oracle) */
+#define PIO_SPLASH 8    /* splash particles: the GlobalSplash marking of
+                           src/evaluator.cpp:675,690 switched on, GEN_SPLASH on */
 
 typedef struct pio_frame pio_frame;
 
+/* splash flag per particle (after stage 2; zeros without PIO_SPLASH) */
+int pio_get_splash(const pio_frame* h, int8_t* out);
 pio_frame* pio_create(const float* xyz, int64_t n, float radius, float smooth_factor,
                       float iso_factor, int flags);
 /* Variable radius (per-particle radii, the reference's non-constant-radius

@@ -18,6 +18,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libpioracle.so")
 STD_SORT = 1
 QEF = 2
 FP64 = 4
+SPLASH = 8
 
 _lib = None
 
@@ -56,6 +57,7 @@ def lib():
             "pio_in_box": (i64, [P, fp, fp, C.POINTER(C.c_int32), i64]),
             "pio_get_aniso": (C.c_int, [P, dp, dp, dp]),
             "pio_get_normals": (C.c_int, [P, dp]),
+            "pio_get_splash": (C.c_int, [P, C.POINTER(C.c_int8)]),
             "pio_scalars": (C.c_int, [P, dp]),
             "pio_depths": (C.c_int, [P, C.POINTER(C.c_int32), fp, fp]),
             "pio_eval": (C.c_int, [P, fp, i64, dp, dp]),
@@ -222,6 +224,11 @@ class OracleFrame:
         d = np.zeros(self.n)
         lib().pio_get_aniso(self.h, _p(xm, C.c_double), _p(g, C.c_double), _p(d, C.c_double))
         return xm, g, d
+
+    def splash(self):
+        out = np.zeros(self.n, np.int8)
+        assert lib().pio_get_splash(self.h, _p(out, C.c_int8)) == 0
+        return out
 
     def normals(self):
         nr = np.zeros((self.n, 3))

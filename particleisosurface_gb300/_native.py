@@ -19,7 +19,7 @@ PI_OK, PI_ERR_INVALID, PI_ERR_CUDA, PI_ERR_NOMEM, PI_ERR_STATE, PI_ERR_LIMIT = 0
 ERRORS = {-1: "PI_ERR_INVALID", -2: "PI_ERR_CUDA", -3: "PI_ERR_NOMEM", -4: "PI_ERR_STATE", -5: "PI_ERR_LIMIT"}
 
 DUMP_KEYS, DUMP_INDEX_LIST, DUMP_CELL_OFFSETS, DUMP_XMEANS, DUMP_G, DUMP_DET, DUMP_NORMALS, DUMP_NODES, \
-    DUMP_FP64_FLAGS, DUMP_QEF_SAMPLES, DUMP_GRID_OF = range(1, 12)
+    DUMP_FP64_FLAGS, DUMP_QEF_SAMPLES, DUMP_GRID_OF, DUMP_SPLASH = range(1, 13)
 
 
 class PiError(RuntimeError):
@@ -30,7 +30,8 @@ class PiError(RuntimeError):
 
 class Params(C.Structure):
     _fields_ = [("radius", C.c_float), ("smooth_factor", C.c_float), ("iso_factor", C.c_float),
-                ("qef", C.c_int32), ("max_depth", C.c_int32), ("reserved", C.c_int32 * 7)]
+                ("qef", C.c_int32), ("max_depth", C.c_int32), ("splash", C.c_int32),
+                ("reserved", C.c_int32 * 6)]
 
 
 class FrameInfo(C.Structure):
@@ -44,7 +45,7 @@ class FrameInfo(C.Structure):
                 ("candidate_pairs", C.c_int64), ("bisection_evals", C.c_int64), ("fp64_eigen", C.c_int64),
                 ("stage_ms", C.c_float * 8), ("qef_accepted", C.c_int64), ("qef_singular", C.c_int64),
                 ("grid_pairs", C.c_int64), ("field_evals_performed", C.c_int64), ("num_grids", C.c_int32),
-                ("radius_min", C.c_float), ("radius_max", C.c_float)]
+                ("radius_min", C.c_float), ("radius_max", C.c_float), ("num_splash", C.c_int64)]
 
     def as_dict(self):
         out = {}
@@ -142,7 +143,7 @@ def ptr(a, t):
     return a.ctypes.data_as(C.POINTER(t))
 
 
-def default_params(radius, smooth_factor=2.0, iso_factor=1.9, qef=False, max_depth=0):
+def default_params(radius, smooth_factor=2.0, iso_factor=1.9, qef=False, max_depth=0, splash=False):
     p = Params()
     lib().pi_params_default(C.byref(p))
     p.radius = radius
@@ -150,6 +151,7 @@ def default_params(radius, smooth_factor=2.0, iso_factor=1.9, qef=False, max_dep
     p.iso_factor = iso_factor
     p.qef = 1 if qef else 0
     p.max_depth = max_depth
+    p.splash = 1 if splash else 0
     return p
 
 
@@ -449,7 +451,7 @@ class Frame:
             DUMP_G: (np.float32, (-1, 3, 3)), DUMP_DET: (np.float32, (-1,)),
             DUMP_NORMALS: (np.float32, (-1, 3)), DUMP_NODES: (NODE_DTYPE, (-1,)),
             DUMP_FP64_FLAGS: (np.int8, (-1,)), DUMP_QEF_SAMPLES: (np.float32, (-1, 27)),
-            DUMP_GRID_OF: (np.int32, (-1,)),
+            DUMP_GRID_OF: (np.int32, (-1,)), DUMP_SPLASH: (np.int8, (-1,)),
         }[what]
         buf = np.empty(nb.value // np.dtype(dtype).itemsize, dtype)
         check(lib().pi_stage_dump(self.h, what, buf.ctypes.data_as(C.c_void_p), nb.value))

@@ -43,14 +43,20 @@ __device__ __forceinline__ float d2_exact(float dx, float dy, float dz) {
 // the centre is kept as a float pair hi + lo with hi = fl(x) and lo the rest.
 // Coordinates of order 1 against r = 0.01 would otherwise lose ~1e-5 r to the
 // float rounding of x alone.  (c_self + c_mean == 1 exactly in float.)
+//
+// Splash particles (spl not null): a particle with <= 2 candidates or <= 2
+// neighbours within 4r (the GlobalSplash marking of src/evaluator.cpp:675,690
+// switched on) gets spl = 1.
 __global__ void k_xmean(GridView g, const float4* __restrict__ pos, long long n, float nI, float nI2,
-                        float inv_h3, float c_mean, float4* __restrict__ xm, float4* __restrict__ xlo) {
+                        float inv_h3, float c_mean, float4* __restrict__ xm, float4* __restrict__ xlo,
+                        int8_t* __restrict__ spl) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   float4 p = pos[t];
   int cx, cy, cz;
   cell_of(g, p.x, p.y, p.z, cx, cy, cz);
   long long cand = 0;
+  int nn = 0;  // neighbours within 4r (compute_xMeans' neighbors.size())
   Kahan ws, sx, sy, sz;
   for (int dz = -1; dz <= 1; ++dz)
     for (int dy = -1; dy <= 1; ++dy) {
@@ -67,6 +73,7 @@ __global__ void k_xmean(GridView g, const float4* __restrict__ pos, long long n,
           const float dx = __fsub_rn(q.x, p.x), dy2 = __fsub_rn(q.y, p.y), dz2 = __fsub_rn(q.z, p.z);
           m |= (d2_exact(dx, dy2, dz2) < nI2 && j0 + k != t ? 1u : 0u) << k;
         }
+        nn += __popc(m);
         while (m) {
           const int j = j0 + __ffs(m) - 1;
           m &= m - 1u;
@@ -93,6 +100,7 @@ __global__ void k_xmean(GridView g, const float4* __restrict__ pos, long long n,
   }
   xm[t] = hi;
   xlo[t] = lo;
+  if (spl) spl[t] = (cand <= 2 || nn <= 2) ? 1 : 0;
 }
 
 // Cyclic Jacobi on a symmetric 3x3 (a: 00 01 02 11 12 22).  On return
@@ -162,12 +170,24 @@ __global__ void __launch_bounds__(128, 8) k_cov_G(GridView g, const float4* __re
                         float nI, float nI2, float inv_h3, float h2, float inv_h, float sigma,
                         float4* __restrict__ ga, float4* __restrict__ gb, float* __restrict__ gfull,
                         float* __restrict__ det_out, int8_t* __restrict__ f64flag,
-                        unsigned long long* __restrict__ f64count) {
+                        unsigned long long* __restrict__ f64count, const int8_t* __restrict__ spl) {
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   float4 p = pos[t];
   float4 xp = xm0[t];
   const float4 lp = xlo[t];
+  if (spl && spl[t]) {
+    // a splash particle keeps pass 1's identity G (pass 2 skips it,
+    // src/evaluator.cpp:723-726) and takes part in no field sum: its cull
+    // radius is negative, so no support test passes
+    xm[t] = make_float4(xp.x, xp.y, xp.z, -1.0f);
+    ga[t] = make_float4(inv_h, 0.f, 0.f, inv_h);
+    gb[t] = make_float4(0.f, inv_h, sigma, 0.f);
+    for (int k = 0; k < 9; ++k) gfull[9 * t + k] = (k % 4 == 0) ? 1.0f : 0.0f;
+    det_out[t] = 1.0f;
+    f64flag[t] = 0;
+    return;
+  }
   int cx, cy, cz;
   cell_of(g, p.x, p.y, p.z, cx, cy, cz);
   Kahan ws, c00, c01, c02, c11, c12, c22;
@@ -429,10 +449,15 @@ void stage_aniso(pi_frame* f) {
   f->gfull.alloc(f->ctx, s, n * 9);
   f->det.alloc(f->ctx, s, n);
   f->f64flag.alloc(f->ctx, s, n);
+  const bool splash = f->P.splash != 0;
+  if (splash) f->spl.alloc(f->ctx, s, n);
   counters_reset(f);
-  PI_LAUNCH(k_xmean, div_up(n, 128), 128, 0, s, g, f->pos.p, n, nI, nI2, inv_h3, c_mean, f->nrm.p, f->xlo.p);
+  PI_LAUNCH(k_xmean, div_up(n, 128), 128, 0, s, g, f->pos.p, n, nI, nI2, inv_h3, c_mean, f->nrm.p, f->xlo.p,
+            splash ? f->spl.p : nullptr);
   PI_LAUNCH(k_cov_G, div_up(n, 128), 128, 0, s, g, f->pos.p, f->nrm.p, f->xlo.p, f->xm.p, n, nI, nI2, inv_h3, f->influ2,
-            1.0f / h, f->sigma, f->ga.p, f->gb.p, f->gfull.p, f->det.p, f->f64flag.p, f->dcount.p);
+            1.0f / h, f->sigma, f->ga.p, f->gb.p, f->gfull.p, f->det.p, f->f64flag.p, f->dcount.p,
+            splash ? f->spl.p : nullptr);
+  if (splash) stage_splash_list(f);
   counters_snapshot(f, kPinAniso);
 }
 

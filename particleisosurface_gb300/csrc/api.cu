@@ -328,6 +328,7 @@ void check_params(const pi_params* p) {
   if (!(std::isfinite(p->radius) && p->radius > 0)) throw std::invalid_argument("radius must be positive");
   if (!(std::isfinite(p->smooth_factor) && p->smooth_factor > 0))
     throw std::invalid_argument("smooth_factor must be positive");
+  if (p->splash != 0 && p->splash != 1) throw std::invalid_argument("splash must be 0 or 1");
 }
 
 // Back to `stage` (0: nothing uploaded, 1: particles uploaded) with every
@@ -339,6 +340,7 @@ void frame_clear(pi_frame* f, int stage) {
   f->fieldEvals = f->pairs = f->bisectEvals = f->fp64Count = f->nLeaves = f->nEmpty = 0;
   f->doneEvals = 0;
   f->qefAccepted = f->qefSingular = 0;
+  f->nSplash = 0;
   f->ev_pending = f->pin_pending = 0;
   for (int k = 0; k < 8; ++k) f->stage_ms[k] = 0;
 }
@@ -757,6 +759,7 @@ int pi_frame_info_get(const pi_frame* f, pi_frame_info* o) {
   o->num_grids = f->varR ? (int32_t)f->bins.size() : (f->stage >= 2 ? 1 : 0);
   o->radius_min = f->varR ? f->vrMinR : f->P.radius;
   o->radius_max = f->varR ? f->vrMaxR : f->P.radius;
+  o->num_splash = f->nSplash;
   PI_API_END
 }
 
@@ -1023,6 +1026,7 @@ static size_t dump_size(const pi_frame* f, int what) {
     case PI_DUMP_NORMALS: return sizeof(float) * 3 * f->N;
     case PI_DUMP_NODES: return sizeof(pi_node) * f->nNodes;
     case PI_DUMP_FP64_FLAGS: return sizeof(int8_t) * f->N;
+    case PI_DUMP_SPLASH: return sizeof(int8_t) * f->N;
     case PI_DUMP_QEF_SAMPLES: return f->P.qef ? sizeof(float) * 27 * f->nNodes : 0;
   }
   return 0;
@@ -1104,6 +1108,18 @@ int pi_stage_dump(pi_frame* f, int what, void* buf, size_t bytes) {
       std::vector<float> v(3 * N);
       for (long long t = 0; t < N; ++t) v[3 * t] = x[t].x, v[3 * t + 1] = x[t].y, v[3 * t + 2] = x[t].z;
       sorted_to_orig(v, 3, (float*)buf);
+      break;
+    }
+    case PI_DUMP_SPLASH: {
+      need(f, 3);
+      int8_t* o = (int8_t*)buf;
+      if (!f->P.splash) {
+        std::memset(o, 0, N);
+        break;
+      }
+      auto x = d2h(f->spl.p, N, s);
+      std::vector<uint32_t> sidx = d2h(f->sidx.p, N, s);
+      for (long long t = 0; t < N; ++t) o[sidx[t]] = x[t];
       break;
     }
     case PI_DUMP_FP64_FLAGS: {

@@ -714,21 +714,28 @@ void stage_extract(pi_frame* f) {
   PI_LAUNCH(k_first_flag, div_up(nt0 + 1, 256), 256, 0, s, nt0, ttab.p, twhere.p, trank.p);
   exclusive_scan_i32(trank.p, trank.p, nt0 + 1, nullptr, tmp.p, s);
   read_int_start(f, trank.p + nt0);
-  f->mt.alloc(c, s, nt0 * 3 > 0 ? nt0 * 3 : 3);  // room for every generated triangle
+  // room for every generated triangle and the splash icosahedra
+  const long long nsp = f->P.splash ? f->nSplash : 0;
+  const long long tcap = (nt0 + 20 * nsp) * 3;
+  f->mt.alloc(c, s, tcap > 0 ? tcap : 3);
   PI_LAUNCH(k_tri_write, div_up(nt0, 256), 256, 0, s, nt0, trank.p, otri.p, f->mt.p);
+  f->mv.alloc(c, s, (nv + 12 * nsp) * 3 > 0 ? (nv + 12 * nsp) * 3 : 3);
+  f->mk.alloc(c, s, (nv + 12 * nsp) * 2 > 0 ? (nv + 12 * nsp) * 2 : 2);
   const long long nt = read_int_finish(f);
-  f->nT = nt;
-  if (f->host_tris && nt > 0 && nt <= f->host_tcap) {
+  // splash icosahedra after the surface (Mesh::AppendSplash_ConstR runs
+  // after generate_mesh, src/surface_reconstructor.cpp:299-320)
+  if (nsp > 0) splash_mesh(f, nv, nt);
+  f->nT = nt + 20 * nsp;
+  if (f->host_tris && f->nT > 0 && f->nT <= f->host_tcap) {
     PI_CUDA(cudaEventRecord(c->ev_tris_ready, s));
     PI_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ev_tris_ready, 0));
-    PI_CUDA(cudaMemcpyAsync(f->host_tris, f->mt.p, sizeof(int) * 3 * nt, cudaMemcpyDeviceToHost, c->copy_stream));
+    PI_CUDA(cudaMemcpyAsync(f->host_tris, f->mt.p, sizeof(int) * 3 * f->nT, cudaMemcpyDeviceToHost,
+                            c->copy_stream));
     PI_CUDA(cudaEventRecord(c->ev_tris_copied, c->copy_stream));
     f->tris_sent = true;
   }
-  // 7. vertex positions by bisection
-  f->nV = nv;
-  f->mv.alloc(c, s, nv * 3 > 0 ? nv * 3 : 3);
-  f->mk.alloc(c, s, nv * 2 > 0 ? nv * 2 : 2);
+  // 7. vertex positions by bisection (the splash vertices follow them)
+  f->nV = nv + 12 * nsp;
   const GridHost& gh = f->g;
   BisectArgs ba{GridView{gh.bounding[0], gh.bounding[2], gh.bounding[4], gh.cell, gh.nx, gh.ny, gh.nz, f->off.p},
                 PartView{f->pos.p, f->xm.p, f->ga.p, f->gb.p, f->xlo.p}, f->iso, f->P.radius / 2, nullptr};

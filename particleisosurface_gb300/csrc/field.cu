@@ -64,6 +64,10 @@ __global__ void __launch_bounds__(128, 12) k_normals(GridView g, PartView P, lon
   long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   float4 p = P.pos[t];
+  if (p.w != 0.f) {  // a splash particle's normal stays zero
+    nrm[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
   float gx, gy, gz;
   grad_sum(g, P, p.x, p.y, p.z, gx, gy, gz);
   gx *= gscale;

@@ -20,7 +20,10 @@
 // Jacobi, run to convergence in double.
 //
 // Per-particle state (sorted order): x64[3N], g64[9N], det64[N], 104 bytes
-// per particle, allocated on the first call and kept with the frame.
+// per particle, allocated on the first call and kept with the frame.  With
+// splash particles on, the oracle marks them itself (<= 2 candidates or <= 2
+// neighbours within 4r, distances in double) into spl64[N], gives them the
+// identity G and leaves them out of its sums.
 #include <cmath>
 #include <vector>
 
@@ -97,7 +100,7 @@ __device__ void jacobi_eig3_d(double A[3][3], double V[3][3]) {
 }
 
 __global__ void k_f64_xmean(GridView g, const float4* __restrict__ pos, long long n, F64Consts k,
-                            double* __restrict__ x64) {
+                            double* __restrict__ x64, int8_t* __restrict__ spl64) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const float4 pf = pos[t];
@@ -105,6 +108,7 @@ __global__ void k_f64_xmean(GridView g, const float4* __restrict__ pos, long lon
   int cx, cy, cz;
   cell_of(g, pf.x, pf.y, pf.z, cx, cy, cz);
   long long cand = 0;
+  int nn = 0;
   double ws = 0.0, mx = 0.0, my = 0.0, mz = 0.0;
   for (int dz = -1; dz <= 1; ++dz)
     for (int dy = -1; dy <= 1; ++dy) {
@@ -117,6 +121,7 @@ __global__ void k_f64_xmean(GridView g, const float4* __restrict__ pos, long lon
         const double dx = (double)q.x - px, dyy = (double)q.y - py, dzz = (double)q.z - pz;
         const double d2 = dx * dx + dyy * dyy + dzz * dzz;
         if (d2 >= k.nI2) continue;
+        ++nn;
         const double w = wij_d(sqrt(d2), k.nI);
         ws += w;
         mx += (double)q.x * w;
@@ -134,12 +139,19 @@ __global__ void k_f64_xmean(GridView g, const float4* __restrict__ pos, long lon
   x64[3 * t] = ox;
   x64[3 * t + 1] = oy;
   x64[3 * t + 2] = oz;
+  if (spl64) spl64[t] = (cand <= 2 || nn <= 2) ? 1 : 0;
 }
 
 __global__ void k_f64_G(GridView g, const float4* __restrict__ pos, long long n, F64Consts k,
-                        const double* __restrict__ x64, double* __restrict__ g64, double* __restrict__ det64) {
+                        const double* __restrict__ x64, const int8_t* __restrict__ spl64, double* __restrict__ g64,
+                        double* __restrict__ det64) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
+  if (spl64 && spl64[t]) {  // splash: pass 1's identity
+    for (int a = 0; a < 9; ++a) g64[9 * t + a] = (a % 4 == 0) ? 1.0 : 0.0;
+    det64[t] = 1.0;
+    return;
+  }
   const float4 pf = pos[t];
   const double xp[3] = {x64[3 * t], x64[3 * t + 1], x64[3 * t + 2]};
   int cx, cy, cz;
@@ -185,7 +197,8 @@ __global__ void k_f64_G(GridView g, const float4* __restrict__ pos, long long n,
 
 __global__ void k_f64_eval(GridView g, long long m, const float* __restrict__ pts, F64Consts k,
                            const double* __restrict__ x64, const double* __restrict__ g64,
-                           const double* __restrict__ det64, double* __restrict__ val, double* __restrict__ grad) {
+                           const double* __restrict__ det64, const int8_t* __restrict__ spl64,
+                           double* __restrict__ val, double* __restrict__ grad) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   const float qf[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
@@ -197,6 +210,7 @@ __global__ void k_f64_eval(GridView g, long long m, const float* __restrict__ pt
       int s, e;
       if (!nb_row(g, cx, cy + dy, cz + dz, &s, &e)) continue;
       for (int j = s; j < e; ++j) {
+        if (spl64 && spl64[j]) continue;  // CheckSplash (src/evaluator.cpp:73-76)
         const double d[3] = {(double)qf[0] - x64[3 * j], (double)qf[1] - x64[3 * j + 1],
                              (double)qf[2] - x64[3 * j + 2]};
         const double* G = g64 + 9 * j;
@@ -252,10 +266,15 @@ void fp64_state(pi_frame* f) {
   f->x64.alloc(f->ctx, s, 3 * n);
   f->g64.alloc(f->ctx, s, 9 * n);
   f->det64.alloc(f->ctx, s, n);
+  int8_t* spl = nullptr;
+  if (f->P.splash) {
+    f->spl64.alloc(f->ctx, s, n);
+    spl = f->spl64.p;
+  }
   const F64Consts k = f64_consts(f);
   const GridView g = f64_gview(f);
-  PI_LAUNCH(k_f64_xmean, div_up(n, 128), 128, 0, s, g, f->pos.p, n, k, f->x64.p);
-  PI_LAUNCH(k_f64_G, div_up(n, 128), 128, 0, s, g, f->pos.p, n, k, f->x64.p, f->g64.p, f->det64.p);
+  PI_LAUNCH(k_f64_xmean, div_up(n, 128), 128, 0, s, g, f->pos.p, n, k, f->x64.p, spl);
+  PI_LAUNCH(k_f64_G, div_up(n, 128), 128, 0, s, g, f->pos.p, n, k, f->x64.p, spl, f->g64.p, f->det64.p);
   f->f64_ready = true;
 }
 
@@ -281,7 +300,7 @@ void fp64_aniso_get(pi_frame* f, double* h_x3, double* h_g9, double* h_det) {
 void fp64_eval(pi_frame* f, const float* d_pts, long long m, double* d_val, double* d_grad) {
   fp64_state(f);
   PI_LAUNCH(k_f64_eval, div_up(m, 128), 128, 0, f->ctx->stream, f64_gview(f), m, d_pts, f64_consts(f), f->x64.p,
-            f->g64.p, f->det64.p, d_val, d_grad);
+            f->g64.p, f->det64.p, f->P.splash ? f->spl64.p : nullptr, d_val, d_grad);
 }
 
 void fp64_scalars(const pi_frame* f, double out4[4]) {

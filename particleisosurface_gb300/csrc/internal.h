@@ -119,6 +119,12 @@ struct pi_frame {
   pisurf::DBuf<float> gfull;     // N*9, sorted order (dumps)
   pisurf::DBuf<float> det;       // N, sorted order (dumps)
   pisurf::DBuf<int8_t> f64flag;  // N, sorted order
+  // splash particles (pi_params.splash): the flag per particle (sorted
+  // order), the sorted positions of the splash particles listed in particle
+  // order, and their count
+  pisurf::DBuf<int8_t> spl;
+  pisurf::DBuf<int> splList;
+  long long nSplash = 0;
   // variable radius (pi_frame_upload_radii): host and device radii, the grid
   // index of each particle, the bins' grids (host and a device view), the
   // searcher's min / max / average radius and the per-node min radius
@@ -136,6 +142,7 @@ struct pi_frame {
   // FP64 oracle state (fp64.cu), sorted order: centres, G, det; computed on
   // demand and invalid once the hash grid changes
   pisurf::DBuf<double> x64, g64, det64;
+  pisurf::DBuf<int8_t> spl64;   // splash flags decided in double (splash mode)
   bool f64_ready = false;
   pisurf::DBuf<int> tmp;         // scan / sort scratch
   pisurf::DBuf<uint32_t> u32a, u32b, u32c;  // sort ping-pong scratch
@@ -232,6 +239,10 @@ void stage_aniso(pi_frame* f);
 void stage_normals(pi_frame* f);
 void stage_octree(pi_frame* f);
 void stage_extract(pi_frame* f);
+// Splash particles (splash.cu): pos.w = 1 and the list in particle order
+// after the anisotropy pass; the icosahedra at vertex v0 and triangle t0.
+void stage_splash_list(pi_frame* f);
+void splash_mesh(pi_frame* f, long long v0, long long t0);
 // Grid (blocks) of the cooperative coarse-level octree kernel on `device`,
 // 0 where cooperative launches are not available.
 int top_levels_grid(int device, int sm_count);

@@ -88,8 +88,10 @@ __device__ __forceinline__ GrownBox grown_box(const GridView& g, float4 c, float
   return b;
 }
 
+// A particle counts for a node when it lies in the grown box and is not a
+// splash particle (pos.w = 1, checkEmptyAndCalcCurv's CheckSplash test).
 __device__ __forceinline__ bool inside(const GrownBox& b, float4 p) {
-  return p.x > b.lox && p.x < b.hix && p.y > b.loy && p.y < b.hiy && p.z > b.loz && p.z < b.hiz;
+  return p.x > b.lox && p.x < b.hix && p.y > b.loy && p.y < b.hiy && p.z > b.loz && p.z < b.hiz && p.w == 0.f;
 }
 
 // Particle range of cell c (linear index over the block) of a grown box.
@@ -647,7 +649,7 @@ __global__ void __launch_bounds__(32 * kSpawnWarps, CURV ? 16 : 24) k_spawn_scan
         const int mx = ((p.x > clo[0][0] && p.x < chi[0][0]) ? 1 : 0) | ((p.x > clo[0][1] && p.x < chi[0][1]) ? 2 : 0);
         const int my = ((p.y > clo[1][0] && p.y < chi[1][0]) ? 1 : 0) | ((p.y > clo[1][1] && p.y < chi[1][1]) ? 2 : 0);
         const int mz = ((p.z > clo[2][0] && p.z < chi[2][0]) ? 1 : 0) | ((p.z > clo[2][1] && p.z < chi[2][1]) ? 2 : 0);
-        if (mx && my && mz) {
+        if (mx && my && mz && p.w == 0.f) {  // splash particles (pos.w = 1) do not count
           unsigned m8 = 0;
 #pragma unroll
           for (int k = 0; k < 8; ++k)

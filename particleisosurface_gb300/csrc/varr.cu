@@ -120,6 +120,7 @@ void stage_upload_radii(pi_frame* f, const float* radii, long long n) {
   for (long long i = 0; i < n; ++i)
     if (!(std::isfinite(radii[i]) && radii[i] > 0)) throw std::invalid_argument("radii must be positive");
   if (f->P.qef) throw std::invalid_argument("the QEF vertices are not available with per-particle radii");
+  if (f->P.splash) throw std::invalid_argument("splash particles are not available with per-particle radii");
   f->hrad.assign(radii, radii + n);
   // Evaluator ctor, variable radius (src/evaluator.cpp:16-29): Influnce2 and
   // Sigma from 2 r in the reference's float / double mix, and the neighbour

@@ -143,6 +143,38 @@ def small_blob(n=2000, radius=0.025, seed=3, jitter=0.2) -> Frame:
     return Frame(np.concatenate([pts, loose]), radius, s, seed, "small_blob_%d" % n)
 
 
+def spray_frame(n=6000, radius=0.02, seed=21, jitter=0.2) -> Frame:
+    """A jittered lattice slab with spray above it: 3 % of the particles as
+    singletons, pairs and triples (splash particles: <= 2 neighbours within
+    4r) and 7 % as loose Gaussian droplets (sigma = 2r, 4-12 particles),
+    whose edge particles may or may not have three neighbours."""
+    rng = np.random.default_rng(seed)
+    sp = 2.0 * radius
+    n_small = max(3, int(0.03 * n))
+    n_drop = int(0.07 * n)
+    n_slab = n - n_small - n_drop
+
+    def slab(s):
+        return _lattice_box((0.0, 0.0, 0.0), (0.6 * s, 0.1 * s, 0.6 * s), sp)
+
+    pts, s = _scaled_lattice(slab, n_slab, rng)
+    pts = _jitter(pts, jitter * radius, rng)
+    parts = [pts]
+    left = n_small
+    while left > 0:
+        k = int(min(left, rng.integers(1, 4)))
+        ctr = np.array([rng.uniform(0, 0.6 * s), rng.uniform(0.2 * s, 0.6 * s), rng.uniform(0, 0.6 * s)])
+        parts.append(ctr + rng.uniform(-1.5 * radius, 1.5 * radius, size=(k, 3)))
+        left -= k
+    left = n_drop
+    while left > 0:
+        k = int(min(left, rng.integers(4, 13)))
+        ctr = np.array([rng.uniform(0, 0.6 * s), rng.uniform(0.2 * s, 0.6 * s), rng.uniform(0, 0.6 * s)])
+        parts.append(ctr + rng.normal(0.0, 2.0 * radius, size=(k, 3)))
+        left -= k
+    return Frame(np.concatenate(parts), radius, s, seed, "spray_%d" % n)
+
+
 CONFIGS = {
     "slab_sphere": slab_and_sphere,
     "dam_break": dam_break,

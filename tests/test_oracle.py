@@ -272,3 +272,53 @@ def test_variable_radius_bins_and_frame():
     nodes = o.nodes()
     leaves = nodes["type"] == 2
     assert leaves.any()
+
+
+def test_splash_particles_marked_and_appended():
+    """PIO_SPLASH: a particle is a splash particle exactly when it has <= 2
+    candidates or <= 2 neighbours within 4r (src/evaluator.cpp:670-697 with
+    the marking switched on); it keeps the identity G, has a zero normal,
+    takes part in no field sum, and the mesh ends with one icosahedron of
+    radius r per splash particle in particle order (12 vertices, 20
+    triangles, src/global.cpp:94-115)."""
+    fr = synth.spray_frame(n=3000, seed=22)
+    xyz, r = fr.xyz, np.float32(fr.radius)
+    o = O.OracleFrame(xyz, fr.radius, flags=O.SPLASH).run()
+    sp = o.splash().astype(bool)
+    # candidates and neighbours counted here, distances rounded as the
+    # reference rounds them: x^2 + (y^2 + z^2) in float
+    off, idx = o.neighbors(xyz)
+    nI2 = np.float32(r * np.float32(4.0)) ** 2
+    want = np.zeros(fr.n, bool)
+    for i in range(fr.n):
+        c = idx[off[i]:off[i + 1]]
+        d = xyz[c] - xyz[i]
+        d2 = d[:, 0] * d[:, 0] + (d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
+        nn = int(np.count_nonzero((d2 < nI2) & (c != i)))
+        want[i] = len(c) <= 2 or nn <= 2
+    np.testing.assert_array_equal(sp, want)
+    ns = int(sp.sum())
+    assert 20 < ns < fr.n // 5
+    xm, G, det = o.aniso()
+    assert np.all(G[sp] == np.eye(3)) and np.all(det[sp] == 1.0)
+    assert np.all(o.normals()[sp] == 0.0)
+    v, t, k = o.mesh()
+    vs, ts, ks = v[-12 * ns:], t[-20 * ns:], k[-12 * ns:]
+    d = np.linalg.norm(vs.reshape(ns, 12, 3) - xyz[sp][:, None, :], axis=2)
+    assert np.abs(d / r - 1.0).max() < 1e-5
+    pid = np.flatnonzero(sp)
+    np.testing.assert_array_equal(ks[:, 0], (12 * pid[:, None] + np.arange(12)).ravel())
+    assert np.all(ks[:, 1] == np.iinfo(np.uint64).max)
+    first = len(v) - 12 * ns + 1  # 1-based, as Mesh::tris
+    tri0 = ts[:20] - first
+    assert tri0.min() == 0 and tri0.max() == 11
+    # a closed surface: every edge of an icosahedron is in two triangles
+    edges = {}
+    for a, b, c in tri0:
+        for e in ((a, b), (b, c), (c, a)):
+            edges[tuple(sorted(e))] = edges.get(tuple(sorted(e)), 0) + 1
+    assert len(edges) == 30 and set(edges.values()) == {2}
+    # without the flag nothing is marked and no key is a splash key
+    o0 = O.OracleFrame(xyz, fr.radius).run()
+    assert o0.splash().sum() == 0
+    assert not np.any(o0.mesh()[2][:, 1] == np.iinfo(np.uint64).max)
