@@ -62,8 +62,9 @@ FLOPS_PER_PAIR = 38
 QEF_FLOPS_PER_LEAF = 27 * 15 * 2 + 150
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_q_eval launch on the
 # leaf level of the 1M-particle frame with the QEF on, from one ncu capture
-# (None until a capture of the current build exists)
-CHUNK_DRAM_BYTES_PER_LAUNCH = None
+# (profiles/k_q_eval_traffic_dam_break_qef.md): 924,604,672 read +
+# 546,845,952 written
+CHUNK_DRAM_BYTES_PER_LAUNCH = 924_604_672 + 546_845_952
 
 
 def parse():

@@ -110,6 +110,9 @@ typedef struct pi_frame_info {
 #define PI_DUMP_QEF_SAMPLES 10 /* float[num_nodes*27] GridEval sample values (qef mode) */
 #define PI_DUMP_GRID_OF 11    /* int32[N]  hash grid (radius bin) of each particle */
 #define PI_DUMP_SPLASH 12     /* int8[N]   1 for a splash particle (Evaluator::GlobalSplash) */
+#define PI_DUMP_VERTEX_EDGES 13 /* int32[nV*2] the two leaves (indices into PI_DUMP_NODES) whose
+                                   node points bound each mesh vertex's bisection; -1 for
+                                   splash vertices */
 
 typedef struct pi_node {
   uint64_t id;      /* TNode::id */

@@ -19,7 +19,7 @@ PI_OK, PI_ERR_INVALID, PI_ERR_CUDA, PI_ERR_NOMEM, PI_ERR_STATE, PI_ERR_LIMIT = 0
 ERRORS = {-1: "PI_ERR_INVALID", -2: "PI_ERR_CUDA", -3: "PI_ERR_NOMEM", -4: "PI_ERR_STATE", -5: "PI_ERR_LIMIT"}
 
 DUMP_KEYS, DUMP_INDEX_LIST, DUMP_CELL_OFFSETS, DUMP_XMEANS, DUMP_G, DUMP_DET, DUMP_NORMALS, DUMP_NODES, \
-    DUMP_FP64_FLAGS, DUMP_QEF_SAMPLES, DUMP_GRID_OF, DUMP_SPLASH = range(1, 13)
+    DUMP_FP64_FLAGS, DUMP_QEF_SAMPLES, DUMP_GRID_OF, DUMP_SPLASH, DUMP_VERTEX_EDGES = range(1, 14)
 
 
 class PiError(RuntimeError):
@@ -452,6 +452,7 @@ class Frame:
             DUMP_NORMALS: (np.float32, (-1, 3)), DUMP_NODES: (NODE_DTYPE, (-1,)),
             DUMP_FP64_FLAGS: (np.int8, (-1,)), DUMP_QEF_SAMPLES: (np.float32, (-1, 27)),
             DUMP_GRID_OF: (np.int32, (-1,)), DUMP_SPLASH: (np.int8, (-1,)),
+            DUMP_VERTEX_EDGES: (np.int32, (-1, 2)),
         }[what]
         buf = np.empty(nb.value // np.dtype(dtype).itemsize, dtype)
         check(lib().pi_stage_dump(self.h, what, buf.ctypes.data_as(C.c_void_p), nb.value))

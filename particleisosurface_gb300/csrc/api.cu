@@ -1027,6 +1027,7 @@ static size_t dump_size(const pi_frame* f, int what) {
     case PI_DUMP_NODES: return sizeof(pi_node) * f->nNodes;
     case PI_DUMP_FP64_FLAGS: return sizeof(int8_t) * f->N;
     case PI_DUMP_SPLASH: return sizeof(int8_t) * f->N;
+    case PI_DUMP_VERTEX_EDGES: return sizeof(int32_t) * 2 * f->nV;
     case PI_DUMP_QEF_SAMPLES: return f->P.qef ? sizeof(float) * 27 * f->nNodes : 0;
   }
   return 0;
@@ -1108,6 +1109,12 @@ int pi_stage_dump(pi_frame* f, int what, void* buf, size_t bytes) {
       std::vector<float> v(3 * N);
       for (long long t = 0; t < N; ++t) v[3 * t] = x[t].x, v[3 * t + 1] = x[t].y, v[3 * t + 2] = x[t].z;
       sorted_to_orig(v, 3, (float*)buf);
+      break;
+    }
+    case PI_DUMP_VERTEX_EDGES: {
+      need(f, 6);
+      if (f->nV) PI_CUDA(cudaMemcpyAsync(buf, f->vedge.p, sizeof(int2) * f->nV, cudaMemcpyDeviceToHost, s));
+      PI_CUDA(cudaStreamSynchronize(s));
       break;
     }
     case PI_DUMP_SPLASH: {

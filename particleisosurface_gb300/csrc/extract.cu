@@ -476,12 +476,14 @@ __global__ void k_bisect(BisectArgs a, long long nv, const int* __restrict__ ord
                          const int* __restrict__ slotA,
                          const int* __restrict__ slotB, const float4* __restrict__ nd_v,
                          const uint64_t* __restrict__ nd_id, float* __restrict__ out,
-                         uint64_t* __restrict__ vkeys, unsigned long long* __restrict__ counters) {
+                         uint64_t* __restrict__ vkeys, int2* __restrict__ vedge,
+                         unsigned long long* __restrict__ counters) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nv) return;
   const long long v = order[t];
   const int s = rep[v];
   const int A = slotA[s], B = slotB[s];
+  vedge[v] = make_int2(A, B);
   float4 p = nd_v[A], q = nd_v[B];
   const float dx = __fsub_rn(p.x, q.x), dy = __fsub_rn(p.y, q.y), dz = __fsub_rn(p.z, q.z);
   float d = __fsqrt_rn(__fadd_rn(__fmul_rn(dx, dx), __fadd_rn(__fmul_rn(dy, dy), __fmul_rn(dz, dz))));
@@ -721,6 +723,8 @@ void stage_extract(pi_frame* f) {
   PI_LAUNCH(k_tri_write, div_up(nt0, 256), 256, 0, s, nt0, trank.p, otri.p, f->mt.p);
   f->mv.alloc(c, s, (nv + 12 * nsp) * 3 > 0 ? (nv + 12 * nsp) * 3 : 3);
   f->mk.alloc(c, s, (nv + 12 * nsp) * 2 > 0 ? (nv + 12 * nsp) * 2 : 2);
+  f->vedge.alloc(c, s, nv + 12 * nsp > 0 ? nv + 12 * nsp : 1);
+  if (nsp > 0) PI_CUDA(cudaMemsetAsync(f->vedge.p + nv, 0xff, sizeof(int2) * 12 * nsp, s));
   const long long nt = read_int_finish(f);
   // splash icosahedra after the surface (Mesh::AppendSplash_ConstR runs
   // after generate_mesh, src/surface_reconstructor.cpp:299-320)
@@ -767,10 +771,10 @@ void stage_extract(pi_frame* f) {
     prof_begin(c, s, PG_BISECT);
     if (f->varR)
       PI_LAUNCH(k_bisect<true>, div_up(nv, 128), 128, 0, s, ba, nv, vorder.p, rep.p, slotA.p, slotB.p, f->nd_v.p,
-                f->nd_id.p, f->mv.p, f->mk.p, f->dcount.p);
+                f->nd_id.p, f->mv.p, f->mk.p, f->vedge.p, f->dcount.p);
     else
       PI_LAUNCH(k_bisect<false>, div_up(nv, 128), 128, 0, s, ba, nv, vorder.p, rep.p, slotA.p, slotB.p, f->nd_v.p,
-                f->nd_id.p, f->mv.p, f->mk.p, f->dcount.p);
+                f->nd_id.p, f->mv.p, f->mk.p, f->vedge.p, f->dcount.p);
     prof_end(c, s, PG_BISECT);
   }
   counters_snapshot(f, kPinExtract);

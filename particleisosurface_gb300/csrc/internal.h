@@ -171,6 +171,7 @@ struct pi_frame {
   pisurf::DBuf<float> mv;        // nV*3
   pisurf::DBuf<int> mt;          // nT*3
   pisurf::DBuf<uint64_t> mk;     // nV*2
+  pisurf::DBuf<int2> vedge;      // nV: the two leaf nodes whose edge each vertex bisects (-1 for splash)
 
   // counters
   long long fieldEvals = 0, pairs = 0, bisectEvals = 0, fp64Count = 0, nLeaves = 0, nEmpty = 0;

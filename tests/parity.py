@@ -311,12 +311,96 @@ def compare_meshes_fast(o_mesh, g_mesh, radius):
     to = np.unique(_tri_view(io[np.asarray(ot, np.int64) - 1]))
     tg = np.unique(_tri_view(ig[np.asarray(gt, np.int64)]))
     tc = np.intersect1d(to, tg, assume_unique=True)
+    # GPU vertices present in both meshes but off the float oracle's by more
+    # than the tolerance (indices into the GPU mesh), for arbitrate_vertices
+    gd = np.zeros(len(gv))
+    gb = so[ig]
+    gd[gb] = np.abs(po[ig[gb]] - gv[gb]).max(1)
     return dict(verts_oracle=int(so.sum()), verts_gpu=int(sg.sum()), verts_only_oracle=int((so & ~sg).sum()),
                 verts_only_gpu=int((sg & ~so).sum()), tris_oracle=len(to), tris_gpu=len(tg),
                 tris_only_oracle=len(to) - len(tc), tris_only_gpu=len(tg) - len(tc),
                 vert_maxdiff_over_r=float(d.max() / radius),
                 vert_rmsdiff_over_r=float(np.sqrt(np.mean(d.astype(np.float64) ** 2)) / radius),
-                verts_off_tol=int(np.sum(d > VERT_TOL * radius)))
+                verts_off_tol=int(np.sum(d > VERT_TOL * radius)),
+                off_gpu_idx=np.flatnonzero(gd > VERT_TOL * radius))
+
+
+def _fnorm(dx, dy, dz):
+    """|d| rounded as the library's bisection rounds it (float32,
+    x^2 + (y^2 + z^2), then sqrt)."""
+    return np.sqrt(dx * dx + (dy * dy + dz * dz)).astype(np.float32)
+
+
+def bisect_fp64(p, q, rr, eval64, max_scalar):
+    """The edge bisection of calc_vertices (src/visitorextract.cpp:41-93), as
+    the library runs it (float midpoints, halved float length, stop at
+    length <= rr, lerp with the 0.1 / 0.9 snap), with every midpoint value
+    from the FP64 oracle, for many edges at once.  p, q: float32 (n, 4) node
+    points (xyz, value) of the two leaves.  Returns the FP64 vertex (n, 3),
+    and for each edge whether a decision was a near tie: a midpoint value
+    within 2 FIELD_TOL_FP64 * MaxScalar of zero, or a lerp ratio whose
+    distance to a snap threshold is within what that error moves it; and the
+    distance that error moves the lerped vertex."""
+    p = np.asarray(p, np.float32).copy()
+    q = np.asarray(q, np.float32).copy()
+    pw = p[:, 3].astype(np.float64)
+    qw = q[:, 3].astype(np.float64)
+    n = len(p)
+    d = _fnorm(p[:, 0] - q[:, 0], p[:, 1] - q[:, 1], p[:, 2] - q[:, 2])
+    rr = np.float32(rr)
+    tie = np.zeros(n, bool)
+    band = 2 * FIELD_TOL_FP64 * max_scalar
+    for _ in range(64):
+        act = d > rr
+        if not act.any():
+            break
+        m = ((p[act, :3] + q[act, :3]) * np.float32(0.5)).astype(np.float32)
+        mw = eval64(m)
+        tie[np.flatnonzero(act)[np.abs(mw) < band]] = True
+        keep_p = (mw > 0) == (pw[act] > 0)
+        ia = np.flatnonzero(act)
+        tp, tq = ia[keep_p], ia[~keep_p]
+        p[tp, :3], pw[tp] = m[keep_p], mw[keep_p]
+        q[tq, :3], qw[tq] = m[~keep_p], mw[~keep_p]
+        d[act] = (d[act] * np.float32(0.5)).astype(np.float32)
+    den = qw - pw
+    ratio = -pw / den
+    dr = band / np.maximum(np.abs(den), 1e-300)
+    tie |= (np.abs(ratio - 0.1) < dr) | (np.abs(ratio - 0.9) < dr)
+    P, Q = p[:, :3].astype(np.float64), q[:, :3].astype(np.float64)
+    v = P + (Q - P) * ratio[:, None]
+    v[ratio < 0.1] = P[ratio < 0.1]
+    v[ratio > 0.9] = Q[ratio > 0.9]
+    slack = np.linalg.norm(Q - P, axis=1) * dr
+    return v, tie, slack
+
+
+def check_vertices_fp64(g, m, radius, max_scalar, dump_nodes, dump_edges):
+    """arbitrate_vertices for a library frame g (a constant radius: the
+    bisection stops at r / 2) and the report m of compare_meshes_fast; the
+    dump codes are the library's PI_DUMP_NODES and PI_DUMP_VERTEX_EDGES."""
+    gv = g.mesh()[0]
+    rr = np.float32(radius) / np.float32(2)
+    return arbitrate_vertices(g.dump(dump_nodes), g.dump(dump_edges), gv, m["off_gpu_idx"], rr, g.eval_fp64,
+                              max_scalar, radius)
+
+
+def arbitrate_vertices(g_nodes, edges, gv, idx, rr, eval64, max_scalar, radius):
+    """GPU vertices idx that differ from the float oracle's by more than
+    VERT_TOL * r, against the FP64 bisection of the same edge (bisect_fp64):
+    each must lie within VERT_TOL * r (plus what the FP64 tolerance moves the
+    lerp) of the FP64 vertex, or have a near-tie decision on its FP64 chain.
+    Returns (agree, explained, unexplained indices)."""
+    idx = np.asarray(idx, np.int64)
+    if len(idx) == 0:
+        return 0, 0, idx
+    nv = g_nodes["node"]
+    e = edges[idx]
+    p, q = nv[e[:, 0]], nv[e[:, 1]]
+    v64, tie, slack = bisect_fp64(p, q, rr, eval64, max_scalar)
+    dist = np.abs(gv[idx].astype(np.float64) - v64).max(1)
+    ok = dist <= VERT_TOL * radius + slack
+    return int(ok.sum()), int((~ok & tie).sum()), idx[~ok & ~tie]
 
 
 def qef_solve_f64_batch(centers, halves, samples):

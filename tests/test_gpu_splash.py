@@ -135,11 +135,13 @@ def test_splash_octree_and_mesh(ctx, name):
     _check_icosahedra(o, g)
     # the surface as in the constant-radius tests
     m = PR.compare_meshes_fast(o.mesh(), g.mesh(keys=True), fr.radius)
-    print(name, m)
+    print(name, {k: v for k, v in m.items() if k != "off_gpu_idx"})
     n_v = m["verts_oracle"]
     assert m["verts_only_oracle"] + m["verts_only_gpu"] <= max(4, n_v // 2000)
     assert m["tris_only_oracle"] + m["tris_only_gpu"] <= max(8, m["tris_oracle"] // 1000)
-    assert m["verts_off_tol"] <= max(4, n_v // 2000)
+    agree, expl, bad = PR.check_vertices_fp64(g, m, fr.radius, ms, N.DUMP_NODES, N.DUMP_VERTEX_EDGES)
+    assert len(bad) == 0, bad[:10]
+    assert expl <= max(4, n_v // 2000)
 
 
 def test_splash_with_qef(ctx):

@@ -142,7 +142,7 @@ def test_varr_octree_and_mesh(ctx, name):
     if rep["explained"] == 0:
         assert info["field_evals"] - info["bisection_evals"] == o.frame_counts[0] - o.frame_counts[1]
     m = PR.compare_meshes_fast(o.mesh(), g.mesh(keys=True), float(fr.radii.min()))
-    print(name, m)
+    print(name, {k: v for k, v in m.items() if k != "off_gpu_idx"})
     n_v = m["verts_oracle"]
     assert n_v > 0
     assert m["verts_only_oracle"] + m["verts_only_gpu"] <= max(4, n_v // 2000)
@@ -166,7 +166,7 @@ def test_varr_equal_radii_equal_constant_radius_field(ctx):
         np.testing.assert_array_equal(gv.dump(what), gc.dump(what))
     pts = fr.xyz[::5] + np.float32(0.3 * fr.radius)
     iv, ic = gv.info()["iso_value"], gc.info()["iso_value"]
-    assert iv > ic
+    assert iv < ic  # the kernel decreases: B(0.25) < B(0.01)
     ev, ec = gv.eval(pts).astype(np.float64), gc.eval(pts).astype(np.float64)
     # each value is iso - sum rounded to float: the sums agree to that rounding
     assert np.all(np.abs((iv - ev) - (ic - ec)) <= 2 * np.spacing(np.abs(ev).astype(np.float32)).astype(np.float64)
