@@ -281,6 +281,27 @@ int pi_grid_write_vti(pi_frame* f, const char* path);
  * "uchar"-counted "int" list per face with 0-based indices (tris given
  * 0-based, or 1-based when one_based is set). */
 int pi_load_csv(const char* path, float* xyz, float* radius, int64_t cap, int64_t* n, int32_t* cols4);
+/* pi_load_hdf5: readShonDyParticleData (src/main.cpp:281-327): the dataset
+ * "position" (3N values, flat as the reference reads it, or N x 3) and, when
+ * radius is not null, "particleRadius" (N values), converted to float; call
+ * with xyz = null to count (*n).  The HDF5 library is not needed: the file
+ * format is read by the library (superblock versions 0-3, version 1 and 2
+ * object headers, symbol-table and compact groups, compact / contiguous /
+ * chunked layouts with the deflate, shuffle and Fletcher-32 filters, integer
+ * and IEEE float elements of either byte order).  PI_ERR_INVALID for a
+ * missing file or dataset or an unsupported structure (named in the
+ * message); PI_ERR_LIMIT when cap < N (with *n set).
+ * pi_hdf5_dataset: any dataset of such a file as double (count, dims, rank).
+ * pi_load_xdmf: readShonDyParticleXDMF (src/hdf5Utils.cpp:7-47): the frame
+ * files of <dir>/<xdmf_file> (the text of each Xdmf/Domain/Grid/Grid/
+ * Geometry/DataItem up to its first ':'), all of them, or only frame
+ * target_frame (1-based) when it is in range; written to out separated by
+ * '\n' and NUL-terminated, *len the bytes that takes, *frames the count. */
+int pi_load_hdf5(const char* path, float* xyz, float* radius, int64_t cap, int64_t* n);
+int pi_hdf5_dataset(const char* path, const char* name, double* out, int64_t cap, int64_t* count,
+                    int64_t* dims8, int32_t* rank);
+int pi_load_xdmf(const char* dir, const char* xdmf_file, int32_t target_frame, char* out, int64_t cap,
+                 int64_t* len, int32_t* frames);
 int pi_write_ply(const char* path, const float* verts, int64_t nv, const int32_t* tris, int64_t nt,
                  int32_t one_based);
 int pi_mesh_write_ply(pi_frame* f, const char* path);

@@ -24,6 +24,8 @@
 //   Mesh, Vertex, Triangle  include/global.h:13-60, 86-115
 //   writeObjFile        src/main.cpp:54-67
 //   writePlyFile, loadParticlesFromCSV  src/main.cpp:69-114, 215-275
+//   readShonDyParticleData  src/main.cpp:281-327 (HDF5, read by the library)
+//   readShonDyParticleXDMF  src/hdf5Utils.cpp:7-47
 //   UniformGrid         include/marching.h:18-70 (dense-grid mode)
 //   MultiLevelSearcher  include/multi_level_researcher.h:8-40 (per-particle radii)
 //   IS_CONST_RADIUS     include/iso_common.h:6, defined by the host program
@@ -35,6 +37,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -215,6 +218,42 @@ inline bool const_radius_mode() {
 #endif
 }
 }  // namespace detail
+
+// readShonDyParticleData (src/main.cpp:281-327): "position" and, unless the
+// radius is constant, "particleRadius" of an HDF5 particle file.  The
+// library reads the HDF5 format itself; errors throw.
+inline bool readShonDyParticleData(const std::string& fileName, std::vector<Vector3f>& positions,
+                                   std::vector<float>& radiuses,
+                                   bool is_const_radius = detail::const_radius_mode()) {
+  int64_t n = 0;
+  check(pi_load_hdf5(fileName.c_str(), nullptr, nullptr, 0, &n));
+  std::vector<float> xyz((size_t)n * 3);
+  std::vector<float> rad(is_const_radius ? 0 : (size_t)n);
+  check(pi_load_hdf5(fileName.c_str(), xyz.data(), is_const_radius ? nullptr : rad.data(), n, &n));
+  positions.resize((size_t)n);
+  for (int64_t i = 0; i < n; ++i) positions[i] = Vector3f(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+  if (!is_const_radius) radiuses = rad;
+  return true;
+}
+
+// readShonDyParticleXDMF (src/hdf5Utils.cpp:7-47): the frame files listed by
+// <dir_path>/<xdmf_file>, all or only frame target_frame (1-based).
+inline bool readShonDyParticleXDMF(const std::string& dir_path, const std::string& xdmf_file,
+                                   std::vector<std::string>& files, const int target_frame) {
+  int64_t len = 0;
+  int32_t frames = 0;
+  check(pi_load_xdmf(dir_path.c_str(), xdmf_file.c_str(), target_frame, nullptr, 0, &len, &frames));
+  std::string buf((size_t)len, '\0');
+  check(pi_load_xdmf(dir_path.c_str(), xdmf_file.c_str(), target_frame, &buf[0], len, &len, &frames));
+  size_t s = 0;
+  for (int32_t k = 0; k < frames; ++k) {
+    size_t e = buf.find('\n', s);
+    if (e == std::string::npos) e = std::strlen(buf.c_str());
+    files.push_back(buf.substr(s, e - s));
+    s = e + 1;
+  }
+  return true;
+}
 
 // MultiLevelSearcher (src/multi_level_reseacher.cpp): the radius bins of a
 // frame with per-particle radii, one hash grid per non-empty bin, built by
@@ -630,6 +669,8 @@ using pisurf::TNode;
 using pisurf::Triangle;
 using pisurf::Vertex;
 using pisurf::loadParticlesFromCSV;
+using pisurf::readShonDyParticleData;
+using pisurf::readShonDyParticleXDMF;
 using pisurf::writeObjFile;
 using pisurf::writePlyFile;
 #endif

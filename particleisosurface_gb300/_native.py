@@ -105,6 +105,11 @@ def _declare(L):
         "pi_fp64_scalars": (C.c_int, [P, C.POINTER(C.c_double)]),
         "pi_grid_dims": (C.c_int, [P, C.POINTER(C.c_int32), fp, pi64]),
         "pi_load_csv": (C.c_int, [C.c_char_p, fp, fp, i64, pi64, C.POINTER(C.c_int32)]),
+        "pi_load_hdf5": (C.c_int, [C.c_char_p, fp, fp, i64, pi64]),
+        "pi_hdf5_dataset": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(C.c_double), i64, pi64, pi64,
+                                      C.POINTER(C.c_int32)]),
+        "pi_load_xdmf": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int32, C.c_char_p, i64, pi64,
+                                   C.POINTER(C.c_int32)]),
         "pi_write_ply": (C.c_int, [C.c_char_p, fp, i64, C.POINTER(C.c_int32), i64, C.c_int32]),
         "pi_mesh_write_ply": (C.c_int, [P, C.c_char_p]),
         "pi_grid_sample": (C.c_int, [P, fp, i64]),
@@ -174,6 +179,43 @@ def load_csv(path, radius=False):
     check(lib().pi_load_csv(str(path).encode(), ptr(xyz, C.c_float), ptr(rad, C.c_float) if radius else None,
                             n.value, C.byref(n), ptr(cols, C.c_int32)))
     return xyz, rad, cols
+
+
+def load_hdf5(path, radius=False):
+    """readShonDyParticleData: (xyz float32 [n, 3], radius float32 [n] or None)."""
+    n = C.c_int64()
+    check(lib().pi_load_hdf5(str(path).encode(), None, None, 0, C.byref(n)))
+    xyz = np.empty((n.value, 3), np.float32)
+    rad = np.empty(n.value, np.float32) if radius else None
+    check(lib().pi_load_hdf5(str(path).encode(), ptr(xyz, C.c_float), ptr(rad, C.c_float) if radius else None,
+                             n.value, C.byref(n)))
+    return xyz, rad
+
+
+def hdf5_dataset(path, name):
+    """One dataset of an HDF5 file as float64, shaped by its dataspace."""
+    cnt = C.c_int64()
+    dims = np.zeros(8, np.int64)
+    rank = C.c_int32()
+    check(lib().pi_hdf5_dataset(str(path).encode(), name.encode(), None, 0, C.byref(cnt), ptr(dims, C.c_int64),
+                                C.byref(rank)))
+    out = np.empty(cnt.value, np.float64)
+    check(lib().pi_hdf5_dataset(str(path).encode(), name.encode(), ptr(out, C.c_double), cnt.value, C.byref(cnt),
+                                None, None))
+    return out.reshape(tuple(int(d) for d in dims[:rank.value]))
+
+
+def load_xdmf(directory, xdmf_file, target_frame=0):
+    """readShonDyParticleXDMF: the frame file names of an XDMF frame list."""
+    ln = C.c_int64()
+    nf = C.c_int32()
+    check(lib().pi_load_xdmf(str(directory).encode(), str(xdmf_file).encode(), target_frame, None, 0, C.byref(ln),
+                             C.byref(nf)))
+    buf = C.create_string_buffer(ln.value)
+    check(lib().pi_load_xdmf(str(directory).encode(), str(xdmf_file).encode(), target_frame, buf, ln.value,
+                             C.byref(ln), C.byref(nf)))
+    s = buf.value.decode()
+    return s.split("\n") if nf.value else []
 
 
 def write_ply(path, verts, tris, one_based=False):

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libpisurf.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["sort.cu", "grid.cu", "aniso.cu", "field.cu", "octree.cu", "extract.cu", "api.cu", "noalloc.cu", "qef.cu", "server.cu", "sample.cu", "io.cu", "fp64.cu", "varr.cu", "splash.cu"]
+SOURCES = ["sort.cu", "grid.cu", "aniso.cu", "field.cu", "octree.cu", "extract.cu", "api.cu", "noalloc.cu", "qef.cu", "server.cu", "sample.cu", "io.cu", "fp64.cu", "varr.cu", "splash.cu", "h5.cu"]
 
 
 def nvcc():

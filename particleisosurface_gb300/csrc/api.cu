@@ -965,6 +965,54 @@ int pi_load_csv(const char* path, float* xyz, float* radius, int64_t cap, int64_
   PI_API_END
 }
 
+int pi_load_hdf5(const char* path, float* xyz, float* radius, int64_t cap, int64_t* n) {
+  PI_API_BEGIN
+  PI_CHECK(path && n, "bad arguments");
+  long long rows = 0;
+  *n = 0;
+  try {
+    load_hdf5(path, xyz, radius, xyz ? cap : 0, radius != nullptr, &rows);
+  } catch (...) {
+    *n = rows;
+    throw;
+  }
+  *n = rows;
+  PI_API_END
+}
+
+int pi_hdf5_dataset(const char* path, const char* name, double* out, int64_t cap, int64_t* count,
+                    int64_t* dims8, int32_t* rank) {
+  PI_API_BEGIN
+  PI_CHECK(path && name && count, "bad arguments");
+  std::vector<uint64_t> dims;
+  const std::vector<double> v = load_hdf5_dataset(path, name, &dims);
+  *count = (int64_t)v.size();
+  if (rank) *rank = (int32_t)dims.size();
+  if (dims8)
+    for (size_t i = 0; i < dims.size() && i < 8; ++i) dims8[i] = (int64_t)dims[i];
+  if (out) {
+    if ((int64_t)v.size() > cap) throw std::length_error("buffer holds fewer values than the dataset");
+    std::memcpy(out, v.data(), sizeof(double) * v.size());
+  }
+  PI_API_END
+}
+
+int pi_load_xdmf(const char* dir, const char* xdmf_file, int32_t target_frame, char* out, int64_t cap,
+                 int64_t* len, int32_t* frames) {
+  PI_API_BEGIN
+  PI_CHECK(dir && xdmf_file && len, "bad arguments");
+  const std::vector<std::string> v = load_xdmf(dir, xdmf_file, target_frame);
+  std::string s;
+  for (size_t i = 0; i < v.size(); ++i) s += (i ? "\n" : "") + v[i];
+  *len = (int64_t)s.size() + 1;
+  if (frames) *frames = (int32_t)v.size();
+  if (out) {
+    if (*len > cap) throw std::length_error("buffer too small for the frame list");
+    std::memcpy(out, s.c_str(), s.size() + 1);
+  }
+  PI_API_END
+}
+
 int pi_write_ply(const char* path, const float* verts, int64_t nv, const int32_t* tris, int64_t nt,
                  int32_t one_based) {
   PI_API_BEGIN

@@ -257,6 +257,13 @@ long long grid_sample(pi_frame* f, float* d_out, long long cap);
 // Host formats: CSV particles (returns the row count; fills xyz / radius up
 // to cap rows; cols = x, y, z, radius column indices) and binary PLY meshes.
 long long load_csv(const char* path, float* xyz, float* radius, long long cap, int cols[4]);
+// HDF5 particle files and XDMF frame lists (h5.cu): positions (and radii)
+// as float, *n_out set before a short buffer is reported; one dataset as
+// double; the frame files of an XDMF list.
+long long load_hdf5(const char* path, float* xyz, float* radius, long long cap, bool want_radius,
+                    long long* n_out);
+std::vector<double> load_hdf5_dataset(const char* path, const char* name, std::vector<uint64_t>* dims);
+std::vector<std::string> load_xdmf(const char* dir, const char* file, int target_frame);
 void write_ply(const char* path, const float* verts, long long nv, const int32_t* tris, long long nt,
                int one_based);
 void eval_points(pi_frame* f, const float* d_pts, long long m, float* d_val, float* d_grad);

@@ -70,6 +70,22 @@ def writePlyFile(mesh: Mesh, fn: str):
     N.write_ply(fn, mesh.vertices, mesh.tris, one_based=True)
 
 
+def readShonDyParticleData(file_name, is_const_radius=None):
+    """readShonDyParticleData (src/main.cpp:281-327): "position" and, unless
+    the radius is constant (IS_CONST_RADIUS by default), "particleRadius" of
+    an HDF5 particle file, as float32 (positions [n, 3], radiuses [n] or
+    empty).  The library reads the HDF5 format itself."""
+    const = IS_CONST_RADIUS if is_const_radius is None else is_const_radius
+    xyz, rad = N.load_hdf5(file_name, radius=not const)
+    return xyz, (rad if rad is not None else np.zeros(0, np.float32))
+
+
+def readShonDyParticleXDMF(dir_path, xdmf_file, target_frame=0):
+    """readShonDyParticleXDMF (src/hdf5Utils.cpp:7-47): the frame files of
+    an XDMF frame list, all or only frame target_frame (1-based)."""
+    return N.load_xdmf(dir_path, xdmf_file, target_frame)
+
+
 def loadParticlesFromCSV(csv_path, is_const_radius=True):
     """loadParticlesFromCSV (src/main.cpp:215-275): (particles [n, 3] float32,
     radiuses [n] float32, empty when is_const_radius)."""

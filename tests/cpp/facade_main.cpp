@@ -1,6 +1,6 @@
 // Host program written against the reference's C++ API (the calls of
 // runOurs, src/main.cpp:330-405), compiled against include/pisurf.hpp.
-//   facade_main <xyz float32 file | particles .csv> <n> <radius> <out.obj> [radii float32 file]
+//   facade_main <xyz float32 file | particles .csv | particles .h5> <n> <radius> <out.obj> [radii float32 file]
 // (also writes <out.obj>.ply, and <out.obj's directory>/grid.vti through
 // UniformGrid).  With a radii file the program runs as the reference does
 // with IS_CONST_RADIUS false: per-particle radii and MultiLevelSearcher.
@@ -53,6 +53,13 @@ int main(int argc, char** argv) {
   if (src.size() > 4 && src.substr(src.size() - 4) == ".csv") {
     try {
       loadParticlesFromCSV(src, particles, radiuses, true);
+    } catch (const pisurf::Error& e) {
+      std::printf("{\"error\": %d, \"message\": \"%s\"}\n", e.code(), e.what());
+      return 1;
+    }
+  } else if (src.size() > 3 && src.substr(src.size() - 3) == ".h5") {
+    try {
+      readShonDyParticleData(src, particles, radiuses);
     } catch (const pisurf::Error& e) {
       std::printf("{\"error\": %d, \"message\": \"%s\"}\n", e.code(), e.what());
       return 1;

@@ -91,3 +91,23 @@ def test_facade_variable_radius_equals_library(tmp_path):
     assert out["neighbors0"] == len(idx)
     f.close()
     ctx.close()
+
+
+def test_facade_hdf5_input_equals_array_input(tmp_path):
+    """readShonDyParticleData through the facade: an HDF5 particle file
+    (flat "position" of doubles) gives the mesh of the same particles
+    passed as floats."""
+    import h5write as W
+    exe = facade.build()
+    fr = synth.small_blob(n=2500, seed=11)
+    W.write_particles(tmp_path / "p.h5", fr.xyz64, layout="v0", storage="chunked", chunk=1000,
+                      filters=("shuffle", "deflate"))
+    r = subprocess.run([exe, str(tmp_path / "p.h5"), "0", repr(fr.radius), str(tmp_path / "h5.obj")],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    ctx = N.Context(0)
+    f = N.Frame(ctx, N.default_params(fr.radius)).upload(fr.xyz).run()
+    f.write_obj(str(tmp_path / "lib.obj"))
+    f.close()
+    ctx.close()
+    assert (tmp_path / "h5.obj").read_bytes() == (tmp_path / "lib.obj").read_bytes()
