@@ -48,6 +48,19 @@ struct CudaError : std::runtime_error {
 
 inline unsigned int div_up(long long a, long long b) { return (unsigned int)((a + b - 1) / b); }
 
+// The reference compares floats with double literals (the float promoted to
+// double): `cellsize - r < 1e-8`, `curv < 0.99` (src/surface_reconstructor.cpp:
+// 247,262) and the 0.1 / 0.9 snap of the bisection (src/visitorextract.cpp:
+// 71-80).  None of these literals is a float, so for a float x each
+// comparison equals one float comparison with the float next to the literal:
+// (double)x < d  <=>  x < (smallest float above d), and
+// (double)x > d  <=>  x > (largest float below d).
+// This keeps the decisions off the FP64 pipe, which is narrow on this GPU.
+constexpr float kAbove1em8 = 0x1.5798fp-27f;  // smallest float above 1e-8
+constexpr float kAbove099 = 0x1.fae148p-1f;   // smallest float above 0.99
+constexpr float kAbove01 = 0x1.99999ap-4f;    // smallest float above 0.1
+constexpr float kBelow09 = 0x1.ccccccp-1f;    // largest float below 0.9
+
 // Striped device event counters (see stripe_add in device.cuh): kCounters
 // counters x 64 stripes, 32 bytes apart.
 constexpr int kStripes = 64;

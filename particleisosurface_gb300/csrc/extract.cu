@@ -504,9 +504,9 @@ __global__ void k_bisect(BisectArgs a, long long nv, const int* __restrict__ ord
   }
   const float ratio = __fdiv_rn(__fsub_rn(0.0f, p.w), __fsub_rn(q.w, p.w));
   float3 r;
-  if ((double)ratio < 0.1) {
+  if (ratio < kAbove01) {  // (double)ratio < 0.1
     r = make_float3(p.x, p.y, p.z);
-  } else if ((double)ratio > 0.9) {
+  } else if (ratio > kBelow09) {  // (double)ratio > 0.9
     r = make_float3(q.x, q.y, q.z);
   } else {
     r.x = __fadd_rn(p.x, __fmul_rn(__fsub_rn(q.x, p.x), ratio));

@@ -194,17 +194,17 @@ __global__ void k_q_count(QArgs a, const float4* __restrict__ nd_c, const float4
   if (valid) {
     float qx, qy, qz;
     sample_point(nd_c[node], nd_v[node], (int)(i % kQ), qx, qy, qz);
-    int cx, cy, cz;
-    cell_of(a.g, qx, qy, qz, cx, cy, cz);
+    // the cell (CalcXYZIdx) and, from the same quotients, the octant
+    float fx, fy, fz;
+    const int cx = cell_coord_q(qx, a.g.b0, a.g.cell, a.g.nx, fx);
+    const int cy = cell_coord_q(qy, a.g.b2, a.g.cell, a.g.ny, fy);
+    const int cz = cell_coord_q(qz, a.g.b4, a.g.cell, a.g.nz, fz);
     k = ext_key(a, cx, cy, cz);
-    if (a.octants) {
-      const float fx = __fdiv_rn(__fsub_rn(qx, a.g.b0), a.g.cell) - (float)cx;
-      const float fy = __fdiv_rn(__fsub_rn(qy, a.g.b2), a.g.cell) - (float)cy;
-      const float fz = __fdiv_rn(__fsub_rn(qz, a.g.b4), a.g.cell) - (float)cz;
-      k = k * 8 + ((fx >= 0.5f ? 1 : 0) | (fy >= 0.5f ? 2 : 0) | (fz >= 0.5f ? 4 : 0));
-    }
+    if (a.octants)
+      k = k * 8 + ((fx - (float)cx >= 0.5f ? 1 : 0) | (fy - (float)cy >= 0.5f ? 2 : 0) |
+                   (fz - (float)cz >= 0.5f ? 4 : 0));
   }
-  const unsigned peers = __match_any_sync(0xffffffffu, k);
+  const unsigned peers = run_peers(k);
   const int leader = __ffs(peers) - 1;
   if (valid && lane == leader) atomicAdd(qcnt + k, __popc(peers));
   if (in_level) qkey[i] = k;
@@ -244,9 +244,27 @@ __global__ void k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c
     nc = nd_c[node];
     nv = nd_v[node];
   }
-  if (k >= 0) {
+  const int si = (int)(i % kQ);
+  if (k >= 0 && (si == 13 || si == 27)) {
+    // the centre sample and the node position lie on no other node's
+    // lattice of this level (lattice points of a node are its centre +- 0 or
+    // h per axis, and centres are 2h apart): the centre sample represents
+    // itself, the node position is the centre sample's point when the two
+    // are bit-identical and else its own
+    int r = (int)i;
+    if (si == 27) {
+      float ax, ay, az, bx, by, bz;
+      sample_point(nc, nv, 27, ax, ay, az);
+      sample_point(nc, nv, 13, bx, by, bz);
+      if (__float_as_uint(ax) == __float_as_uint(bx) && __float_as_uint(ay) == __float_as_uint(by) &&
+          __float_as_uint(az) == __float_as_uint(bz))
+        r = (int)(i - 14);
+    }
+    rep[i] = r;
+    uniq = r == (int)i;
+  } else if (k >= 0) {
     float qx, qy, qz;
-    sample_point(nc, nv, (int)(i % kQ), qx, qy, qz);
+    sample_point(nc, nv, si, qx, qy, qz);
     const long long base = 2LL * qoff[k];
     const uint32_t m = 2u * (uint32_t)(qoff[k + 1] - qoff[k]);
     uint32_t pos = __umulhi(hash3(qx, qy, qz), m);
@@ -271,9 +289,10 @@ __global__ void k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c
     rep[i] = r;
     uniq = r == (int)i;
   }
-  // places for the representatives, one atomic per bucket and warp
+  // places for the representatives, one atomic per run of a bucket's
+  // samples in the warp
   const unsigned um = __ballot_sync(0xffffffffu, uniq);
-  const unsigned peers = __match_any_sync(0xffffffffu, uniq ? k : -1) & um;
+  const unsigned peers = run_peers(k) & um;
   if (uniq) {
     const int leader = __ffs(peers) - 1;
     int b0 = 0;
@@ -472,12 +491,12 @@ __global__ void __launch_bounds__(64, 24) k_classify(LevelArgs a, const float* _
   // leaf by size: the node is no larger than the radius (variable radius:
   // the smallest radius of the particles reaching it, src/surface_
   // reconstructor.cpp:156,203-208,247)
-  const bool leaf_by_size = (double)(cellsize - (nd_minr ? nd_minr[node] : a.radius)) < 1e-8;
+  const bool leaf_by_size = cellsize - (nd_minr ? nd_minr[node] : a.radius) < kAbove1em8;
   int8_t type = T_LEAF;
   float curv = -1.0f;
   if (!leaf_by_size && signchange && curv_known) {
     curv = nd_curv[node];  // summed by the parent's scan (k_spawn_scan)
-    if ((double)curv < 0.99) type = T_INTERNAL;
+    if (curv < kAbove099) type = T_INTERNAL;
   } else if (!leaf_by_size && signchange) {
     // checkEmptyAndCalcCurv sums over particles inside the grown box
     const GrownBox b = grown_box(a.g, c, a.expand);
@@ -500,7 +519,7 @@ __global__ void __launch_bounds__(64, 24) k_classify(LevelArgs a, const float* _
     const float nx = warp_sum(sx.s - sx.c), ny = warp_sum(sy.s - sy.c), nz = warp_sum(sz.s - sz.c);
     const float area = warp_sum(ar.s - ar.c);
     curv = (area == 0.f) ? 1.0f : sqrtf(nx * nx + ny * ny + nz * nz) / area;
-    if ((double)curv < 0.99) type = T_INTERNAL;
+    if (curv < kAbove099) type = T_INTERNAL;
   }
   if (lane == 0) {
     nd_type[node] = type;
@@ -1052,7 +1071,7 @@ __global__ void __launch_bounds__(64) k_vr_empty(const MultiGridView* __restrict
       // above D_min a node is INTERNAL unless it is a leaf by size already
       // (every particle reaching it is at least its size; afterSampleEval
       // tests the size first, :247): then it waits for its value
-      const bool leaf_by_size = (double)(2.0f * h - minr) < 1e-8;
+      const bool leaf_by_size = 2.0f * h - minr < kAbove1em8;
       nd_type[node] = (a.big && !leaf_by_size) ? T_INTERNAL : T_UNCERTAIN;
       nd_curv[node] = (area == 0.f) ? 1.0f : sqrtf(nx * nx + ny * ny + nz * nz) / area;
       nd_minr[node] = minr;

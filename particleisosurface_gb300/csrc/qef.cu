@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, const int* __res
     stripe_add(counters, C_QEF_ACCEPTED, 1ull);
   }
   // leaf by size keeps the zeroing (no SingleEval follows it)
-  const bool leaf_by_size = (double)(cellsize - a.radius) < 1e-8;
+  const bool leaf_by_size = cellsize - a.radius < kAbove1em8;
   if (leaf_by_size && err / cellsize < 0.0001f) v.w = 0.0f;
   nd_v[node] = v;
   if (qef_err) qef_err[node] = err;
