@@ -572,7 +572,10 @@ def ours(a):
                        "l2": "512 MiB buffer written between steps", "depth_max": qinfo["depth_max"],
                        "nodes": qinfo["num_nodes"], "vertices": qinfo["num_vertices"],
                        "triangles": qinfo["num_triangles"],
-                       "samples_per_lane": dict(zip(["leaf_level", "level_above"], ctx.tuning()))},
+                       "samples_per_lane": dict(zip(["leaf_level", "level_above"], ctx.tuning())),
+                       "eval_config": dict(zip(["leaf_level", "level_above"],
+                                               [dict(zip(["samples_per_lane", "warps_per_block", "staged_candidates"],
+                                                         c)) for c in ctx.tuning_config()]))},
             "field_evals_per_s": world * ev_ref / (ms / 1000.0),
             "field_evals_per_frame": {"reference_equivalent": ev_ref, "performed": ev_done,
                                       "note": "reference_equivalent: the SingleEval calls the reference makes for "

@@ -82,6 +82,8 @@ def _declare(L):
         "pi_ctx_stream": (P, [P]),
         "pi_ctx_tune": (C.c_int, [P, C.c_int32]),
         "pi_ctx_tuning": (C.c_int, [P, C.POINTER(C.c_int32)]),
+        "pi_ctx_tuning_config": (C.c_int, [P, C.POINTER(C.c_int32)]),
+        "pi_ctx_tune_config": (C.c_int, [P, C.c_int32]),
         "pi_frame_create": (C.c_int, [P, C.POINTER(Params), PP]),
         "pi_frame_destroy": (C.c_int, [P]),
         "pi_frame_upload": (C.c_int, [P, fp, i64]),
@@ -260,6 +262,16 @@ class Context:
         out = (C.c_int32 * 2)()
         check(lib().pi_ctx_tuning(self.h, out))
         return [out[0], out[1]]
+
+    def tuning_config(self):
+        """[leaf level, level above]: (K, warps per block, staged candidates) in use."""
+        out = (C.c_int32 * 6)()
+        check(lib().pi_ctx_tuning_config(self.h, out))
+        return [tuple(out[0:3]), tuple(out[3:6])]
+
+    def tune_config(self, index):
+        """Fix entry `index` (0-7) of the evaluation configuration table; -1 = time them."""
+        check(lib().pi_ctx_tune_config(self.h, index))
 
     def profile(self, enable=True):
         check(lib().pi_ctx_profile(self.h, 1 if enable else 0))

@@ -539,15 +539,37 @@ int pi_ctx_tune(pi_ctx* c, int32_t samples_per_lane) {
   PI_CHECK(samples_per_lane == 0 || samples_per_lane == 1 || samples_per_lane == 2 || samples_per_lane == 4,
            "samples per lane must be 0, 1, 2 or 4");
   c->eval_forced = samples_per_lane;
-  c->eval_lanes[0] = c->eval_lanes[1] = 0;
+  c->eval_cfg[0] = c->eval_cfg[1] = 0;
   PI_API_END
 }
 
 int pi_ctx_tuning(const pi_ctx* c, int32_t* out2) {
   PI_API_BEGIN
   PI_CHECK(c && out2, "null argument");
-  out2[0] = c->eval_forced ? c->eval_forced : c->eval_lanes[0];
-  out2[1] = c->eval_forced ? c->eval_forced : c->eval_lanes[1];
+  for (int k = 0; k < 2; ++k)
+    out2[k] = c->eval_forced ? c->eval_forced : c->eval_cfg[k] ? kEvalTable[c->eval_cfg[k] - 1].K : 0;
+  PI_API_END
+}
+
+int pi_ctx_tune_config(pi_ctx* c, int32_t index) {
+  PI_API_BEGIN
+  PI_CHECK(c, "ctx is null");
+  PI_CHECK(index >= -1 && index < kEvalConfigs, "configuration index out of range");
+  c->eval_forced = 0;
+  c->eval_cfg[0] = c->eval_cfg[1] = index + 1;
+  PI_API_END
+}
+
+int pi_ctx_tuning_config(const pi_ctx* c, int32_t* out6) {
+  PI_API_BEGIN
+  PI_CHECK(c && out6, "null argument");
+  for (int k = 0; k < 2; ++k) {
+    int cfg = c->eval_cfg[k] - 1;
+    if (c->eval_forced) cfg = c->eval_forced == 1 ? 0 : c->eval_forced == 2 ? 1 : 2;
+    out6[3 * k] = cfg >= 0 ? kEvalTable[cfg].K : 0;
+    out6[3 * k + 1] = cfg >= 0 ? kEvalTable[cfg].W : 0;
+    out6[3 * k + 2] = cfg >= 0 ? kEvalTable[cfg].CB : 0;
+  }
   PI_API_END
 }
 

@@ -13,7 +13,7 @@
 
 namespace pisurf {
 
-constexpr int kCandBuf = 96;  // staged candidate records per warp
+constexpr int kCandBuf = 96;  // staged candidate records per warp (default; k_q_eval tunes it)
 
 // Order-preserving map of a float onto a signed int (for warp min / max).
 __device__ __forceinline__ int fkey(float v) {
@@ -31,7 +31,7 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Per-warp staging buffer (shared memory): the staged candidates' records,
-// one array of kCandBuf floats per component (structure of arrays), so that a
+// one array of CB floats per component (structure of arrays), so that a
 // component of two consecutive candidates is one 8-byte load feeding the
 // packed FP32 instructions below.
 enum : int {
@@ -41,10 +41,11 @@ enum : int {
   SC_B0, SC_B1, SC_B2,     // a12 a22 det * Sigma
   kStageComps
 };
-constexpr int kStageFloats = kStageComps * kCandBuf;  // per warp
+__host__ __device__ constexpr int stage_floats(int cb) { return kStageComps * cb; }  // per warp
+constexpr int kStageFloats = stage_floats(kCandBuf);
 
 struct ChunkStage {
-  float* c;  // c[k * kCandBuf + t]: component k of staged candidate t
+  float* c;  // c[k * CB + t]: component k of staged candidate t
 };
 
 // 4-byte asynchronous copy global -> shared.
@@ -53,8 +54,9 @@ __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
 
+template <int CB>
 __device__ __forceinline__ float2 ld_pair(const ChunkStage& st, int k, int t) {
-  return *reinterpret_cast<const float2*>(st.c + k * kCandBuf + t);
+  return *reinterpret_cast<const float2*>(st.c + k * CB + t);
 }
 
 // Sums over the chunk's candidates for the K points of this lane.  act[m]
@@ -72,7 +74,9 @@ __device__ __forceinline__ float2 ld_pair(const ChunkStage& st, int k, int t) {
 // as fma(b, -1, a), exact in the product, one rounding), so every term is
 // bit for bit the scalar one; the compensated sum then takes the two terms
 // one after the other, in candidate order.
-template <int K>
+// CB staged candidates per warp (a multiple of 32 above 32); the flush
+// points move with it, the terms and their order do not.
+template <int K, int CB = kCandBuf>
 __device__ __forceinline__ void chunk_field(const GridView& g, const PartView& P, int cx, int cy, int cz,
                                             const float (&qx)[K], const float (&qy)[K], const float (&qz)[K],
                                             const bool (&act)[K], const bool (&slots)[K], const ChunkStage& st,
@@ -126,11 +130,11 @@ __device__ __forceinline__ void chunk_field(const GridView& g, const PartView& P
 #pragma unroll 1
     for (int t = 0; t < nc; t += 2) {
       const bool two = t + 1 < nc;  // warp-uniform: a second candidate in this pair
-      const float2 X = ld_pair(st, SC_X, t), Y = ld_pair(st, SC_Y, t), Z = ld_pair(st, SC_Z, t);
-      const float2 LX = ld_pair(st, SC_LX, t), LY = ld_pair(st, SC_LY, t), LZ = ld_pair(st, SC_LZ, t);
-      const float2 A0 = ld_pair(st, SC_A0, t), A1 = ld_pair(st, SC_A1, t), A2 = ld_pair(st, SC_A2, t),
-                   A3 = ld_pair(st, SC_A3, t);
-      const float2 B0 = ld_pair(st, SC_B0, t), B1 = ld_pair(st, SC_B1, t), B2 = ld_pair(st, SC_B2, t);
+      const float2 X = ld_pair<CB>(st, SC_X, t), Y = ld_pair<CB>(st, SC_Y, t), Z = ld_pair<CB>(st, SC_Z, t);
+      const float2 LX = ld_pair<CB>(st, SC_LX, t), LY = ld_pair<CB>(st, SC_LY, t), LZ = ld_pair<CB>(st, SC_LZ, t);
+      const float2 A0 = ld_pair<CB>(st, SC_A0, t), A1 = ld_pair<CB>(st, SC_A1, t), A2 = ld_pair<CB>(st, SC_A2, t),
+                   A3 = ld_pair<CB>(st, SC_A3, t);
+      const float2 B0 = ld_pair<CB>(st, SC_B0, t), B1 = ld_pair<CB>(st, SC_B1, t), B2 = ld_pair<CB>(st, SC_B2, t);
 #pragma unroll
       for (int m = 0; m < K; ++m) {
         if (!slots[m]) continue;  // warp-uniform
@@ -182,25 +186,25 @@ __device__ __forceinline__ void chunk_field(const GridView& g, const PartView& P
         if (pass) {
           const int p = nc + __popc(pm & lt);
           float* const c0 = st.c + p;
-          c0[SC_X * kCandBuf] = x.x;
-          c0[SC_Y * kCandBuf] = x.y;
-          c0[SC_Z * kCandBuf] = x.z;
+          c0[SC_X * CB] = x.x;
+          c0[SC_Y * CB] = x.y;
+          c0[SC_Z * CB] = x.z;
           const float* ga = reinterpret_cast<const float*>(P.ga + j);
           const float* gb = reinterpret_cast<const float*>(P.gb + j);
           const float* gl = reinterpret_cast<const float*>(P.xlo + j);
-          cp_async4(c0 + SC_LX * kCandBuf, gl);
-          cp_async4(c0 + SC_LY * kCandBuf, gl + 1);
-          cp_async4(c0 + SC_LZ * kCandBuf, gl + 2);
-          cp_async4(c0 + SC_A0 * kCandBuf, ga);
-          cp_async4(c0 + SC_A1 * kCandBuf, ga + 1);
-          cp_async4(c0 + SC_A2 * kCandBuf, ga + 2);
-          cp_async4(c0 + SC_A3 * kCandBuf, ga + 3);
-          cp_async4(c0 + SC_B0 * kCandBuf, gb);
-          cp_async4(c0 + SC_B1 * kCandBuf, gb + 1);
-          cp_async4(c0 + SC_B2 * kCandBuf, gb + 2);
+          cp_async4(c0 + SC_LX * CB, gl);
+          cp_async4(c0 + SC_LY * CB, gl + 1);
+          cp_async4(c0 + SC_LZ * CB, gl + 2);
+          cp_async4(c0 + SC_A0 * CB, ga);
+          cp_async4(c0 + SC_A1 * CB, ga + 1);
+          cp_async4(c0 + SC_A2 * CB, ga + 2);
+          cp_async4(c0 + SC_A3 * CB, ga + 3);
+          cp_async4(c0 + SC_B0 * CB, gb);
+          cp_async4(c0 + SC_B1 * CB, gb + 1);
+          cp_async4(c0 + SC_B2 * CB, gb + 2);
         }
         nc += __popc(pm);
-        if (nc > kCandBuf - 32) flush();
+        if (nc > CB - 32) flush();
       }
     }
   flush();

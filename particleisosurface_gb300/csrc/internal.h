@@ -58,6 +58,14 @@ struct GridHost {
   int bits;  // radix sort width for key+1
 };
 
+// Configurations of the chunked field evaluation at octree samples
+// (octree.cu): samples per lane, warps per block, staged candidates per warp.
+struct EvalConfig {
+  int K, W, CB;
+};
+constexpr int kEvalConfigs = 8;
+extern const EvalConfig kEvalTable[kEvalConfigs];
+
 }  // namespace pisurf
 
 struct pi_ctx {
@@ -80,7 +88,7 @@ struct pi_ctx {
   // samples per lane of the chunked field evaluation, per dense-level kind
   // (0: leaf level, cell-octant buckets; 1: the level above, cell buckets);
   // 0 = not chosen yet (timed on the first such level), forced by pi_ctx_tune
-  int eval_lanes[2] = {0, 0};
+  int eval_cfg[2] = {0, 0};  // chosen configuration + 1 per dense level kind (0: not yet)
   int eval_forced = 0;
   // pinned host area for reads that need no synchronisation of their own:
   // per-stage counter snapshots (kPinSlots x kCounterWords words) and one

@@ -43,7 +43,6 @@ namespace pisurf {
 enum : int8_t { T_EMPTY = 0, T_INTERNAL = 1, T_LEAF = 2, T_UNCERTAIN = 3 };
 
 constexpr int kQ = 28;  // 27 samples + the centre per node
-constexpr int kEvalWarps = 8;   // warps per block of k_q_eval
 constexpr int kSpawnWarps = 2;  // warps per block of k_spawn_scan (small blocks: a warp that scans a whole block does not hold up seven others)
 
 struct LevelArgs {
@@ -327,13 +326,16 @@ __global__ void k_q_chunks(long long nb, const int* __restrict__ ucnt, int chunk
 
 // Field at the samples of one chunk per warp (persistent, grid-stride over
 // the chunks); a chunk holds up to 32 K samples and lane l holds samples
-// l, l + 32, ..., K per lane (K is autotuned per context, see
-// eval_lanes_for).  All samples of a chunk share a hash cell, hence the
+// l, l + 32, ..., K per lane (K, W and CB are autotuned per context, see
+// eval_config_for).  All samples of a chunk share a hash cell, hence the
 // 27-cell candidate list of Evaluator::SingleEval; chunk_field filters the
 // candidates against the chunk's bounding box, stages the survivors in
 // shared memory and sums in candidate order.
-template <int K>
-__global__ void __launch_bounds__(32 * kEvalWarps, (K > 2 ? 3 : 4)) k_q_eval(QArgs a, const int* __restrict__ order,
+// Blocks of W warps, each with a staging buffer of CB candidates (static
+// shared memory W * 13 * CB floats, at most 48 KiB); the register bound
+// keeps 768 (K = 4) or 1024 threads per SM whatever W.
+template <int K, int W, int CB>
+__global__ void __launch_bounds__(32 * W, (K > 2 ? 24 : 32) / W) k_q_eval(QArgs a, const int* __restrict__ order,
                                                             const int* __restrict__ qoff,
                                                             const int* __restrict__ ucnt,
                                                             const int2* __restrict__ chunks,
@@ -342,14 +344,14 @@ __global__ void __launch_bounds__(32 * kEvalWarps, (K > 2 ? 3 : 4)) k_q_eval(QAr
                                                             const float4* __restrict__ nd_v,
                                                             float* __restrict__ qval,
                                                             unsigned long long* __restrict__ counters) {
-  __shared__ __align__(16) float s_stage[kEvalWarps][kStageFloats];
+  __shared__ __align__(16) float s_stage[W][stage_floats(CB)];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const ChunkStage st{s_stage[wib]};
   const int nchunks = *nchunks_ptr;
-  const int nwarps = gridDim.x * kEvalWarps;
+  const int nwarps = gridDim.x * W;
   long long pairs = 0, done = 0;
-  for (int ci = blockIdx.x * kEvalWarps + wib; ci < nchunks; ci += nwarps) {
+  for (int ci = blockIdx.x * W + wib; ci < nchunks; ci += nwarps) {
     const int2 ch = chunks[ci];
     const int len = min(32 * K, __ldg(ucnt + ch.x) - ch.y);
     done += len;
@@ -373,7 +375,7 @@ __global__ void __launch_bounds__(32 * kEvalWarps, (K > 2 ? 3 : 4)) k_q_eval(QAr
     cell_of(a.g, __shfl_sync(0xffffffffu, x[0], 0), __shfl_sync(0xffffffffu, y[0], 0),
             __shfl_sync(0xffffffffu, z[0], 0), cx, cy, cz);
     float sum[K];
-    chunk_field<K>(a.g, a.P, cx, cy, cz, x, y, z, act, slots, st, sum, pairs);
+    chunk_field<K, CB>(a.g, a.P, cx, cy, cz, x, y, z, act, slots, st, sum, pairs);
 #pragma unroll
     for (int m = 0; m < K; ++m)
       if (act[m]) qval[q[m]] = a.iso - sum[m];
@@ -904,73 +906,91 @@ __global__ void k_root(float cx, float cy, float cz, float h, int size, float4* 
   nd_org[0] = make_int4(0, 0, 0, size);
 }
 
-template <int K>
-static void launch_eval(pi_frame* f, const QArgs& qa, long long qn, const int* order, const int* qoff,
+template <int K, int W, int CB>
+static void launch_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, const int* order, const int* qoff,
                         const int* ucnt, const int2* chunks, const int* nchunks, float* qval,
                         unsigned long long* counters) {
   pi_ctx* ctx = f->ctx;
-  static thread_local int occ[64][3] = {};
-  const int dev = ctx->device & 63, slot = K == 1 ? 0 : K == 2 ? 1 : 2;
-  if (occ[dev][slot] == 0) {
+  static thread_local int occ[64][kEvalConfigs] = {};
+  const int dev = ctx->device & 63;
+  if (occ[dev][cfg] == 0) {
     int nb = 0;
-    PI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_q_eval<K>, 32 * kEvalWarps, 0));
-    occ[dev][slot] = nb > 0 ? nb : 1;
+    PI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_q_eval<K, W, CB>, 32 * W, 0));
+    occ[dev][cfg] = nb > 0 ? nb : 1;
   }
-  const int blocks = (int)std::min<long long>((long long)ctx->smCount * occ[dev][slot],
-                                              div_up(qn, 32 * kEvalWarps));
-  PI_LAUNCH(k_q_eval<K>, blocks, 32 * kEvalWarps, 0, ctx->stream, qa, order, qoff, ucnt, chunks, nchunks, f->nd_c.p,
-            f->nd_v.p, qval, counters);
+  const int blocks = (int)std::min<long long>((long long)ctx->smCount * occ[dev][cfg], div_up(qn, 32 * W));
+  PI_LAUNCH((k_q_eval<K, W, CB>), blocks, 32 * W, 0, ctx->stream, qa, order, qoff, ucnt, chunks, nchunks,
+            f->nd_c.p, f->nd_v.p, qval, counters);
 }
 
-// Chunk list for K samples per lane, then the chunked evaluation.
-static void dense_eval(pi_frame* f, int K, const QArgs& qa, long long qn, long long nbuckets, const int* order,
+// The chunked evaluator's configurations: samples per lane K, warps per
+// block W, staged candidates per warp CB.  Index 1 (K 2, W 8, CB 96) is the
+// default; every configuration gives the same values (each sample's sum runs
+// over the same candidates in the same order).
+const EvalConfig kEvalTable[kEvalConfigs] = {{1, 8, 96}, {2, 8, 96}, {4, 8, 96}, {2, 4, 96},
+                                             {4, 4, 96}, {2, 8, 64}, {4, 8, 64}, {2, 16, 48}};
+
+// Chunk list for configuration cfg, then the chunked evaluation.
+static void dense_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, long long nbuckets, const int* order,
                        const int* qoff, const int* ucnt, int2* chunks, int* nchunks, float* qval,
                        unsigned long long* counters) {
   cudaStream_t s = f->ctx->stream;
+  const int K = kEvalTable[cfg].K;
   PI_CUDA(cudaMemsetAsync(nchunks, 0, sizeof(int), s));
   PI_LAUNCH(k_q_chunks, div_up(nbuckets, 256), 256, 0, s, nbuckets, ucnt, 32 * K, chunks, nchunks);
-  if (K == 1)
-    launch_eval<1>(f, qa, qn, order, qoff, ucnt, chunks, nchunks, qval, counters);
-  else if (K == 2)
-    launch_eval<2>(f, qa, qn, order, qoff, ucnt, chunks, nchunks, qval, counters);
-  else
-    launch_eval<4>(f, qa, qn, order, qoff, ucnt, chunks, nchunks, qval, counters);
+#define PI_EVAL_CASE(i, k, w, cb) \
+  case i:                         \
+    launch_eval<k, w, cb>(f, i, qa, qn, order, qoff, ucnt, chunks, nchunks, qval, counters); \
+    break;
+  switch (cfg) {
+    PI_EVAL_CASE(0, 1, 8, 96)
+    PI_EVAL_CASE(1, 2, 8, 96)
+    PI_EVAL_CASE(2, 4, 8, 96)
+    PI_EVAL_CASE(3, 2, 4, 96)
+    PI_EVAL_CASE(4, 4, 4, 96)
+    PI_EVAL_CASE(5, 2, 8, 64)
+    PI_EVAL_CASE(6, 4, 8, 64)
+    PI_EVAL_CASE(7, 2, 16, 48)
+    default:
+      throw std::logic_error("unknown evaluation configuration");
+  }
+#undef PI_EVAL_CASE
 }
 
-// Samples per lane for a dense level of the given kind: the context's choice,
-// or, the first time, the fastest of K = 1, 2, 4 timed on this level (the
-// evaluation is pure, so the runs give identical values).
-static int eval_lanes_for(pi_frame* f, int kind, const QArgs& qa, long long qn, long long nbuckets,
-                          const int* order, const int* qoff, const int* ucnt, int2* chunks, int* nchunks,
-                          float* qval) {
+// Configuration for a dense level of the given kind: the context's choice,
+// or, the first time, the fastest of the table timed on this level (the
+// evaluation is pure, so the runs give identical values).  A context whose K
+// is fixed (pi_ctx_tune) runs that K with the default W and CB.
+static int eval_config_for(pi_frame* f, int kind, const QArgs& qa, long long qn, long long nbuckets,
+                           const int* order, const int* qoff, const int* ucnt, int2* chunks, int* nchunks,
+                           float* qval) {
   pi_ctx* ctx = f->ctx;
-  if (ctx->eval_forced) return ctx->eval_forced;
-  if (ctx->eval_lanes[kind]) return ctx->eval_lanes[kind];
+  if (ctx->eval_forced) return ctx->eval_forced == 1 ? 0 : ctx->eval_forced == 2 ? 1 : 2;
+  if (ctx->eval_cfg[kind]) return ctx->eval_cfg[kind] - 1;
   cudaStream_t s = ctx->stream;
   cudaEvent_t e0, e1;
   PI_CUDA(cudaEventCreate(&e0));
   PI_CUDA(cudaEventCreate(&e1));
-  static const int cand[3] = {1, 2, 4};
   float best = 1e30f;
-  int bestk = 2;
+  int bestc = 1;
   DBuf<unsigned long long> scratch;  // the trial runs' event counters are not the frame's
   scratch.alloc(ctx, s, kCounterWords);
-  for (int c = 0; c < 3; ++c) {
+  for (int c = 0; c < kEvalConfigs; ++c) {
     PI_CUDA(cudaEventRecord(e0, s));
-    dense_eval(f, cand[c], qa, qn, nbuckets, order, qoff, ucnt, chunks, nchunks, qval, scratch.p);
+    dense_eval(f, c, qa, qn, nbuckets, order, qoff, ucnt, chunks, nchunks, qval, scratch.p);
     PI_CUDA(cudaEventRecord(e1, s));
     PI_CUDA(cudaEventSynchronize(e1));
     float ms = 0.f;
     PI_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     if (ms < best) {
       best = ms;
-      bestk = cand[c];
+      bestc = c;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  ctx->eval_lanes[kind] = bestk;
-  return bestk;
+  ctx->eval_cfg[kind] = bestc + 1;
+  return bestc;
 }
 
 static void ensure_nodes(pi_frame* f, long long need) {
@@ -1331,14 +1351,14 @@ void stage_octree(pi_frame* f) {
         exclusive_scan_i32(ucnt.p, ucum.p, nb + 1, nullptr, f->tmp.p, s);
         PI_LAUNCH(k_q_compact, div_up(nb, 256), 256, 0, s, nb, qcnt.p, ucnt.p, ucum.p, order.p, list);
       }
-      int lanes = 0;
+      int cfg = 0;
       if (dense)
-        lanes = eval_lanes_for(f, depth == f->dmax ? 0 : 1, qa, qn, nb, order.p, qcnt.p, ucnt.p, chunks.p,
-                               qcnt.p + nb + 1, qval.p);
+        cfg = eval_config_for(f, depth == f->dmax ? 0 : 1, qa, qn, nb, order.p, qcnt.p, ucnt.p, chunks.p,
+                              qcnt.p + nb + 1, qval.p);
       const int pg = dense ? PG_CHUNK : PG_THREAD;
       prof_begin(ctx, s, pg);
       if (dense)
-        dense_eval(f, lanes, qa, qn, nb, order.p, qcnt.p, ucnt.p, chunks.p, qcnt.p + nb + 1, qval.p, f->dcount.p);
+        dense_eval(f, cfg, qa, qn, nb, order.p, qcnt.p, ucnt.p, chunks.p, qcnt.p + nb + 1, qval.p, f->dcount.p);
       else
         PI_LAUNCH(k_q_eval_thread, (int)std::min<long long>((long long)ctx->smCount * 8, div_up(qn, 256)), 256, 0,
                   s, qa, list, ucum.p + nb, f->nd_c.p, f->nd_v.p, qval.p, f->dcount.p);

@@ -49,8 +49,38 @@ def test_samples_per_lane_change_no_result(ctx, qef):
     ctx.tune(0)
 
 
+@pytest.mark.parametrize("qef", [False, True])
+def test_every_evaluation_configuration_gives_the_same_frame(ctx, qef):
+    """Warps per block and staged candidates per warp (with K, the table the
+    timing chooses from) change neither a node nor the mesh."""
+    fr = synth.slab_and_sphere(n=20000, seed=1)
+    ref = run_frame(ctx, fr, qef, 2)
+    seen = set()
+    for i in range(8):
+        ctx.tune_config(i)
+        g = N.Frame(ctx, N.default_params(fr.radius, qef=qef)).upload(fr.xyz).run()
+        nodes = g.dump(N.DUMP_NODES)
+        v, t = g.mesh()
+        cfg = ctx.tuning_config()
+        g.close()
+        assert nodes.tobytes() == ref[0].tobytes(), i
+        assert np.array_equal(v, ref[1]) and np.array_equal(t, ref[2]), i
+        assert cfg[0] == cfg[1]
+        seen.add(cfg[1])
+    assert len(seen) == 8
+    ctx.tune_config(-1)
+    g = N.Frame(ctx, N.default_params(fr.radius, qef=qef)).upload(fr.xyz).run()
+    assert g.dump(N.DUMP_NODES).tobytes() == ref[0].tobytes()
+    assert ctx.tuning_config()[1] in seen
+    g.close()
+    ctx.tune(0)
+
+
 def test_tune_rejects_other_values(ctx):
     for k in (3, 8, -1):
         with pytest.raises(N.PiError):
             ctx.tune(k)
+    for i in (8, -2):
+        with pytest.raises(N.PiError):
+            ctx.tune_config(i)
     ctx.tune(0)
