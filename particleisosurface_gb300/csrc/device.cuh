@@ -74,22 +74,6 @@ __device__ __forceinline__ int cell_coord_q(float p, float lo, float cell, int n
   return c;
 }
 
-// Lanes of a full warp whose keys equal their lower neighbour's form runs;
-// returns the mask of this lane's run.  Aggregates atomics where equal keys
-// sit in adjacent lanes (a node's samples are consecutive and mostly share a
-// bucket) for a fraction of __match_any_sync's cost; equal keys in separate
-// runs simply take separate atomics.
-__device__ __forceinline__ unsigned run_peers(int key) {
-  const int lane = threadIdx.x & 31;
-  const int prev = __shfl_up_sync(0xffffffffu, key, 1);
-  const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != key);
-  const unsigned upto = 0xffffffffu >> (31 - lane);  // lanes 0..lane
-  const int start = 31 - __clz(heads & upto);
-  const unsigned above = heads & ~upto;
-  const unsigned below_end = above ? (1u << (__ffs(above) - 1)) - 1u : 0xffffffffu;
-  return below_end & ~((1u << start) - 1u);
-}
-
 __device__ __forceinline__ void cell_of(const GridView& g, float x, float y, float z, int& cx,
                                         int& cy, int& cz) {
   cx = cell_coord(x, g.b0, g.cell, g.nx);

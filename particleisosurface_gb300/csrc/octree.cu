@@ -203,7 +203,7 @@ __global__ void k_q_count(QArgs a, const float4* __restrict__ nd_c, const float4
       k = k * 8 + ((fx - (float)cx >= 0.5f ? 1 : 0) | (fy - (float)cy >= 0.5f ? 2 : 0) |
                    (fz - (float)cz >= 0.5f ? 4 : 0));
   }
-  const unsigned peers = run_peers(k);
+  const unsigned peers = __match_any_sync(0xffffffffu, k);
   const int leader = __ffs(peers) - 1;
   if (valid && lane == leader) atomicAdd(qcnt + k, __popc(peers));
   if (in_level) qkey[i] = k;
@@ -288,10 +288,9 @@ __global__ void k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c
     rep[i] = r;
     uniq = r == (int)i;
   }
-  // places for the representatives, one atomic per run of a bucket's
-  // samples in the warp
+  // places for the representatives, one atomic per bucket and warp
   const unsigned um = __ballot_sync(0xffffffffu, uniq);
-  const unsigned peers = run_peers(k) & um;
+  const unsigned peers = __match_any_sync(0xffffffffu, uniq ? k : -1) & um;
   if (uniq) {
     const int leader = __ffs(peers) - 1;
     int b0 = 0;
