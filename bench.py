@@ -37,6 +37,7 @@ from __future__ import annotations
 
 import argparse
 import concurrent.futures as cf
+import hashlib
 import json
 import multiprocessing as mp
 import os
@@ -83,6 +84,8 @@ def parse():
     p.add_argument("--qef", action="store_true", help="with --single: per-leaf QEF vertices on")
     p.add_argument("--samples-per-lane", type=int, default=0, choices=[0, 1, 2, 4],
                    help="with --single: fix the chunked evaluation's samples per lane (0 = timed choice)")
+    p.add_argument("--eval-config", type=int, default=-1,
+                   help="with --single: fix the chunked evaluator's configuration (table index) and time it")
     p.add_argument("--single", action="store_true",
                    help="reconstruct one frame once and print its counters (for profiler captures)")
     p.add_argument("--workload", choices=["dam_break_1m", "batch64", "serving", "stress", "grid"],
@@ -574,7 +577,7 @@ def ours(a):
                        "triangles": qinfo["num_triangles"],
                        "samples_per_lane": dict(zip(["leaf_level", "level_above"], ctx.tuning())),
                        "eval_config": dict(zip(["leaf_level", "level_above"],
-                                               [dict(zip(["samples_per_lane", "warps_per_block", "staged_candidates"],
+                                               [dict(zip(["samples_per_lane", "warps_per_block", "staged_candidates", "bulk_staging"],
                                                          c)) for c in ctx.tuning_config()]))},
             "field_evals_per_s": world * ev_ref / (ms / 1000.0),
             "field_evals_per_frame": {"reference_equivalent": ev_ref, "performed": ev_done,
@@ -834,17 +837,33 @@ def stress(a):
 
 
 def single(a):
+    """One frame (the ncu launch lists run this); with --eval-config i, the
+    chunked evaluator fixed at table entry i and its event-timed kernel group
+    over --steps frames after one (an A/B of evaluation configurations)."""
     from particleisosurface_gb300 import _native as N
     from particleisosurface_gb300 import build as B
     B.build()
     fr = make_frame(a.n)
     ctx = N.Context(0)
     ctx.tune(a.samples_per_lane)
+    if a.eval_config >= 0:
+        ctx.tune_config(a.eval_config)
     p = N.default_params(fr.radius, qef=a.qef)
     f = N.Frame(ctx, p).upload(fr.xyz).run()
     info = f.info()
-    print(json.dumps({k: info[k] for k in ("num_nodes", "num_vertices", "num_triangles", "field_evals",
-                                           "field_evals_performed", "candidate_pairs", "stage_ms", "qef_accepted")}))
+    out = {k: info[k] for k in ("num_nodes", "num_vertices", "num_triangles", "field_evals", "field_evals_performed",
+                                "candidate_pairs", "stage_ms", "qef_accepted")}
+    if a.eval_config >= 0:
+        ctx.profile(True)
+        ms = []
+        for _ in range(a.steps):
+            ctx.kernel_groups()
+            f.reset().run()
+            ms.append(ctx.kernel_groups()["chunked_sampling"]["ms"])
+        out.update(eval_config=ctx.tuning_config(), chunked_sampling_ms=ms,
+                   chunked_sampling_median_ms=float(np.median(ms)),
+                   nodes_sha256=hashlib.sha256(f.dump(N.DUMP_NODES).tobytes()).hexdigest())
+    print(json.dumps(out))
     f.close()
     ctx.close()
 

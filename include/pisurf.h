@@ -163,13 +163,17 @@ int pi_ctx_kernel_groups(pi_ctx* ctx, int32_t ngroups, double* ms, int64_t* laun
 int pi_ctx_tune(pi_ctx* ctx, int32_t samples_per_lane);
 int pi_ctx_tuning(const pi_ctx* ctx, int32_t* out2);
 /* The whole configuration the timing chose per level kind (leaf level, level
- * above): out6 = K, warps per block, staged candidates per warp, for each.
- * The timing runs every configuration of a fixed table (K 1, 2, 4; 4, 8 or
- * 16 warps; 48, 64 or 96 staged candidates) once on the first level of each
- * kind; pi_ctx_tune(ctx, K) fixes K with 8 warps and 96 candidates. */
-int pi_ctx_tuning_config(const pi_ctx* ctx, int32_t* out6);
-/* Fixes entry `index` (0-7) of that table for both level kinds; -1 returns
- * to timing. */
+ * above): out8 = K, warps per block, staged candidates per warp, staging (0:
+ * box test from global memory, then cp.async of the survivors; 1: TMA bulk
+ * copies of whole row runs, box test from shared memory), for each.  The
+ * timing runs every configuration of a fixed table (pi_eval_configs()
+ * entries: K 1, 2, 4; 4, 8 or 16 warps; 48, 64 or 96 staged candidates; both
+ * stagings) once on the first level of each kind; pi_ctx_tune(ctx, K) fixes
+ * K with 8 warps, 96 candidates and the first staging. */
+int pi_ctx_tuning_config(const pi_ctx* ctx, int32_t* out8);
+int pi_eval_configs(void);
+/* Fixes entry `index` (0 to pi_eval_configs() - 1) of that table for both
+ * level kinds; -1 returns to timing. */
 int pi_ctx_tune_config(pi_ctx* ctx, int32_t index);
 /* The context stream as a cudaStream_t cast to void*. */
 void* pi_ctx_stream(pi_ctx* ctx);

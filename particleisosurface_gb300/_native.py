@@ -84,6 +84,7 @@ def _declare(L):
         "pi_ctx_tuning": (C.c_int, [P, C.POINTER(C.c_int32)]),
         "pi_ctx_tuning_config": (C.c_int, [P, C.POINTER(C.c_int32)]),
         "pi_ctx_tune_config": (C.c_int, [P, C.c_int32]),
+        "pi_eval_configs": (C.c_int, []),
         "pi_frame_create": (C.c_int, [P, C.POINTER(Params), PP]),
         "pi_frame_destroy": (C.c_int, [P]),
         "pi_frame_upload": (C.c_int, [P, fp, i64]),
@@ -264,13 +265,17 @@ class Context:
         return [out[0], out[1]]
 
     def tuning_config(self):
-        """[leaf level, level above]: (K, warps per block, staged candidates) in use."""
-        out = (C.c_int32 * 6)()
+        """[leaf level, level above]: (K, warps per block, staged candidates, bulk staging) in use."""
+        out = (C.c_int32 * 8)()
         check(lib().pi_ctx_tuning_config(self.h, out))
-        return [tuple(out[0:3]), tuple(out[3:6])]
+        return [tuple(out[0:4]), tuple(out[4:8])]
+
+    @staticmethod
+    def eval_configs():
+        return lib().pi_eval_configs()
 
     def tune_config(self, index):
-        """Fix entry `index` (0-7) of the evaluation configuration table; -1 = time them."""
+        """Fix entry `index` of the evaluation configuration table; -1 = time them."""
         check(lib().pi_ctx_tune_config(self.h, index))
 
     def profile(self, enable=True):

@@ -166,6 +166,8 @@ void resolve_pending(pi_frame* f) {
     f->pairs = (long long)c[C_SAMPLE_PAIRS];
     f->qefAccepted = (long long)c[C_QEF_ACCEPTED];
     f->qefSingular = (long long)c[C_QEF_SINGULAR];
+    if (c[C_STAGE_TIMEOUT])
+      throw CudaError("a bulk-staging wait of the field evaluation ran out; the frame's values are void", 0);
     if (ctx->profile) {
       ctx->group_pairs[PG_CHUNK] += (int64_t)c[C_PAIRS_CHUNK];
       ctx->group_pairs[PG_THREAD] += (int64_t)c[C_PAIRS_THREAD];
@@ -560,18 +562,21 @@ int pi_ctx_tune_config(pi_ctx* c, int32_t index) {
   PI_API_END
 }
 
-int pi_ctx_tuning_config(const pi_ctx* c, int32_t* out6) {
+int pi_ctx_tuning_config(const pi_ctx* c, int32_t* out8) {
   PI_API_BEGIN
-  PI_CHECK(c && out6, "null argument");
+  PI_CHECK(c && out8, "null argument");
   for (int k = 0; k < 2; ++k) {
     int cfg = c->eval_cfg[k] - 1;
     if (c->eval_forced) cfg = c->eval_forced == 1 ? 0 : c->eval_forced == 2 ? 1 : 2;
-    out6[3 * k] = cfg >= 0 ? kEvalTable[cfg].K : 0;
-    out6[3 * k + 1] = cfg >= 0 ? kEvalTable[cfg].W : 0;
-    out6[3 * k + 2] = cfg >= 0 ? kEvalTable[cfg].CB : 0;
+    out8[4 * k] = cfg >= 0 ? kEvalTable[cfg].K : 0;
+    out8[4 * k + 1] = cfg >= 0 ? kEvalTable[cfg].W : 0;
+    out8[4 * k + 2] = cfg >= 0 ? kEvalTable[cfg].CB : 0;
+    out8[4 * k + 3] = cfg >= 0 ? kEvalTable[cfg].bulk : 0;
   }
   PI_API_END
 }
+
+int pi_eval_configs(void) { return kEvalConfigs; }
 
 int pi_frame_create(pi_ctx* c, const pi_params* p, pi_frame** out) {
   PI_API_BEGIN

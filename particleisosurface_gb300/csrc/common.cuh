@@ -80,6 +80,7 @@ enum Counter : int {
   C_QEF_LEAVES = 12,   // leaves whose QEF k_qef solved
   C_DONE_THREAD = 13,  // evaluations performed by k_q_eval_thread (distinct samples)
   C_DONE_LEAF = 14,    // evaluations performed by k_leaf_level (one per leaf)
+  C_STAGE_TIMEOUT = 15,  // bulk-staging waits that ran out (an error: the frame's values are void)
   kCounters = 16
 };
 constexpr int kCounterWords = kCounters * kStripes * 4;

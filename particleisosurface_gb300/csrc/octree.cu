@@ -222,69 +222,111 @@ __device__ __forceinline__ uint32_t hash3(float x, float y, float z) {
 // same float coordinates bit for bit (about 2.4 per point on liquid
 // surfaces).  Equal coordinates give equal field values (same cell, same
 // candidates, same summation order), so each distinct point is evaluated
-// once.  Equal points share a bucket; bucket k owns hash slots
+// once; a pair of points is merged only when their coordinates are equal bit
+// for bit, so a merge never changes a value and a missed one only costs an
+// evaluation.
+//
+// A level's nodes come in sibling groups of 8 (the children of one parent,
+// octant k at group position k), and one block takes one group: its 8 x 27
+// lattice samples fall on the 5 x 5 x 5 lattice of the parent's box.  Each
+// lattice point's lowest slot owns it (a shared-memory atomicMin); another
+// slot on the same point with the same coordinates takes the owner's
+// representative without touching the hash.  Points inside the parent's box
+// lie on no other group's lattice, so their owners represent themselves;
+// owners of points on the box's faces (and any slot whose coordinates differ
+// from its owner's) go through the level's hash, in which bucket k owns slots
 // [2 qoff[k], 2 qoff[k+1]) and a point's first inserter becomes its
-// representative.  Representatives get consecutive places in the bucket's
-// range of `order` (on a dense level k_q_chunks then cuts them into chunks, on
-// a sparse level k_q_compact lists them in bucket order).
-__global__ void k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c, const float4* __restrict__ nd_v,
-                           const int* __restrict__ qkey, const int* __restrict__ qoff, unsigned* __restrict__ hslot,
-                           int* __restrict__ ucnt, int* __restrict__ rep, int* __restrict__ order) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
+// representative.  The node position (slot 27) is the centre sample's point
+// when the two are equal and else its own.  Representatives get consecutive
+// places in the bucket's range of `order` (on a dense level k_q_chunks then
+// cuts them into chunks, on a sparse level k_q_compact lists them in bucket
+// order).
+constexpr int kGroupSlots = 8 * kQ;  // one sibling group's slots: one block of k_q_dedupe
+
+__device__ __forceinline__ int hash_rep(const QArgs& a, long long i, int k, float qx, float qy, float qz,
+                                        const float4* __restrict__ nd_c, const float4* __restrict__ nd_v,
+                                        const int* __restrict__ qoff, unsigned* __restrict__ hslot) {
+  const long long base = 2LL * qoff[k];
+  const uint32_t m = 2u * (uint32_t)(qoff[k + 1] - qoff[k]);
+  uint32_t pos = __umulhi(hash3(qx, qy, qz), m);
+  for (uint32_t t = 0; t < m; ++t) {  // the region is at most half full
+    unsigned cur = hslot[base + pos];
+    if (cur == 0u) {
+      cur = atomicCAS(hslot + base + pos, 0u, (unsigned)i + 1u);
+      if (cur == 0u) return (int)i;  // first inserter: i represents the point
+    }
+    const long long j = (long long)cur - 1;
+    const long long nj = a.lb + j / kQ;
+    float px, py, pz;
+    sample_point(nd_c[nj], nd_v[nj], (int)(j % kQ), px, py, pz);
+    if (__float_as_uint(px) == __float_as_uint(qx) && __float_as_uint(py) == __float_as_uint(qy) &&
+        __float_as_uint(pz) == __float_as_uint(qz))
+      return (int)j;
+    pos = pos + 1u == m ? 0u : pos + 1u;
+  }
+  return (int)i;
+}
+
+__global__ void __launch_bounds__(kGroupSlots) k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c,
+                                                          const float4* __restrict__ nd_v,
+                                                          const int* __restrict__ qkey, const int* __restrict__ qoff,
+                                                          unsigned* __restrict__ hslot, int* __restrict__ ucnt,
+                                                          int* __restrict__ rep, int* __restrict__ order) {
+  __shared__ int s_owner[125];
+  __shared__ float s_pt[125][3];
+  __shared__ int s_rep[125];
+  const int tid = threadIdx.x;
+  const long long i = (long long)blockIdx.x * kGroupSlots + tid;
+  const int lane = tid & 31;
+  if (tid < 125) s_owner[tid] = 0x7fffffff;
   const int k = i < n ? qkey[i] : -1;
-  bool uniq = false;
-  int place = 0;
-  // the node's records load beside the key (the node index is valid for
-  // every i < n)
+  const int si = tid % kQ, child = tid / kQ;
   float4 nc = make_float4(0.f, 0.f, 0.f, 0.f), nv = nc;
   if (i < n) {
     const long long node = a.lb + i / kQ;
     nc = nd_c[node];
     nv = nd_v[node];
   }
-  const int si = (int)(i % kQ);
-  if (k >= 0 && (si == 13 || si == 27)) {
-    // the centre sample and the node position lie on no other node's
-    // lattice of this level (lattice points of a node are its centre +- 0 or
-    // h per axis, and centres are 2h apart): the centre sample represents
-    // itself, the node position is the centre sample's point when the two
-    // are bit-identical and else its own
-    int r = (int)i;
-    if (si == 27) {
-      float ax, ay, az, bx, by, bz;
-      sample_point(nc, nv, 27, ax, ay, az);
-      sample_point(nc, nv, 13, bx, by, bz);
-      if (__float_as_uint(ax) == __float_as_uint(bx) && __float_as_uint(ay) == __float_as_uint(by) &&
-          __float_as_uint(az) == __float_as_uint(bz))
-        r = (int)(i - 14);
-    }
-    rep[i] = r;
-    uniq = r == (int)i;
-  } else if (k >= 0) {
-    float qx, qy, qz;
+  float qx = 0.f, qy = 0.f, qz = 0.f;
+  int p = -1;  // the sample's point on the group's 5 x 5 x 5 lattice
+  if (k >= 0 && si < 27) {
     sample_point(nc, nv, si, qx, qy, qz);
-    const long long base = 2LL * qoff[k];
-    const uint32_t m = 2u * (uint32_t)(qoff[k + 1] - qoff[k]);
-    uint32_t pos = __umulhi(hash3(qx, qy, qz), m);
-    int r = (int)i;
-    for (uint32_t t = 0; t < m; ++t) {  // the region is at most half full
-      unsigned cur = hslot[base + pos];
-      if (cur == 0u) {
-        cur = atomicCAS(hslot + base + pos, 0u, (unsigned)i + 1u);
-        if (cur == 0u) break;  // first inserter: i represents the point
-      }
-      const long long j = (long long)cur - 1;
-      const long long nj = a.lb + j / kQ;
-      float px, py, pz;
-      sample_point(nd_c[nj], nd_v[nj], (int)(j % kQ), px, py, pz);
-      if (__float_as_uint(px) == __float_as_uint(qx) && __float_as_uint(py) == __float_as_uint(qy) &&
-          __float_as_uint(pz) == __float_as_uint(qz)) {
-        r = (int)j;
-        break;
-      }
-      pos = pos + 1u == m ? 0u : pos + 1u;
-    }
+    p = (2 * (child & 1) + si % 3) + 5 * (2 * ((child >> 1) & 1) + (si / 3) % 3) + 25 * (2 * (child >> 2) + si / 9);
+  }
+  __syncthreads();
+  if (p >= 0) atomicMin(&s_owner[p], tid);
+  __syncthreads();
+  const bool owner = p >= 0 && s_owner[p] == tid;
+  if (owner) {
+    s_pt[p][0] = qx;
+    s_pt[p][1] = qy;
+    s_pt[p][2] = qz;
+  }
+  __syncthreads();
+  int r = (int)i;
+  bool local = false;  // takes its owner's representative
+  if (p >= 0 && !owner) {
+    local = __float_as_uint(s_pt[p][0]) == __float_as_uint(qx) && __float_as_uint(s_pt[p][1]) == __float_as_uint(qy) &&
+            __float_as_uint(s_pt[p][2]) == __float_as_uint(qz);
+  }
+  if (p >= 0 && !local) {
+    const int X = p % 5, Y = (p / 5) % 5, Z = p / 25;
+    const bool face = X == 0 || X == 4 || Y == 0 || Y == 4 || Z == 0 || Z == 4;
+    if (face || !owner) r = hash_rep(a, i, k, qx, qy, qz, nd_c, nd_v, qoff, hslot);
+    if (owner) s_rep[p] = r;
+  } else if (k >= 0 && si == 27) {
+    float bx, by, bz;
+    sample_point(nc, nv, 13, bx, by, bz);
+    const float ax = nv.x, ay = nv.y, az = nv.z;
+    if (__float_as_uint(ax) == __float_as_uint(bx) && __float_as_uint(ay) == __float_as_uint(by) &&
+        __float_as_uint(az) == __float_as_uint(bz))
+      r = (int)(i - 14);  // the centre sample, which represents itself (an interior point)
+  }
+  __syncthreads();
+  if (local) r = s_rep[p];
+  bool uniq = false;
+  int place = 0;
+  if (k >= 0) {
     rep[i] = r;
     uniq = r == (int)i;
   }
@@ -331,9 +373,10 @@ __global__ void k_q_chunks(long long nb, const int* __restrict__ ucnt, int chunk
 // candidates against the chunk's bounding box, stages the survivors in
 // shared memory and sums in candidate order.
 // Blocks of W warps, each with a staging buffer of CB candidates (static
-// shared memory W * 13 * CB floats, at most 48 KiB); the register bound
-// keeps 768 (K = 4) or 1024 threads per SM whatever W.
-template <int K, int W, int CB>
+// shared memory W * 13 * CB floats, plus 4 KiB per warp with bulk staging,
+// at most 48 KiB); the register bound keeps 768 (K = 4) or 1024 threads per
+// SM whatever W.  BULK selects the bulk (TMA) staging of chunk_field_bulk.
+template <int K, int W, int CB, bool BULK>
 __global__ void __launch_bounds__(32 * W, (K > 2 ? 24 : 32) / W) k_q_eval(QArgs a, const int* __restrict__ order,
                                                             const int* __restrict__ qoff,
                                                             const int* __restrict__ ucnt,
@@ -344,9 +387,16 @@ __global__ void __launch_bounds__(32 * W, (K > 2 ? 24 : 32) / W) k_q_eval(QArgs 
                                                             float* __restrict__ qval,
                                                             unsigned long long* __restrict__ counters) {
   __shared__ __align__(16) float s_stage[W][stage_floats(CB)];
+  __shared__ __align__(16) float4 s_bulk[BULK ? W : 1][BULK ? 4 * kBulkCap : 1];
+  __shared__ __align__(8) uint64_t s_bar[W];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const ChunkStage st{s_stage[wib]};
+  BulkStage bs{s_bulk[BULK ? wib : 0], &s_bar[wib], 0u};
+  if (BULK) {
+    if (lane == 0) mbar_init(bs.bar);
+    __syncwarp();
+  }
   const int nchunks = *nchunks_ptr;
   const int nwarps = gridDim.x * W;
   long long pairs = 0, done = 0;
@@ -374,7 +424,12 @@ __global__ void __launch_bounds__(32 * W, (K > 2 ? 24 : 32) / W) k_q_eval(QArgs 
     cell_of(a.g, __shfl_sync(0xffffffffu, x[0], 0), __shfl_sync(0xffffffffu, y[0], 0),
             __shfl_sync(0xffffffffu, z[0], 0), cx, cy, cz);
     float sum[K];
-    chunk_field<K, CB>(a.g, a.P, cx, cy, cz, x, y, z, act, slots, st, sum, pairs);
+    if (BULK) {
+      if (!chunk_field_bulk<K, CB>(a.g, a.P, cx, cy, cz, x, y, z, act, slots, st, bs, counters, sum, pairs))
+        return;  // a staging wait ran out: the frame fails (C_STAGE_TIMEOUT)
+    } else {
+      chunk_field<K, CB>(a.g, a.P, cx, cy, cz, x, y, z, act, slots, st, sum, pairs);
+    }
 #pragma unroll
     for (int m = 0; m < K; ++m)
       if (act[m]) qval[q[m]] = a.iso - sum[m];
@@ -905,7 +960,7 @@ __global__ void k_root(float cx, float cy, float cz, float h, int size, float4* 
   nd_org[0] = make_int4(0, 0, 0, size);
 }
 
-template <int K, int W, int CB>
+template <int K, int W, int CB, bool BULK>
 static void launch_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, const int* order, const int* qoff,
                         const int* ucnt, const int2* chunks, const int* nchunks, float* qval,
                         unsigned long long* counters) {
@@ -914,20 +969,22 @@ static void launch_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, con
   const int dev = ctx->device & 63;
   if (occ[dev][cfg] == 0) {
     int nb = 0;
-    PI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_q_eval<K, W, CB>, 32 * W, 0));
+    PI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_q_eval<K, W, CB, BULK>, 32 * W, 0));
     occ[dev][cfg] = nb > 0 ? nb : 1;
   }
   const int blocks = (int)std::min<long long>((long long)ctx->smCount * occ[dev][cfg], div_up(qn, 32 * W));
-  PI_LAUNCH((k_q_eval<K, W, CB>), blocks, 32 * W, 0, ctx->stream, qa, order, qoff, ucnt, chunks, nchunks,
+  PI_LAUNCH((k_q_eval<K, W, CB, BULK>), blocks, 32 * W, 0, ctx->stream, qa, order, qoff, ucnt, chunks, nchunks,
             f->nd_c.p, f->nd_v.p, qval, counters);
 }
 
 // The chunked evaluator's configurations: samples per lane K, warps per
-// block W, staged candidates per warp CB.  Index 1 (K 2, W 8, CB 96) is the
-// default; every configuration gives the same values (each sample's sum runs
-// over the same candidates in the same order).
-const EvalConfig kEvalTable[kEvalConfigs] = {{1, 8, 96}, {2, 8, 96}, {4, 8, 96}, {2, 4, 96},
-                                             {4, 4, 96}, {2, 8, 64}, {4, 8, 64}, {2, 16, 48}};
+// block W, staged candidates per warp CB, bulk (TMA) staging.  Index 1
+// (K 2, W 8, CB 96, filter then cp.async) is the default; every
+// configuration gives the same values (each sample's sum runs over the same
+// candidates in the same order).
+const EvalConfig kEvalTable[kEvalConfigs] = {{1, 8, 96, 0}, {2, 8, 96, 0}, {4, 8, 96, 0}, {2, 4, 96, 0},
+                                             {4, 4, 96, 0}, {2, 8, 64, 0}, {4, 8, 64, 0}, {2, 16, 48, 0},
+                                             {2, 4, 96, 1}, {4, 4, 96, 1}};
 
 // Chunk list for configuration cfg, then the chunked evaluation.
 static void dense_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, long long nbuckets, const int* order,
@@ -937,19 +994,21 @@ static void dense_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, long
   const int K = kEvalTable[cfg].K;
   PI_CUDA(cudaMemsetAsync(nchunks, 0, sizeof(int), s));
   PI_LAUNCH(k_q_chunks, div_up(nbuckets, 256), 256, 0, s, nbuckets, ucnt, 32 * K, chunks, nchunks);
-#define PI_EVAL_CASE(i, k, w, cb) \
-  case i:                         \
-    launch_eval<k, w, cb>(f, i, qa, qn, order, qoff, ucnt, chunks, nchunks, qval, counters); \
+#define PI_EVAL_CASE(i, k, w, cb, bulk) \
+  case i:                               \
+    launch_eval<k, w, cb, bulk>(f, i, qa, qn, order, qoff, ucnt, chunks, nchunks, qval, counters); \
     break;
   switch (cfg) {
-    PI_EVAL_CASE(0, 1, 8, 96)
-    PI_EVAL_CASE(1, 2, 8, 96)
-    PI_EVAL_CASE(2, 4, 8, 96)
-    PI_EVAL_CASE(3, 2, 4, 96)
-    PI_EVAL_CASE(4, 4, 4, 96)
-    PI_EVAL_CASE(5, 2, 8, 64)
-    PI_EVAL_CASE(6, 4, 8, 64)
-    PI_EVAL_CASE(7, 2, 16, 48)
+    PI_EVAL_CASE(0, 1, 8, 96, false)
+    PI_EVAL_CASE(1, 2, 8, 96, false)
+    PI_EVAL_CASE(2, 4, 8, 96, false)
+    PI_EVAL_CASE(3, 2, 4, 96, false)
+    PI_EVAL_CASE(4, 4, 4, 96, false)
+    PI_EVAL_CASE(5, 2, 8, 64, false)
+    PI_EVAL_CASE(6, 4, 8, 64, false)
+    PI_EVAL_CASE(7, 2, 16, 48, false)
+    PI_EVAL_CASE(8, 2, 4, 96, true)
+    PI_EVAL_CASE(9, 4, 4, 96, true)
     default:
       throw std::logic_error("unknown evaluation configuration");
   }
@@ -1195,8 +1254,8 @@ static void stage_octree_vr(pi_frame* f) {
       QArgs qa{bg, P, f->iso, lb, le, ekx, eky, 0};
       PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
       exclusive_scan_i32(qcnt.p, qcnt.p, nb + 1, nullptr, f->tmp.p, s);
-      PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
-                ucnt.p, rep.p, order.p);
+      PI_LAUNCH(k_q_dedupe, div_up(qn, kGroupSlots), kGroupSlots, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p,
+                qcnt.p, hslot.p, ucnt.p, rep.p, order.p);
       int* list = reinterpret_cast<int*>(hslot.p);
       exclusive_scan_i32(ucnt.p, ucum.p, nb + 1, nullptr, f->tmp.p, s);
       PI_LAUNCH(k_q_compact, div_up(nb, 256), 256, 0, s, nb, qcnt.p, ucnt.p, ucum.p, order.p, list);
@@ -1343,8 +1402,8 @@ void stage_octree(pi_frame* f) {
       QArgs qa{g, P, f->iso, lb, le, ekx, eky, octants};
       PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
       exclusive_scan_i32(qcnt.p, qcnt.p, nb + 1, nullptr, f->tmp.p, s);
-      PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
-                ucnt.p, rep.p, order.p);
+      PI_LAUNCH(k_q_dedupe, div_up(qn, kGroupSlots), kGroupSlots, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p,
+                qcnt.p, hslot.p, ucnt.p, rep.p, order.p);
       int* list = reinterpret_cast<int*>(hslot.p);  // the hash slots are free once the samples are placed
       if (!dense) {
         exclusive_scan_i32(ucnt.p, ucum.p, nb + 1, nullptr, f->tmp.p, s);
