@@ -222,111 +222,51 @@ __device__ __forceinline__ uint32_t hash3(float x, float y, float z) {
 // same float coordinates bit for bit (about 2.4 per point on liquid
 // surfaces).  Equal coordinates give equal field values (same cell, same
 // candidates, same summation order), so each distinct point is evaluated
-// once; a pair of points is merged only when their coordinates are equal bit
-// for bit, so a merge never changes a value and a missed one only costs an
-// evaluation.
-//
-// A level's nodes come in sibling groups of 8 (the children of one parent,
-// octant k at group position k), and one block takes one group: its 8 x 27
-// lattice samples fall on the 5 x 5 x 5 lattice of the parent's box.  Each
-// lattice point's lowest slot owns it (a shared-memory atomicMin); another
-// slot on the same point with the same coordinates takes the owner's
-// representative without touching the hash.  Points inside the parent's box
-// lie on no other group's lattice, so their owners represent themselves;
-// owners of points on the box's faces (and any slot whose coordinates differ
-// from its owner's) go through the level's hash, in which bucket k owns slots
+// once.  Equal points share a bucket; bucket k owns hash slots
 // [2 qoff[k], 2 qoff[k+1]) and a point's first inserter becomes its
-// representative.  The node position (slot 27) is the centre sample's point
-// when the two are equal and else its own.  Representatives get consecutive
-// places in the bucket's range of `order` (on a dense level k_q_chunks then
-// cuts them into chunks, on a sparse level k_q_compact lists them in bucket
-// order).
-constexpr int kGroupSlots = 8 * kQ;  // one sibling group's slots: one block of k_q_dedupe
-
-__device__ __forceinline__ int hash_rep(const QArgs& a, long long i, int k, float qx, float qy, float qz,
-                                        const float4* __restrict__ nd_c, const float4* __restrict__ nd_v,
-                                        const int* __restrict__ qoff, unsigned* __restrict__ hslot) {
-  const long long base = 2LL * qoff[k];
-  const uint32_t m = 2u * (uint32_t)(qoff[k + 1] - qoff[k]);
-  uint32_t pos = __umulhi(hash3(qx, qy, qz), m);
-  for (uint32_t t = 0; t < m; ++t) {  // the region is at most half full
-    unsigned cur = hslot[base + pos];
-    if (cur == 0u) {
-      cur = atomicCAS(hslot + base + pos, 0u, (unsigned)i + 1u);
-      if (cur == 0u) return (int)i;  // first inserter: i represents the point
-    }
-    const long long j = (long long)cur - 1;
-    const long long nj = a.lb + j / kQ;
-    float px, py, pz;
-    sample_point(nd_c[nj], nd_v[nj], (int)(j % kQ), px, py, pz);
-    if (__float_as_uint(px) == __float_as_uint(qx) && __float_as_uint(py) == __float_as_uint(qy) &&
-        __float_as_uint(pz) == __float_as_uint(qz))
-      return (int)j;
-    pos = pos + 1u == m ? 0u : pos + 1u;
-  }
-  return (int)i;
-}
-
-__global__ void __launch_bounds__(kGroupSlots) k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c,
-                                                          const float4* __restrict__ nd_v,
-                                                          const int* __restrict__ qkey, const int* __restrict__ qoff,
-                                                          unsigned* __restrict__ hslot, int* __restrict__ ucnt,
-                                                          int* __restrict__ rep, int* __restrict__ order) {
-  __shared__ int s_owner[125];
-  __shared__ float s_pt[125][3];
-  __shared__ int s_rep[125];
-  const int tid = threadIdx.x;
-  const long long i = (long long)blockIdx.x * kGroupSlots + tid;
-  const int lane = tid & 31;
-  if (tid < 125) s_owner[tid] = 0x7fffffff;
+// representative.  Representatives get consecutive places in the bucket's
+// range of `order` (on a dense level k_q_chunks then cuts them into chunks, on
+// a sparse level k_q_compact lists them in bucket order).
+__global__ void k_q_dedupe(QArgs a, long long n, const float4* __restrict__ nd_c, const float4* __restrict__ nd_v,
+                           const int* __restrict__ qkey, const int* __restrict__ qoff, unsigned* __restrict__ hslot,
+                           int* __restrict__ ucnt, int* __restrict__ rep, int* __restrict__ order) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
   const int k = i < n ? qkey[i] : -1;
-  const int si = tid % kQ, child = tid / kQ;
+  bool uniq = false;
+  int place = 0;
+  // the node's records load beside the key (the node index is valid for
+  // every i < n)
   float4 nc = make_float4(0.f, 0.f, 0.f, 0.f), nv = nc;
   if (i < n) {
     const long long node = a.lb + i / kQ;
     nc = nd_c[node];
     nv = nd_v[node];
   }
-  float qx = 0.f, qy = 0.f, qz = 0.f;
-  int p = -1;  // the sample's point on the group's 5 x 5 x 5 lattice
-  if (k >= 0 && si < 27) {
-    sample_point(nc, nv, si, qx, qy, qz);
-    p = (2 * (child & 1) + si % 3) + 5 * (2 * ((child >> 1) & 1) + (si / 3) % 3) + 25 * (2 * (child >> 2) + si / 9);
-  }
-  __syncthreads();
-  if (p >= 0) atomicMin(&s_owner[p], tid);
-  __syncthreads();
-  const bool owner = p >= 0 && s_owner[p] == tid;
-  if (owner) {
-    s_pt[p][0] = qx;
-    s_pt[p][1] = qy;
-    s_pt[p][2] = qz;
-  }
-  __syncthreads();
-  int r = (int)i;
-  bool local = false;  // takes its owner's representative
-  if (p >= 0 && !owner) {
-    local = __float_as_uint(s_pt[p][0]) == __float_as_uint(qx) && __float_as_uint(s_pt[p][1]) == __float_as_uint(qy) &&
-            __float_as_uint(s_pt[p][2]) == __float_as_uint(qz);
-  }
-  if (p >= 0 && !local) {
-    const int X = p % 5, Y = (p / 5) % 5, Z = p / 25;
-    const bool face = X == 0 || X == 4 || Y == 0 || Y == 4 || Z == 0 || Z == 4;
-    if (face || !owner) r = hash_rep(a, i, k, qx, qy, qz, nd_c, nd_v, qoff, hslot);
-    if (owner) s_rep[p] = r;
-  } else if (k >= 0 && si == 27) {
-    float bx, by, bz;
-    sample_point(nc, nv, 13, bx, by, bz);
-    const float ax = nv.x, ay = nv.y, az = nv.z;
-    if (__float_as_uint(ax) == __float_as_uint(bx) && __float_as_uint(ay) == __float_as_uint(by) &&
-        __float_as_uint(az) == __float_as_uint(bz))
-      r = (int)(i - 14);  // the centre sample, which represents itself (an interior point)
-  }
-  __syncthreads();
-  if (local) r = s_rep[p];
-  bool uniq = false;
-  int place = 0;
   if (k >= 0) {
+    float qx, qy, qz;
+    sample_point(nc, nv, (int)(i % kQ), qx, qy, qz);
+    const long long base = 2LL * qoff[k];
+    const uint32_t m = 2u * (uint32_t)(qoff[k + 1] - qoff[k]);
+    uint32_t pos = __umulhi(hash3(qx, qy, qz), m);
+    int r = (int)i;
+    for (uint32_t t = 0; t < m; ++t) {  // the region is at most half full
+      unsigned cur = hslot[base + pos];
+      if (cur == 0u) {
+        cur = atomicCAS(hslot + base + pos, 0u, (unsigned)i + 1u);
+        if (cur == 0u) break;  // first inserter: i represents the point
+      }
+      const long long j = (long long)cur - 1;
+      const long long nj = a.lb + j / kQ;
+      float px, py, pz;
+      sample_point(nd_c[nj], nd_v[nj], (int)(j % kQ), px, py, pz);
+      if (__float_as_uint(px) == __float_as_uint(qx) && __float_as_uint(py) == __float_as_uint(qy) &&
+          __float_as_uint(pz) == __float_as_uint(qz)) {
+        r = (int)j;
+        break;
+      }
+      pos = pos + 1u == m ? 0u : pos + 1u;
+    }
     rep[i] = r;
     uniq = r == (int)i;
   }
@@ -1254,8 +1194,8 @@ static void stage_octree_vr(pi_frame* f) {
       QArgs qa{bg, P, f->iso, lb, le, ekx, eky, 0};
       PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
       exclusive_scan_i32(qcnt.p, qcnt.p, nb + 1, nullptr, f->tmp.p, s);
-      PI_LAUNCH(k_q_dedupe, div_up(qn, kGroupSlots), kGroupSlots, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p,
-                qcnt.p, hslot.p, ucnt.p, rep.p, order.p);
+      PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
+                ucnt.p, rep.p, order.p);
       int* list = reinterpret_cast<int*>(hslot.p);
       exclusive_scan_i32(ucnt.p, ucum.p, nb + 1, nullptr, f->tmp.p, s);
       PI_LAUNCH(k_q_compact, div_up(nb, 256), 256, 0, s, nb, qcnt.p, ucnt.p, ucum.p, order.p, list);
@@ -1402,8 +1342,8 @@ void stage_octree(pi_frame* f) {
       QArgs qa{g, P, f->iso, lb, le, ekx, eky, octants};
       PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
       exclusive_scan_i32(qcnt.p, qcnt.p, nb + 1, nullptr, f->tmp.p, s);
-      PI_LAUNCH(k_q_dedupe, div_up(qn, kGroupSlots), kGroupSlots, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p,
-                qcnt.p, hslot.p, ucnt.p, rep.p, order.p);
+      PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
+                ucnt.p, rep.p, order.p);
       int* list = reinterpret_cast<int*>(hslot.p);  // the hash slots are free once the samples are placed
       if (!dense) {
         exclusive_scan_i32(ucnt.p, ucum.p, nb + 1, nullptr, f->tmp.p, s);
