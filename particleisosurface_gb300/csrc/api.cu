@@ -140,6 +140,7 @@ static void fold_counters(const unsigned long long* h, unsigned long long out[kC
 }
 
 void resolve_pending(pi_frame* f) {
+  qef_join(f);
   if (!f->ev_pending && !f->pin_pending) return;
   PI_CUDA(cudaStreamSynchronize(f->ctx->stream));
   for (int k = 0; k < 8; ++k)
@@ -336,6 +337,7 @@ void check_params(const pi_params* p) {
 // Back to `stage` (0: nothing uploaded, 1: particles uploaded) with every
 // result and counter cleared; device buffers are kept for reuse.
 void frame_clear(pi_frame* f, int stage) {
+  qef_join(f);
   f->stage = stage;
   f->f64_ready = false;
   f->nNodes = f->nV = f->nT = f->nDual = 0;
@@ -430,6 +432,9 @@ int pi_ctx_create(int device, size_t budget_bytes, pi_ctx** out) {
   PI_CUDA(cudaDeviceGetAttribute(&c->smCount, cudaDevAttrMultiProcessorCount, device));
   PI_CUDA(cudaMallocHost(&c->hpin, sizeof(unsigned long long) * (size_t)kPinWords));
   PI_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  PI_CUDA(cudaStreamCreateWithFlags(&c->qef_stream, cudaStreamNonBlocking));
+  PI_CUDA(cudaEventCreateWithFlags(&c->ev_qef_in, cudaEventDisableTiming));
+  PI_CUDA(cudaEventCreateWithFlags(&c->ev_qef_done, cudaEventDisableTiming));
   c->coop_blocks = top_levels_grid(device, c->smCount);
   PI_CUDA(cudaEventCreateWithFlags(&c->ev_tris_ready, cudaEventDisableTiming));
   PI_CUDA(cudaEventCreateWithFlags(&c->ev_tris_copied, cudaEventDisableTiming));
@@ -453,6 +458,12 @@ static void ctx_release(pi_ctx* c) {
     cudaStreamSynchronize(c->copy_stream);
     cudaStreamDestroy(c->copy_stream);
   }
+  if (c->qef_stream) {
+    cudaStreamSynchronize(c->qef_stream);
+    cudaStreamDestroy(c->qef_stream);
+  }
+  if (c->ev_qef_in) cudaEventDestroy(c->ev_qef_in);
+  if (c->ev_qef_done) cudaEventDestroy(c->ev_qef_done);
   if (c->ev_tris_ready) cudaEventDestroy(c->ev_tris_ready);
   if (c->ev_tris_copied) cudaEventDestroy(c->ev_tris_copied);
   if (c->ev_read) cudaEventDestroy(c->ev_read);
@@ -596,6 +607,7 @@ int pi_frame_destroy(pi_frame* f) {
   if (!f) return PI_OK;
   pi_ctx* c = f->ctx;
   set_device(c);
+  qef_join(f);  // the frees below follow any QEF work in flight
   for (auto& e : f->ev)
     if (e) cudaEventDestroy(e);
   delete f;  // device buffers are freed on the context stream
@@ -741,7 +753,15 @@ int pi_run(pi_frame* f) {
   set_device(f->ctx);
   need(f, 1);
   const bool fresh = f->stage < 6;
-  for (int t = 2; t <= 6; ++t) run_stage(f, t);
+  // the octree's last QEF level may overlap the extraction's topology
+  f->defer_qef_join = true;
+  try {
+    for (int t = 2; t <= 6; ++t) run_stage(f, t);
+  } catch (...) {
+    f->defer_qef_join = false;
+    throw;
+  }
+  f->defer_qef_join = false;
   resolve_pending(f);
   if (fresh) metrics_record(f);
   PI_API_END

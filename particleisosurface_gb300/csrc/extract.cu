@@ -649,6 +649,12 @@ void stage_extract(pi_frame* f) {
   procs.alloc(c, s, nu > 0 ? nu : 1);
   toff.alloc(c, s, nu + 1);
   if (tmp.n < scan_tmp_ints(nu + 1)) tmp.alloc(c, s, scan_tmp_ints(nu + 1));
+  // k_dual reads the leaves' values: the octree's last QEF level, if it was
+  // left running, ends here, and the octree's counters are taken
+  if (f->qef_inflight) {
+    qef_join(f);
+    counters_snapshot(f, kPinOctree);
+  }
   counters_reset(f);
   PI_LAUNCH(k_dual, div_up(nu + 1, 128), 128, 0, s, uverts.p, nu, B, f->nd_child.p, f->nd_org.p, f->nd_v.p,
             cells.p, procs.p, toff.p, f->dcount.p);

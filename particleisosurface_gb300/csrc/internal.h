@@ -105,6 +105,11 @@ struct pi_ctx {
   // a second stream for device-to-host copies that overlap the compute
   // stream (pi_reconstruct's triangle download), and its two events
   cudaStream_t copy_stream = nullptr;
+  // the FP64 QEF of a level runs on its own stream beside the FP32 work that
+  // follows it (the next level's sampling, the mesh topology); ev_qef_in
+  // hands it the level's classification, ev_qef_done hands back the result
+  cudaStream_t qef_stream = nullptr;
+  cudaEvent_t ev_qef_in = nullptr, ev_qef_done = nullptr;
   cudaEvent_t ev_tris_ready = nullptr, ev_tris_copied = nullptr;
   cudaEvent_t ev_read = nullptr;  // the extraction's split count reads
 };
@@ -127,6 +132,11 @@ struct pi_frame {
   pisurf::DBuf<float> gfull;     // N*9, sorted order (dumps)
   pisurf::DBuf<float> det;       // N, sorted order (dumps)
   pisurf::DBuf<int8_t> f64flag;  // N, sorted order
+  // QEF work in flight on the context's QEF stream (qef_join waits for it),
+  // and whether the octree stage may leave the last level's QEF running for
+  // the extraction to overlap (pi_run, pi_reconstruct)
+  bool qef_inflight = false;
+  bool defer_qef_join = false;
   // splash particles (pi_params.splash): the flag per particle (sorted
   // order), the sorted positions of the splash particles listed in particle
   // order, and their count
@@ -257,7 +267,9 @@ void splash_mesh(pi_frame* f, long long v0, long long t0);
 int top_levels_grid(int device, int sm_count);
 // QEF vertices of the leaves of level [lb, le); scratch holds at least
 // le - lb + 1 ints (device memory the caller no longer needs).
-void qef_level(pi_frame* f, long long lb, long long le, int depth, int* scratch);
+void qef_level(pi_frame* f, long long lb, long long le, int depth);
+// The context stream waits for the QEF work in flight (no host wait).
+void qef_join(pi_frame* f);
 // UniformGrid: lattice of the loadRootBox box; sampling into d_out (device,
 // x fastest) when cap holds it; returns the number of lattice points.
 void uniform_grid_host(const pi_frame* f, float box[6], int steps[3], int dims[3]);

@@ -965,6 +965,7 @@ static int eval_config_for(pi_frame* f, int kind, const QArgs& qa, long long qn,
   pi_ctx* ctx = f->ctx;
   if (ctx->eval_forced) return ctx->eval_forced == 1 ? 0 : ctx->eval_forced == 2 ? 1 : 2;
   if (ctx->eval_cfg[kind]) return ctx->eval_cfg[kind] - 1;
+  qef_join(f);  // time the trials without the QEF stream beside them
   cudaStream_t s = ctx->stream;
   cudaEvent_t e0, e1;
   PI_CUDA(cudaEventCreate(&e0));
@@ -998,6 +999,7 @@ static void ensure_nodes(pi_frame* f, long long need) {
   const bool samp_ok = !f->P.qef || (long long)f->nd_samp.n >= need * 27;
   const bool minr_ok = !f->varR || (long long)f->nd_minr.n >= need;
   if ((long long)f->nd_c.n >= need && samp_ok && minr_ok) return;
+  qef_join(f);  // the QEF in flight writes node arrays that are about to move
   long long cap = std::max<long long>(need, (long long)(f->nd_c.n * 3 / 2) + 1024);
   pi_ctx* c = f->ctx;
   cudaStream_t s = c->stream;
@@ -1364,7 +1366,7 @@ void stage_octree(pi_frame* f) {
       PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p, f->nd_type.p,
                 f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p,
                 (const float*)nullptr);
-      if (f->P.qef) qef_level(f, lb, le, depth, qkey.p);  // the sample keys are spent (qn >= nl + 1)
+      if (f->P.qef) qef_level(f, lb, le, depth);
     }
     flag.alloc(ctx, s, nl + 1);
     if (f->tmp.n < scan_tmp_ints(nl + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(nl + 1));
@@ -1407,6 +1409,11 @@ void stage_octree(pi_frame* f) {
     lb = le;
     le = le + newn;
   }
+  // the last level's QEF may run on while the extraction builds the mesh
+  // topology (stage_extract joins it before it reads node values, and takes
+  // the octree's counters then)
+  if (f->defer_qef_join && f->qef_inflight) return;
+  qef_join(f);
   counters_snapshot(f, kPinOctree);
 }
 

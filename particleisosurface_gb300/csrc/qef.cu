@@ -398,8 +398,20 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, const int* __res
   if (qef_err) qef_err[node] = err;
 }
 
-void qef_level(pi_frame* f, long long lb, long long le, int depth, int* scratch) {
-  cudaStream_t s = f->ctx->stream;
+// On the context's QEF stream, after the level's classification on the
+// context stream: the FP64 pipe is busy with these leaves while the FP32
+// pipes run the next level's sampling (or the mesh topology after the last
+// level).  The leaf list is the QEF stream's own, allocated and freed in its
+// order.
+void qef_level(pi_frame* f, long long lb, long long le, int depth) {
+  pi_ctx* c = f->ctx;
+  cudaStream_t s = c->qef_stream;
+  PI_CUDA(cudaEventRecord(c->ev_qef_in, c->stream));
+  PI_CUDA(cudaStreamWaitEvent(s, c->ev_qef_in, 0));
+  f->qef_inflight = true;
+  DBuf<int> list;
+  list.alloc(c, s, le - lb + 1);
+  int* const scratch = list.p;
   const GridHost& gh = f->g;
   // half size of the level's nodes (the root's halved exactly per level);
   // the step of GridEval is cellsize / 2 = that half size
@@ -418,6 +430,14 @@ void qef_level(pi_frame* f, long long lb, long long le, int depth, int* scratch)
   PI_LAUNCH(k_qef, div_up(le - lb, kQefThreads), kQefThreads, 0, s, qa, scratch, f->nd_v.p, f->nd_c.p,
             f->nd_samp.p, nullptr, f->dcount.p);
   prof_end(f->ctx, s, PG_QEF);
+  list.release();
+  PI_CUDA(cudaEventRecord(c->ev_qef_done, s));
+}
+
+void qef_join(pi_frame* f) {
+  if (!f->qef_inflight) return;
+  PI_CUDA(cudaStreamWaitEvent(f->ctx->stream, f->ctx->ev_qef_done, 0));
+  f->qef_inflight = false;
 }
 
 }  // namespace pisurf
