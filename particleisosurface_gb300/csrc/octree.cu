@@ -43,8 +43,6 @@ namespace pisurf {
 enum : int8_t { T_EMPTY = 0, T_INTERNAL = 1, T_LEAF = 2, T_UNCERTAIN = 3 };
 
 constexpr int kQ = 28;  // 27 samples + the centre per node
-constexpr int kQefParts = 4;                 // parts of the leaf level with the QEF (see stage_octree)
-constexpr long long kQefSplitMin = 1 << 17;  // nodes below which the leaf level stays whole
 constexpr int kSpawnWarps = 2;  // warps per block of k_spawn_scan (small blocks: a warp that scans a whole block does not hold up seven others)
 
 struct LevelArgs {
@@ -1325,62 +1323,50 @@ void stage_octree(pi_frame* f) {
                 f->nd_c.p, f->nd_v.p, f->nd_type.p, f->dcount.p);
       prof_end(ctx, s, PG_LEAF);
     } else if (depth >= f->dmin) {
+      const long long qn = nl * kQ;
       // buckets: cell octants on the leaf level, whole cells above it
       const int octants = depth == f->dmax ? 1 : 0;
       const long long nb = octants ? ek : ek / 8;
       if (f->tmp.n < scan_tmp_ints(nb + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(nb + 1));
+      qkey.alloc(ctx, s, qn);
+      rep.alloc(ctx, s, qn);
+      hslot.alloc(ctx, s, 2 * qn);
+      qval.alloc(ctx, s, qn);
+      order.alloc(ctx, s, qn);
+      chunks.alloc(ctx, s, qn);
+      PI_CUDA(cudaMemsetAsync(qcnt.p, 0, sizeof(int) * (nb + 2), s));
+      PI_CUDA(cudaMemsetAsync(ucnt.p, 0, sizeof(int) * (nb + 1), s));
+      PI_CUDA(cudaMemsetAsync(hslot.p, 0, sizeof(unsigned) * 2 * qn, s));
       // the leaf level (node size r, samples r/2 apart) holds about 50
       // distinct samples per cell octant, the level above about 50 per cell;
       // coarser levels hold a few per cell
       const int dense = depth >= f->dmax - 1 ? 1 : 0;
-      // With the QEF the leaf level runs in parts of whole sibling groups:
-      // each part's FP64 QEF, on the QEF stream, overlaps the next part's
-      // FP32 sampling.  A lattice point shared by two parts is evaluated in
-      // each (the same value); nothing else changes.
-      const int parts = (f->P.qef && depth == f->dmax && nl >= kQefSplitMin) ? kQefParts : 1;
-      const long long pn = ((nl + parts - 1) / parts + 7) / 8 * 8;  // nodes per part
-      const long long qmax = std::min(nl, pn) * kQ;
-      qkey.alloc(ctx, s, qmax);
-      rep.alloc(ctx, s, qmax);
-      hslot.alloc(ctx, s, 2 * qmax);
-      qval.alloc(ctx, s, qmax);
-      order.alloc(ctx, s, qmax);
-      chunks.alloc(ctx, s, qmax);
-      for (long long pb = lb; pb < le; pb += pn) {
-        const long long pe = std::min(le, pb + pn), pnl = pe - pb, qn = pnl * kQ;
-        PI_CUDA(cudaMemsetAsync(qcnt.p, 0, sizeof(int) * (nb + 2), s));
-        PI_CUDA(cudaMemsetAsync(ucnt.p, 0, sizeof(int) * (nb + 1), s));
-        PI_CUDA(cudaMemsetAsync(hslot.p, 0, sizeof(unsigned) * 2 * qn, s));
-        QArgs qa{g, P, f->iso, pb, pe, ekx, eky, octants};
-        LevelArgs lap = la;
-        lap.lb = pb;
-        lap.le = pe;
-        PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
-        exclusive_scan_i32(qcnt.p, qcnt.p, nb + 1, nullptr, f->tmp.p, s);
-        PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
-                  ucnt.p, rep.p, order.p);
-        int* list = reinterpret_cast<int*>(hslot.p);  // the hash slots are free once the samples are placed
-        if (!dense) {
-          exclusive_scan_i32(ucnt.p, ucum.p, nb + 1, nullptr, f->tmp.p, s);
-          PI_LAUNCH(k_q_compact, div_up(nb, 256), 256, 0, s, nb, qcnt.p, ucnt.p, ucum.p, order.p, list);
-        }
-        int cfg = 0;
-        if (dense)
-          cfg = eval_config_for(f, depth == f->dmax ? 0 : 1, qa, qn, nb, order.p, qcnt.p, ucnt.p, chunks.p,
-                                qcnt.p + nb + 1, qval.p);
-        const int pg = dense ? PG_CHUNK : PG_THREAD;
-        prof_begin(ctx, s, pg);
-        if (dense)
-          dense_eval(f, cfg, qa, qn, nb, order.p, qcnt.p, ucnt.p, chunks.p, qcnt.p + nb + 1, qval.p, f->dcount.p);
-        else
-          PI_LAUNCH(k_q_eval_thread, (int)std::min<long long>((long long)ctx->smCount * 8, div_up(qn, 256)), 256,
-                    0, s, qa, list, ucum.p + nb, f->nd_c.p, f->nd_v.p, qval.p, f->dcount.p);
-        prof_end(ctx, s, pg);
-        PI_LAUNCH(k_classify, div_up(pnl, wpb), 32 * wpb, 0, s, lap, qval.p, rep.p, f->nd_c.p, f->nd_v.p,
-                  f->nd_type.p, f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p,
-                  (const float*)nullptr);
-        if (f->P.qef) qef_level(f, pb, pe, depth);
+      QArgs qa{g, P, f->iso, lb, le, ekx, eky, octants};
+      PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
+      exclusive_scan_i32(qcnt.p, qcnt.p, nb + 1, nullptr, f->tmp.p, s);
+      PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
+                ucnt.p, rep.p, order.p);
+      int* list = reinterpret_cast<int*>(hslot.p);  // the hash slots are free once the samples are placed
+      if (!dense) {
+        exclusive_scan_i32(ucnt.p, ucum.p, nb + 1, nullptr, f->tmp.p, s);
+        PI_LAUNCH(k_q_compact, div_up(nb, 256), 256, 0, s, nb, qcnt.p, ucnt.p, ucum.p, order.p, list);
       }
+      int cfg = 0;
+      if (dense)
+        cfg = eval_config_for(f, depth == f->dmax ? 0 : 1, qa, qn, nb, order.p, qcnt.p, ucnt.p, chunks.p,
+                              qcnt.p + nb + 1, qval.p);
+      const int pg = dense ? PG_CHUNK : PG_THREAD;
+      prof_begin(ctx, s, pg);
+      if (dense)
+        dense_eval(f, cfg, qa, qn, nb, order.p, qcnt.p, ucnt.p, chunks.p, qcnt.p + nb + 1, qval.p, f->dcount.p);
+      else
+        PI_LAUNCH(k_q_eval_thread, (int)std::min<long long>((long long)ctx->smCount * 8, div_up(qn, 256)), 256, 0,
+                  s, qa, list, ucum.p + nb, f->nd_c.p, f->nd_v.p, qval.p, f->dcount.p);
+      prof_end(ctx, s, pg);
+      PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p, f->nd_type.p,
+                f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p,
+                (const float*)nullptr);
+      if (f->P.qef) qef_level(f, lb, le, depth);
     }
     flag.alloc(ctx, s, nl + 1);
     if (f->tmp.n < scan_tmp_ints(nl + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(nl + 1));
