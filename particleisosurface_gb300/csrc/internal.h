@@ -61,9 +61,9 @@ struct GridHost {
 // Configurations of the chunked field evaluation at octree samples
 // (octree.cu): samples per lane, warps per block, staged candidates per warp.
 struct EvalConfig {
-  int K, W, CB, bulk;
+  int K, W, CB, bulk, occ;  // occ: warps per SM the register bound aims at
 };
-constexpr int kEvalConfigs = 10;
+constexpr int kEvalConfigs = 12;
 extern const EvalConfig kEvalTable[kEvalConfigs];
 
 }  // namespace pisurf
