@@ -577,7 +577,7 @@ def ours(a):
                        "triangles": qinfo["num_triangles"],
                        "samples_per_lane": dict(zip(["leaf_level", "level_above"], ctx.tuning())),
                        "eval_config": dict(zip(["leaf_level", "level_above"],
-                                               [dict(zip(["samples_per_lane", "warps_per_block", "staged_candidates", "bulk_staging", "warps_per_sm"],
+                                               [dict(zip(["samples_per_lane", "warps_per_block", "staged_candidates", "bulk_staging"],
                                                          c)) for c in ctx.tuning_config()]))},
             "field_evals_per_s": world * ev_ref / (ms / 1000.0),
             "field_evals_per_frame": {"reference_equivalent": ev_ref, "performed": ev_done,

@@ -163,15 +163,14 @@ int pi_ctx_kernel_groups(pi_ctx* ctx, int32_t ngroups, double* ms, int64_t* laun
 int pi_ctx_tune(pi_ctx* ctx, int32_t samples_per_lane);
 int pi_ctx_tuning(const pi_ctx* ctx, int32_t* out2);
 /* The whole configuration the timing chose per level kind (leaf level, level
- * above): out10 = K, warps per block, staged candidates per warp, staging
- * (0: box test from global memory, then cp.async of the survivors; 1: TMA
- * bulk copies of whole row runs, box test from shared memory), warps per SM
- * the register bound aims at, for each.  The timing runs every
- * configuration of a fixed table (pi_eval_configs() entries: K 1, 2, 4; 4,
- * 8 or 16 warps; 48, 64 or 96 staged candidates; both stagings; 16, 24 or
- * 32 warps per SM) once on the first level of each kind; pi_ctx_tune(ctx,
- * K) fixes K with 8 warps, 96 candidates and the first staging. */
-int pi_ctx_tuning_config(const pi_ctx* ctx, int32_t* out10);
+ * above): out8 = K, warps per block, staged candidates per warp, staging (0:
+ * box test from global memory, then cp.async of the survivors; 1: TMA bulk
+ * copies of whole row runs, box test from shared memory), for each.  The
+ * timing runs every configuration of a fixed table (pi_eval_configs()
+ * entries: K 1, 2, 4; 4, 8 or 16 warps; 48, 64 or 96 staged candidates; both
+ * stagings) once on the first level of each kind; pi_ctx_tune(ctx, K) fixes
+ * K with 8 warps, 96 candidates and the first staging. */
+int pi_ctx_tuning_config(const pi_ctx* ctx, int32_t* out8);
 int pi_eval_configs(void);
 /* Fixes entry `index` (0 to pi_eval_configs() - 1) of that table for both
  * level kinds; -1 returns to timing. */

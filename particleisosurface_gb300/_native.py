@@ -265,10 +265,10 @@ class Context:
         return [out[0], out[1]]
 
     def tuning_config(self):
-        """[leaf level, level above]: (K, warps per block, staged candidates, bulk staging, warps per SM)."""
-        out = (C.c_int32 * 10)()
+        """[leaf level, level above]: (K, warps per block, staged candidates, bulk staging) in use."""
+        out = (C.c_int32 * 8)()
         check(lib().pi_ctx_tuning_config(self.h, out))
-        return [tuple(out[0:5]), tuple(out[5:10])]
+        return [tuple(out[0:4]), tuple(out[4:8])]
 
     @staticmethod
     def eval_configs():

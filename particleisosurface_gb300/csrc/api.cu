@@ -573,18 +573,16 @@ int pi_ctx_tune_config(pi_ctx* c, int32_t index) {
   PI_API_END
 }
 
-int pi_ctx_tuning_config(const pi_ctx* c, int32_t* out10) {
+int pi_ctx_tuning_config(const pi_ctx* c, int32_t* out8) {
   PI_API_BEGIN
-  PI_CHECK(c && out10, "null argument");
+  PI_CHECK(c && out8, "null argument");
   for (int k = 0; k < 2; ++k) {
     int cfg = c->eval_cfg[k] - 1;
     if (c->eval_forced) cfg = c->eval_forced == 1 ? 0 : c->eval_forced == 2 ? 1 : 2;
-    const EvalConfig e = cfg >= 0 ? kEvalTable[cfg] : EvalConfig{0, 0, 0, 0, 0};
-    out10[5 * k] = e.K;
-    out10[5 * k + 1] = e.W;
-    out10[5 * k + 2] = e.CB;
-    out10[5 * k + 3] = e.bulk;
-    out10[5 * k + 4] = e.occ;
+    out8[4 * k] = cfg >= 0 ? kEvalTable[cfg].K : 0;
+    out8[4 * k + 1] = cfg >= 0 ? kEvalTable[cfg].W : 0;
+    out8[4 * k + 2] = cfg >= 0 ? kEvalTable[cfg].CB : 0;
+    out8[4 * k + 3] = cfg >= 0 ? kEvalTable[cfg].bulk : 0;
   }
   PI_API_END
 }

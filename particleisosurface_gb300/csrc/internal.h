@@ -61,9 +61,9 @@ struct GridHost {
 // Configurations of the chunked field evaluation at octree samples
 // (octree.cu): samples per lane, warps per block, staged candidates per warp.
 struct EvalConfig {
-  int K, W, CB, bulk, occ;  // occ: warps per SM the register bound aims at
+  int K, W, CB, bulk;
 };
-constexpr int kEvalConfigs = 12;
+constexpr int kEvalConfigs = 10;
 extern const EvalConfig kEvalTable[kEvalConfigs];
 
 }  // namespace pisurf

@@ -314,11 +314,10 @@ __global__ void k_q_chunks(long long nb, const int* __restrict__ ucnt, int chunk
 // shared memory and sums in candidate order.
 // Blocks of W warps, each with a staging buffer of CB candidates (static
 // shared memory W * 13 * CB floats, plus 4 KiB per warp with bulk staging,
-// at most 48 KiB); the register bound aims at OCC warps per SM whatever W
-// (32: 64 registers a thread, 24: 80, 16: 128, the last without spills).
-// BULK selects the bulk (TMA) staging of chunk_field_bulk.
-template <int K, int W, int CB, bool BULK, int OCC>
-__global__ void __launch_bounds__(32 * W, OCC / W) k_q_eval(QArgs a, const int* __restrict__ order,
+// at most 48 KiB); the register bound keeps 768 (K = 4) or 1024 threads per
+// SM whatever W.  BULK selects the bulk (TMA) staging of chunk_field_bulk.
+template <int K, int W, int CB, bool BULK>
+__global__ void __launch_bounds__(32 * W, (K > 2 ? 24 : 32) / W) k_q_eval(QArgs a, const int* __restrict__ order,
                                                             const int* __restrict__ qoff,
                                                             const int* __restrict__ ucnt,
                                                             const int2* __restrict__ chunks,
@@ -901,7 +900,7 @@ __global__ void k_root(float cx, float cy, float cz, float h, int size, float4* 
   nd_org[0] = make_int4(0, 0, 0, size);
 }
 
-template <int K, int W, int CB, bool BULK, int OCC>
+template <int K, int W, int CB, bool BULK>
 static void launch_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, const int* order, const int* qoff,
                         const int* ucnt, const int2* chunks, const int* nchunks, float* qval,
                         unsigned long long* counters) {
@@ -910,23 +909,22 @@ static void launch_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, con
   const int dev = ctx->device & 63;
   if (occ[dev][cfg] == 0) {
     int nb = 0;
-    PI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_q_eval<K, W, CB, BULK, OCC>, 32 * W, 0));
+    PI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_q_eval<K, W, CB, BULK>, 32 * W, 0));
     occ[dev][cfg] = nb > 0 ? nb : 1;
   }
   const int blocks = (int)std::min<long long>((long long)ctx->smCount * occ[dev][cfg], div_up(qn, 32 * W));
-  PI_LAUNCH((k_q_eval<K, W, CB, BULK, OCC>), blocks, 32 * W, 0, ctx->stream, qa, order, qoff, ucnt, chunks, nchunks,
+  PI_LAUNCH((k_q_eval<K, W, CB, BULK>), blocks, 32 * W, 0, ctx->stream, qa, order, qoff, ucnt, chunks, nchunks,
             f->nd_c.p, f->nd_v.p, qval, counters);
 }
 
 // The chunked evaluator's configurations: samples per lane K, warps per
-// block W, staged candidates per warp CB, bulk (TMA) staging, target warps
-// per SM of the register bound.  Index 1 (K 2, W 8, CB 96, filter then
-// cp.async, 32 warps) is the default; every configuration gives the same
-// values (each sample's sum runs over the same candidates in the same order).
-const EvalConfig kEvalTable[kEvalConfigs] = {
-    {1, 8, 96, 0, 32}, {2, 8, 96, 0, 32}, {4, 8, 96, 0, 24}, {2, 4, 96, 0, 32}, {4, 4, 96, 0, 24}, {2, 8, 64, 0, 32},
-    {4, 8, 64, 0, 24}, {2, 16, 48, 0, 32}, {2, 4, 96, 1, 32}, {4, 4, 96, 1, 24}, {4, 8, 96, 0, 16},
-    {2, 8, 96, 0, 16}};
+// block W, staged candidates per warp CB, bulk (TMA) staging.  Index 1
+// (K 2, W 8, CB 96, filter then cp.async) is the default; every
+// configuration gives the same values (each sample's sum runs over the same
+// candidates in the same order).
+const EvalConfig kEvalTable[kEvalConfigs] = {{1, 8, 96, 0}, {2, 8, 96, 0}, {4, 8, 96, 0}, {2, 4, 96, 0},
+                                             {4, 4, 96, 0}, {2, 8, 64, 0}, {4, 8, 64, 0}, {2, 16, 48, 0},
+                                             {2, 4, 96, 1}, {4, 4, 96, 1}};
 
 // Chunk list for configuration cfg, then the chunked evaluation.
 static void dense_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, long long nbuckets, const int* order,
@@ -936,23 +934,21 @@ static void dense_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, long
   const int K = kEvalTable[cfg].K;
   PI_CUDA(cudaMemsetAsync(nchunks, 0, sizeof(int), s));
   PI_LAUNCH(k_q_chunks, div_up(nbuckets, 256), 256, 0, s, nbuckets, ucnt, 32 * K, chunks, nchunks);
-#define PI_EVAL_CASE(i, k, w, cb, bulk, occ) \
-  case i:                                    \
-    launch_eval<k, w, cb, bulk, occ>(f, i, qa, qn, order, qoff, ucnt, chunks, nchunks, qval, counters); \
+#define PI_EVAL_CASE(i, k, w, cb, bulk) \
+  case i:                               \
+    launch_eval<k, w, cb, bulk>(f, i, qa, qn, order, qoff, ucnt, chunks, nchunks, qval, counters); \
     break;
   switch (cfg) {
-    PI_EVAL_CASE(0, 1, 8, 96, false, 32)
-    PI_EVAL_CASE(1, 2, 8, 96, false, 32)
-    PI_EVAL_CASE(2, 4, 8, 96, false, 24)
-    PI_EVAL_CASE(3, 2, 4, 96, false, 32)
-    PI_EVAL_CASE(4, 4, 4, 96, false, 24)
-    PI_EVAL_CASE(5, 2, 8, 64, false, 32)
-    PI_EVAL_CASE(6, 4, 8, 64, false, 24)
-    PI_EVAL_CASE(7, 2, 16, 48, false, 32)
-    PI_EVAL_CASE(8, 2, 4, 96, true, 32)
-    PI_EVAL_CASE(9, 4, 4, 96, true, 24)
-    PI_EVAL_CASE(10, 4, 8, 96, false, 16)
-    PI_EVAL_CASE(11, 2, 8, 96, false, 16)
+    PI_EVAL_CASE(0, 1, 8, 96, false)
+    PI_EVAL_CASE(1, 2, 8, 96, false)
+    PI_EVAL_CASE(2, 4, 8, 96, false)
+    PI_EVAL_CASE(3, 2, 4, 96, false)
+    PI_EVAL_CASE(4, 4, 4, 96, false)
+    PI_EVAL_CASE(5, 2, 8, 64, false)
+    PI_EVAL_CASE(6, 4, 8, 64, false)
+    PI_EVAL_CASE(7, 2, 16, 48, false)
+    PI_EVAL_CASE(8, 2, 4, 96, true)
+    PI_EVAL_CASE(9, 4, 4, 96, true)
     default:
       throw std::logic_error("unknown evaluation configuration");
   }
