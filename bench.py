@@ -77,7 +77,7 @@ def parse():
     p.add_argument("--n", "--particles", dest="n", type=int, default=1_000_000)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-sub", action="store_true", help="skip the batched and serving sub-records")
-    p.add_argument("--cpu-sample-n", type=int, default=125_000,
+    p.add_argument("--cpu-sample-n", type=int, default=250_000,
                    help="particles of the whole oracle frame timed for cpu_baseline")
     p.add_argument("--ref-budget-s", type=float, default=240.0,
                    help="--impl reference: time budget for whole oracle frames")
