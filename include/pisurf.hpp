@@ -514,6 +514,7 @@ class SurfReconstructor {
     p.smooth_factor = smooth_factor;
     p.iso_factor = iso_factor;
     p.qef = qef_ ? 1 : 0;
+    p.splash = splash_ ? 1 : 0;
     const bool var_r = !detail::const_radius_mode();
     if (var_r && !radii_.empty()) {
       float lo = radii_[0];
@@ -554,6 +555,10 @@ class SurfReconstructor {
   // Per-leaf QEF vertices (TNode::NodeCalcNode, commented out in the
   // reference at src/surface_reconstructor.cpp:258,270); off by default.
   void setQEF(bool on) { qef_ = on; }
+  // Splash particles (GlobalSplash with its marking, commented out in the
+  // reference at src/evaluator.cpp:675,690, switched on; GEN_SPLASH): the
+  // mesh gains an icosahedron per isolated particle; off by default.
+  void setSplash(bool on) { splash_ = on; }
 
   int getOverSampleQEF() const { return 2; }
   float getBorder() const { return 0.0f; }
@@ -598,6 +603,7 @@ class SurfReconstructor {
   int device_ = 0;
   std::vector<float> radii_;
   bool qef_ = false;
+  bool splash_ = false;
   int state_ = 0;
   pi_frame_info info_{};
   std::shared_ptr<detail::Frame> frame_;

@@ -183,13 +183,14 @@ class MultiLevelSearcher:
 
 class SurfReconstructor:
     def __init__(self, particles, radiuses, mesh: Mesh, radius: float, ctx: N.Context | None = None,
-                 qef: bool = False):
+                 qef: bool = False, splash: bool = False):
         self._particles = np.ascontiguousarray(np.asarray(particles, np.float32).reshape(-1, 3))
         self._radiuses = np.ascontiguousarray(np.asarray(radiuses, np.float32).reshape(-1))
         self._radius = float(radius)
         self._mesh = mesh
         self._ctx = ctx or default_context()
         self._qef = qef
+        self._splash = splash
         self._frame = None
         self._var_r = False
 
@@ -197,7 +198,8 @@ class SurfReconstructor:
         self._mesh.reset()
         var_r = not IS_CONST_RADIUS
         radius = float(self._radiuses.min()) if var_r and self._radiuses.size else self._radius
-        params = N.default_params(radius, smooth_factor=smooth_factor, iso_factor=iso_factor, qef=self._qef)
+        params = N.default_params(radius, smooth_factor=smooth_factor, iso_factor=iso_factor, qef=self._qef,
+                                  splash=self._splash)
         f = N.Frame(self._ctx, params).upload(self._particles)
         if var_r:
             f.upload_radii(self._radiuses)
