@@ -531,6 +531,50 @@ __global__ void __launch_bounds__(64, 24) k_classify(LevelArgs a, const float* _
   }
 }
 
+// k_classify for a level that needs no particle scan: its nodes are leaves
+// by size, or their curvature was summed by the parents' scan.  One thread
+// per node gathers its 28 values (independent loads in flight together)
+// instead of a warp per node; the decisions and values are k_classify's.
+__global__ void __launch_bounds__(256) k_classify_thread(LevelArgs a, const float* __restrict__ qval,
+                                                         const int* __restrict__ rep, const float4* __restrict__ nd_c,
+                                                         float4* __restrict__ nd_v, int8_t* __restrict__ nd_type,
+                                                         int8_t* __restrict__ nd_sc, float* __restrict__ nd_curv,
+                                                         float* __restrict__ nd_samp, int qef,
+                                                         unsigned long long* __restrict__ counters) {
+  const long long node = a.lb + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long evals = 0;
+  if (node < a.le && nd_type[node] == T_UNCERTAIN) {
+    const long long qb = (node - a.lb) * kQ;
+    float val[kQ];
+#pragma unroll
+    for (int q = 0; q < kQ; ++q) val[q] = qval[__ldg(rep + qb + q)];
+    // GridEval sign change against sample 0, ">= 0" (src/evaluator.cpp:169-172)
+    const bool origin = val[0] >= 0.f;
+    bool signchange = false;
+#pragma unroll
+    for (int q = 1; q < 27; ++q) signchange |= (val[q] >= 0.f) != origin;
+    if (qef)
+#pragma unroll
+      for (int q = 0; q < 27; ++q) nd_samp[node * 27 + q] = val[q];
+    const float4 c = nd_c[node];
+    const float cellsize = 2.0f * c.w;
+    const bool leaf_by_size = cellsize - a.radius < kAbove1em8;
+    int8_t type = T_LEAF;
+    if (!leaf_by_size && signchange && nd_curv[node] < kAbove099) type = T_INTERNAL;
+    nd_type[node] = type;
+    nd_sc[node] = signchange ? 1 : 0;
+    if (type == T_LEAF) {
+      float4 v = nd_v[node];
+      v.w = val[27];
+      nd_v[node] = v;
+    }
+    evals = 27 + (type == T_LEAF ? 1 : 0);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(0xffffffffu, evals, o);
+  if ((threadIdx.x & 31) == 0) stripe_add(counters, C_REF_EVALS, evals);
+}
+
 __global__ void k_internal_flag(const int8_t* __restrict__ nd_type, long long lb, long long le,
                                 int* __restrict__ flag) {
   long long i = lb + (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1364,9 +1408,13 @@ void stage_octree(pi_frame* f) {
         PI_LAUNCH(k_q_eval_thread, (int)std::min<long long>((long long)ctx->smCount * 8, div_up(qn, 256)), 256, 0,
                   s, qa, list, ucum.p + nb, f->nd_c.p, f->nd_v.p, qval.p, f->dcount.p);
       prof_end(ctx, s, pg);
-      PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p, f->nd_type.p,
-                f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p,
-                (const float*)nullptr);
+      if (known || leaf_level)  // no node needs a particle scan
+        PI_LAUNCH(k_classify_thread, div_up(nl, 256), 256, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p,
+                  f->nd_type.p, f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, f->dcount.p);
+      else
+        PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p,
+                  f->nd_type.p, f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p,
+                  (const float*)nullptr);
       if (f->P.qef) qef_level(f, lb, le, depth);
     }
     flag.alloc(ctx, s, nl + 1);
