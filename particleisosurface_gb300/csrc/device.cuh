@@ -65,18 +65,9 @@ __device__ __forceinline__ int cell_coord(float p, float lo, float cell, int n) 
   return c;
 }
 
-// cell_coord that also returns the quotient (p - lo) / cell it truncates,
-// mostly without a division: with rcell = fl(1 / cell), fl(d * rcell) is
-// within 2 ulp (relative 2.4e-7) of d / cell and fl(d / cell) within 1, so
-// where the product is farther than 1e-6 * max(1, |q|) from every integer
-// both truncate to the same cell; elsewhere (and for non-finite values) the
-// IEEE division decides.  The returned q is the product where it was
-// trusted; it only picks the octant, which needs no exactness.
-__device__ __forceinline__ int cell_coord_q(float p, float lo, float cell, float rcell, int n, float& q) {
-  const float d = __fsub_rn(p, lo);
-  q = __fmul_rn(d, rcell);
-  const float dist = fabsf(q - rintf(q));
-  if (!(dist > 1e-6f * fmaxf(1.0f, fabsf(q)))) q = __fdiv_rn(d, cell);
+// cell_coord that also returns the quotient (p - lo) / cell it truncates.
+__device__ __forceinline__ int cell_coord_q(float p, float lo, float cell, int n, float& q) {
+  q = __fdiv_rn(__fsub_rn(p, lo), cell);
   int c = (int)q;
   c = c < -2 ? -2 : c;
   c = c > n + 1 ? n + 1 : c;

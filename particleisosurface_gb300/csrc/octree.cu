@@ -170,7 +170,6 @@ struct QArgs {
   long long lb, le;
   int ekx, eky;  // extended key strides (nx + 4, ny + 4)
   int octants;   // 1: buckets are cell octants, 0: whole cells
-  float rcell;   // fl(1 / g.cell)
 };
 
 // Hash cell of a point as a key over the grid grown by 2 cells on each side
@@ -196,9 +195,9 @@ __global__ void k_q_count(QArgs a, const float4* __restrict__ nd_c, const float4
     sample_point(nd_c[node], nd_v[node], (int)(i % kQ), qx, qy, qz);
     // the cell (CalcXYZIdx) and, from the same quotients, the octant
     float fx, fy, fz;
-    const int cx = cell_coord_q(qx, a.g.b0, a.g.cell, a.rcell, a.g.nx, fx);
-    const int cy = cell_coord_q(qy, a.g.b2, a.g.cell, a.rcell, a.g.ny, fy);
-    const int cz = cell_coord_q(qz, a.g.b4, a.g.cell, a.rcell, a.g.nz, fz);
+    const int cx = cell_coord_q(qx, a.g.b0, a.g.cell, a.g.nx, fx);
+    const int cy = cell_coord_q(qy, a.g.b2, a.g.cell, a.g.ny, fy);
+    const int cz = cell_coord_q(qz, a.g.b4, a.g.cell, a.g.nz, fz);
     k = ext_key(a, cx, cy, cz);
     if (a.octants)
       k = k * 8 + ((fx - (float)cx >= 0.5f ? 1 : 0) | (fy - (float)cy >= 0.5f ? 2 : 0) |
@@ -1238,7 +1237,7 @@ static void stage_octree_vr(pi_frame* f) {
       PI_CUDA(cudaMemsetAsync(qcnt.p, 0, sizeof(int) * (nb + 2), s));
       PI_CUDA(cudaMemsetAsync(ucnt.p, 0, sizeof(int) * (nb + 1), s));
       PI_CUDA(cudaMemsetAsync(hslot.p, 0, sizeof(unsigned) * 2 * qn, s));
-      QArgs qa{bg, P, f->iso, lb, le, ekx, eky, 0, 1.0f / bg.cell};
+      QArgs qa{bg, P, f->iso, lb, le, ekx, eky, 0};
       PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
       exclusive_scan_i32(qcnt.p, qcnt.p, nb + 1, nullptr, f->tmp.p, s);
       PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
@@ -1386,7 +1385,7 @@ void stage_octree(pi_frame* f) {
       // distinct samples per cell octant, the level above about 50 per cell;
       // coarser levels hold a few per cell
       const int dense = depth >= f->dmax - 1 ? 1 : 0;
-      QArgs qa{g, P, f->iso, lb, le, ekx, eky, octants, 1.0f / g.cell};
+      QArgs qa{g, P, f->iso, lb, le, ekx, eky, octants};
       PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
       exclusive_scan_i32(qcnt.p, qcnt.p, nb + 1, nullptr, f->tmp.p, s);
       PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,

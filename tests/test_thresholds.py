@@ -48,26 +48,3 @@ def test_float_comparison_equals_promoted_comparison():
             np.testing.assert_array_equal(xs < c, xs.astype(np.float64) < d)
         else:
             np.testing.assert_array_equal(xs > c, xs.astype(np.float64) > d)
-
-
-def test_reciprocal_cell_index_agrees_with_division_where_trusted():
-    """The sample bucketing's cell index (csrc/device.cuh, cell_coord_q):
-    where fl(d * fl(1 / cell)) lies farther than 1e-6 * max(1, |q|) from
-    every integer it truncates to the cell of the IEEE quotient fl(d / cell)
-    (HashGrid::CalcXYZIdx); elsewhere the division is used.  Checked on
-    random offsets and on offsets placed next to cell boundaries."""
-    rng = np.random.default_rng(3)
-    n = 2_000_000
-    cell = (rng.uniform(0.5, 2.0, n) * 10.0 ** rng.integers(-4, 2, n)).astype(np.float32)
-    k = rng.integers(-3, 4000, n).astype(np.float64)
-    # offsets at random places and within a few ulps of a cell boundary
-    frac = np.where(rng.random(n) < 0.5, rng.random(n), rng.choice([-1, 1], n) * rng.random(n) * 1e-6)
-    d = ((k + frac) * cell.astype(np.float64)).astype(np.float32)
-    rcell = (np.float32(1.0) / cell).astype(np.float32)
-    with np.errstate(all="ignore"):
-        q = (d * rcell).astype(np.float32)
-        exact = (d / cell).astype(np.float32)
-    dist = np.abs(q - np.rint(q))
-    trusted = dist > np.float32(1e-6) * np.maximum(np.float32(1.0), np.abs(q))
-    assert trusted.mean() > 0.4 and (~trusted).sum() > 1000
-    np.testing.assert_array_equal(np.trunc(q[trusted]), np.trunc(exact[trusted]))
