@@ -138,3 +138,64 @@ def test_lattice_samples_equal_point_evaluation(ctx, n):
     bad = np.nonzero(np.any(val.view(np.uint32) != samp[pick].view(np.uint32), axis=1))[0]
     assert len(bad) == 0, (len(bad), nodes["depth"][pick[bad[:5]]])
     g.close()
+
+
+def bisect_f32(p, q, rr, eval32):
+    """The library's edge bisection (calc_vertices, src/visitorextract.cpp:
+    41-93) replayed on the host in float32 with every midpoint value from
+    pi_eval_field: float midpoints, |p - q| as sqrt(x^2 + (y^2 + z^2)) halved
+    per step, stop at length <= rr (at most 64 steps), ratio -p.w / (q.w -
+    p.w), snapped to p below 0.1 and to q above 0.9 (compared in double, as
+    the reference compares), else p + (q - p) * ratio.  p, q: (n, 4) float32
+    node points (xyz, value)."""
+    import parity as PR
+    p = np.array(p, np.float32)
+    q = np.array(q, np.float32)
+    d = PR._fnorm(p[:, 0] - q[:, 0], p[:, 1] - q[:, 1], p[:, 2] - q[:, 2])
+    rr = np.float32(rr)
+    for _ in range(64):
+        act = np.flatnonzero(d > rr)
+        if len(act) == 0:
+            break
+        m = np.empty((len(act), 4), np.float32)
+        m[:, :3] = (p[act, :3] + q[act, :3]) * np.float32(0.5)
+        m[:, 3] = eval32(np.ascontiguousarray(m[:, :3]))
+        keep_p = (m[:, 3] > 0) == (p[act, 3] > 0)
+        p[act[keep_p]] = m[keep_p]
+        q[act[~keep_p]] = m[~keep_p]
+        d[act] = d[act] * np.float32(0.5)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ratio = (np.float32(0) - p[:, 3]) / (q[:, 3] - p[:, 3])
+    v = p[:, :3] + (q[:, :3] - p[:, :3]) * ratio[:, None]
+    lo, hi = ratio.astype(np.float64) < 0.1, ratio.astype(np.float64) > 0.9
+    v[lo] = p[lo, :3]
+    v[hi] = q[hi, :3]
+    return v
+
+
+@pytest.mark.parametrize("case", ["slab_sphere_20k", "sheets_20k", "spray_splash_20k", "dam_break_1m"])
+def test_vertices_are_the_bisection_of_their_edges(ctx, case):
+    """Every surface vertex is the float bisection of its edge (the two leaf
+    points of PI_DUMP_VERTEX_EDGES) with each midpoint's value SingleEval at
+    the midpoint, i.e. pi_eval_field there, bit for bit.  At 1M particles a
+    size-independent property of the full frame."""
+    splash = case == "spray_splash_20k"
+    fr = {"slab_sphere_20k": lambda: synth.slab_and_sphere(n=20000, seed=1),
+          "sheets_20k": lambda: synth.sheets_and_filaments(n=20000, seed=9),
+          "spray_splash_20k": lambda: synth.spray_frame(n=20000, seed=23, radius=0.01),
+          "dam_break_1m": lambda: synth.dam_break(n=1_000_000, seed=2)}[case]()
+    g = N.Frame(ctx, N.default_params(fr.radius, splash=splash)).upload(fr.xyz).run()
+    nodes = g.dump(N.DUMP_NODES)["node"]
+    e = g.dump(N.DUMP_VERTEX_EDGES)
+    v = g.mesh()[0]
+    assert len(e) == len(v)
+    # splash icosahedra (appended after the surface) have no edge
+    ns = g.info()["num_splash"]
+    assert (ns > 0) == splash and np.all(e[len(e) - 12 * ns:] == -1)
+    e = e[:len(e) - 12 * ns]
+    assert len(e) > 1000 and np.all(e >= 0)
+    want = bisect_f32(nodes[e[:, 0]], nodes[e[:, 1]], np.float32(fr.radius) / np.float32(2), g.eval)
+    got = v[:len(e)]
+    bad = np.nonzero(np.any(got.view(np.uint32) != want.view(np.uint32), axis=1))[0]
+    assert len(bad) == 0, (len(bad), len(e), got[bad[:3]], want[bad[:3]])
+    g.close()
