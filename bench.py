@@ -85,7 +85,8 @@ def parse():
     p.add_argument("--samples-per-lane", type=int, default=0, choices=[0, 1, 2, 4],
                    help="with --single: fix the chunked evaluation's samples per lane (0 = timed choice)")
     p.add_argument("--eval-config", type=int, default=-1,
-                   help="with --single: fix the chunked evaluator's configuration (table index) and time it")
+                   help="fix the chunked evaluator's configuration (table index; -1 = the autotuner's choice); "
+                        "with --single also time it")
     p.add_argument("--single", action="store_true",
                    help="reconstruct one frame once and print its counters (for profiler captures)")
     p.add_argument("--workload", choices=["dam_break_1m", "batch64", "serving", "stress", "grid"],
@@ -524,6 +525,8 @@ def ours(a):
     torch.cuda.set_device(local)
     fr = make_frame(a.n)
     ctx = N.Context(local)
+    if a.eval_config >= 0:
+        ctx.tune_config(a.eval_config)
     stream = torch.cuda.ExternalStream(N.lib().pi_ctx_stream(ctx.h), device=local)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
 
@@ -545,6 +548,14 @@ def ours(a):
     qinfo = fq.info()
     e2e_ms, h2d, d2h = time_e2e(N, torch, ctx, pq, fr, qinfo, stream, flush, a.steps, a.warmup, barrier)
     e2e_ms = rank_max(e2e_ms, world)
+    # the same frame with the leaf level in one piece: the chunked evaluator
+    # and the QEF each alone on the SMs (per-kernel efficiency; the headline
+    # runs them side by side in parts)
+    qparts = ctx.qef_parts()
+    ctx.tune_qef_parts(1)
+    step1, _, groups1, _ = time_resident(N, torch, ctx, fq, stream, flush, a.steps, a.warmup, barrier, profile=True)
+    ctx.tune_qef_parts(qparts)
+    ms1 = rank_max(float(np.mean(step1)), world)
 
     # ---- the reference's active path: leaf values at cell centres, no QEF ----
     p0 = N.default_params(fr.radius)
@@ -563,6 +574,7 @@ def ours(a):
         err0 = errors_vs_fp64(N, f0, fr, qef=False)
         rq = roofline_groups(groups, a.steps, fp32_peak, fp64_peak)
         r0 = roofline_groups(groups0, a.steps, fp32_peak, fp64_peak)
+        r1 = roofline_groups(groups1, a.steps, fp32_peak, fp64_peak)
         ev_ref, ev_done = qinfo["field_evals"], qinfo["field_evals_performed"]
         line = {
             "metric": METRIC, "value": world * 1000.0 / ms, "unit": UNIT, "n_gpus": world, "steps": a.steps,
@@ -575,6 +587,7 @@ def ours(a):
                        "l2": "512 MiB buffer written between steps", "depth_max": qinfo["depth_max"],
                        "nodes": qinfo["num_nodes"], "vertices": qinfo["num_vertices"],
                        "triangles": qinfo["num_triangles"],
+                       "qef_parts": qparts,
                        "samples_per_lane": dict(zip(["leaf_level", "level_above"], ctx.tuning())),
                        "eval_config": dict(zip(["leaf_level", "level_above"],
                                                [dict(zip(["samples_per_lane", "warps_per_block", "staged_candidates", "bulk_staging"],
@@ -609,6 +622,10 @@ def ours(a):
                                               "download"], [round(x, 3) for x in info0["stage_ms"]])),
                         "roofline_groups": r0},
             "roofline_groups": rq,
+            "one_piece": {"note": "the leaf level in one piece (pi_ctx_tune_qef_parts(1)): the chunked evaluator "
+                                  "and the FP64 QEF each alone on the SMs; the headline splits it into parts and "
+                                  "runs each part's QEF beside the next part's sampling",
+                          "ms_per_step": ms1, "frames_per_s": world * 1000.0 / ms1, "roofline_groups": r1},
             "peaks": {"fp32_tflops": fp32_peak, "fp64_tflops": fp64_peak,
                       "source": "measured in this run: cuBLAS SGEMM 8192^3 (TF32 off) and DGEMM 4096^3, best of "
                                 "5 / 3 (MEASURED_PEAKS.json has HBM and bf16 figures only)"},
@@ -616,6 +633,7 @@ def ours(a):
         # dominant FP32 kernel group of the headline frame: chunked field
         # evaluation at octree samples (k_q_eval)
         dom = rq.get("chunked_sampling")
+        dom1 = r1.get("chunked_sampling")
         if dom:
             sm_mhz = ck.get("sm_max_mhz") or 2070.0
             nominal = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
@@ -626,7 +644,12 @@ def ours(a):
                                                "dram__bytes_write.sum",
                                 "peak_source": "measured in this run: cuBLAS FP32 GEMM 8192^3, TF32 off",
                                 "nominal_fp32_peak": nominal, "frac_of_nominal": dom["achieved"] / nominal,
-                                "algorithmic_work": "candidate pairs x %d flops" % FLOPS_PER_PAIR}
+                                "algorithmic_work": "candidate pairs x %d flops" % FLOPS_PER_PAIR,
+                                "frac_alone": dom1["frac"] if dom1 else None,
+                                "note": "frac: event-timed launches of the headline frame, where the leaf level's "
+                                        "parts share the SMs with the FP64 QEF (fewer evaluator blocks per SM, "
+                                        "both kernels resident); frac_alone: the same frame with the level in one "
+                                        "piece, the evaluator alone on the SMs"}
         if sub:
             fq.close()
             f0.close()

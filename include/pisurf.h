@@ -175,6 +175,16 @@ int pi_eval_configs(void);
 /* Fixes entry `index` (0 to pi_eval_configs() - 1) of that table for both
  * level kinds; -1 returns to timing. */
 int pi_ctx_tune_config(pi_ctx* ctx, int32_t index);
+/* With the QEF on, the leaf level runs in `parts` parts (1 to 64; default
+ * 16): buckets of its samples cut into z-ordered ranges of about equal
+ * sample count, each range evaluated and its nodes classified on the context
+ * stream, then those leaves' FP64 QEF solved on the context's QEF stream
+ * while the next range is evaluated (the evaluator leaves room on every SM
+ * for the QEF kernel).  1 runs the level in one piece.  The number of parts
+ * changes no result: every sample, node and vertex is the same bit for bit.
+ * pi_ctx_qef_parts reads it. */
+int pi_ctx_tune_qef_parts(pi_ctx* ctx, int32_t parts);
+int pi_ctx_qef_parts(const pi_ctx* ctx, int32_t* out);
 /* The context stream as a cudaStream_t cast to void*. */
 void* pi_ctx_stream(pi_ctx* ctx);
 

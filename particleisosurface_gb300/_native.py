@@ -84,6 +84,8 @@ def _declare(L):
         "pi_ctx_tuning": (C.c_int, [P, C.POINTER(C.c_int32)]),
         "pi_ctx_tuning_config": (C.c_int, [P, C.POINTER(C.c_int32)]),
         "pi_ctx_tune_config": (C.c_int, [P, C.c_int32]),
+        "pi_ctx_tune_qef_parts": (C.c_int, [P, C.c_int32]),
+        "pi_ctx_qef_parts": (C.c_int, [P, C.POINTER(C.c_int32)]),
         "pi_eval_configs": (C.c_int, []),
         "pi_frame_create": (C.c_int, [P, C.POINTER(Params), PP]),
         "pi_frame_destroy": (C.c_int, [P]),
@@ -277,6 +279,16 @@ class Context:
     def tune_config(self, index):
         """Fix entry `index` of the evaluation configuration table; -1 = time them."""
         check(lib().pi_ctx_tune_config(self.h, index))
+
+    def tune_qef_parts(self, parts):
+        """Parts of the leaf level pipelined against the QEF stream (QEF on);
+        1 = one piece.  Changes no result."""
+        check(lib().pi_ctx_tune_qef_parts(self.h, parts))
+
+    def qef_parts(self):
+        v = C.c_int32()
+        check(lib().pi_ctx_qef_parts(self.h, C.byref(v)))
+        return v.value
 
     def profile(self, enable=True):
         check(lib().pi_ctx_profile(self.h, 1 if enable else 0))

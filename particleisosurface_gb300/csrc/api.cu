@@ -573,6 +573,21 @@ int pi_ctx_tune_config(pi_ctx* c, int32_t index) {
   PI_API_END
 }
 
+int pi_ctx_tune_qef_parts(pi_ctx* c, int32_t parts) {
+  PI_API_BEGIN
+  PI_CHECK(c, "ctx is null");
+  PI_CHECK(parts >= 1 && parts <= kMaxQefParts, "QEF parts out of range");
+  c->qef_parts = parts;
+  PI_API_END
+}
+
+int pi_ctx_qef_parts(const pi_ctx* c, int32_t* out) {
+  PI_API_BEGIN
+  PI_CHECK(c && out, "null argument");
+  *out = c->qef_parts;
+  PI_API_END
+}
+
 int pi_ctx_tuning_config(const pi_ctx* c, int32_t* out8) {
   PI_API_BEGIN
   PI_CHECK(c && out8, "null argument");

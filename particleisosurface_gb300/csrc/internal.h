@@ -60,6 +60,8 @@ struct GridHost {
 
 // Configurations of the chunked field evaluation at octree samples
 // (octree.cu): samples per lane, warps per block, staged candidates per warp.
+constexpr int kMaxQefParts = 64;  // pi_ctx_tune_qef_parts
+
 struct EvalConfig {
   int K, W, CB, bulk;
 };
@@ -90,6 +92,7 @@ struct pi_ctx {
   // 0 = not chosen yet (timed on the first such level), forced by pi_ctx_tune
   int eval_cfg[2] = {0, 0};  // chosen configuration + 1 per dense level kind (0: not yet)
   int eval_forced = 0;
+  int qef_parts = 16;  // leaf level with the QEF on: parts pipelined against the QEF stream (1: none)
   // pinned host area for reads that need no synchronisation of their own:
   // per-stage counter snapshots (kPinSlots x kCounterWords words) and one
   // word for the hash grid's valid-key count; folded into the frame at the
@@ -183,6 +186,7 @@ struct pi_frame {
   pisurf::DBuf<float> nd_curv;
   pisurf::DBuf<int4> nd_org;     // integer origin at depth-max resolution, size
   pisurf::DBuf<float> nd_samp;   // 27 sample values per node (QEF mode)
+  pisurf::DBuf<int8_t> npart;    // leaf level in QEF mode: each node's part (read by the QEF stream too)
 
   // mesh
   long long nV = 0, nT = 0, nDual = 0;
@@ -267,7 +271,7 @@ void splash_mesh(pi_frame* f, long long v0, long long t0);
 int top_levels_grid(int device, int sm_count);
 // QEF vertices of the leaves of level [lb, le); scratch holds at least
 // le - lb + 1 ints (device memory the caller no longer needs).
-void qef_level(pi_frame* f, long long lb, long long le, int depth);
+void qef_level(pi_frame* f, long long lb, long long le, int depth, const int8_t* npart = nullptr, int part = 0);
 // The context stream waits for the QEF work in flight (no host wait).
 void qef_join(pi_frame* f);
 // UniformGrid: lattice of the loadRootBox box; sampling into d_out (device,

@@ -44,6 +44,11 @@ enum : int8_t { T_EMPTY = 0, T_INTERNAL = 1, T_LEAF = 2, T_UNCERTAIN = 3 };
 
 constexpr int kQ = 28;  // 27 samples + the centre per node
 constexpr int kSpawnWarps = 2;  // warps per block of k_spawn_scan (small blocks: a warp that scans a whole block does not hold up seven others)
+// The leaf level with the QEF on runs in pi_ctx::qef_parts parts pipelined
+// against the QEF stream; there the chunked evaluator leaves this many
+// registers per SM free for k_qef's blocks (64 threads at up to 128
+// registers: 8192 per block).
+constexpr int kQefReserveRegs = 2 * 8192;
 
 struct LevelArgs {
   GridView g;
@@ -305,6 +310,84 @@ __global__ void k_q_chunks(long long nb, const int* __restrict__ ucnt, int chunk
   for (int j = 0; j < c; ++j) chunks[base + j] = make_int2((int)k, j * chunk);
 }
 
+// The leaf level with the QEF on runs in parts, so that the FP64 QEF of one
+// part's leaves (QEF stream) overlaps the FP32 sampling of the next part
+// (context stream).  Parts are ranges of buckets (z-major cell order, then
+// the octant), cut where the exclusive scan of the per-bucket sample slots
+// qoff (qoff[nb] slots in all) crosses p / parts of the total.  pinfo holds
+// kb[0 .. parts] (first bucket of each part), pb[0 .. parts] (chunk region of
+// each part: qoff[kb[p]], since a part never has more chunks than sample
+// slots) and the chunk counts cnt[0 .. parts - 1].
+__global__ void k_part_bounds(const int* __restrict__ qoff, int nb, int parts, int* __restrict__ pinfo) {
+  const int p = threadIdx.x;
+  if (p > parts) return;
+  int k = p == parts ? nb : 0;
+  if (p > 0 && p < parts) {
+    const long long target = (long long)qoff[nb] * p / parts;
+    int lo = 0, hi = nb;  // smallest k with qoff[k] >= target
+    while (lo < hi) {
+      const int mid = (int)(((long long)lo + hi) / 2);
+      if (qoff[mid] >= target)
+        hi = mid;
+      else
+        lo = mid + 1;
+    }
+    k = lo;
+  }
+  pinfo[p] = k;
+  pinfo[parts + 1 + p] = qoff[k];
+  if (p < parts) pinfo[2 * (parts + 1) + p] = 0;
+}
+
+// Part of a bucket key (kb increasing, kb[0] = 0, kb[parts] = nb).
+__device__ __forceinline__ int part_of(const int* __restrict__ kb, int parts, int k) {
+  int p = 0;
+  while (p + 1 < parts && kb[p + 1] <= k) ++p;
+  return p;
+}
+
+// A node's part: that of its last lattice sample (the corner c + h on every
+// axis), whose bucket is the largest of the node's 28: cell coordinates and
+// octant bits grow with the coordinates, and the key orders them z, y, x,
+// then the octant's z, y, x bits.  So all of a node's samples are evaluated
+// once the parts up to its own are.  -1 for a node with no samples.
+__global__ void k_node_part(long long nl, const int* __restrict__ qkey, const int* __restrict__ pinfo, int parts,
+                            int8_t* __restrict__ npart) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nl) return;
+  const int k = qkey[t * kQ + 26];
+  npart[t] = k < 0 ? (int8_t)-1 : (int8_t)part_of(pinfo, parts, k);
+}
+
+// k_q_chunks with the chunks of part p in the region [pb[p], pb[p + 1]) of
+// the list, cnt[p] of them (one atomic per part and warp).
+__global__ void k_q_chunks_parts(long long nb, const int* __restrict__ ucnt, int chunk, int parts,
+                                 int* __restrict__ pinfo, int2* __restrict__ chunks) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int u = k < nb ? ucnt[k] : 0;
+  const int c = (u + chunk - 1) / chunk;
+  const int p = k < nb ? part_of(pinfo, parts, (int)k) : parts - 1;
+  const int* pb = pinfo + parts + 1;
+  int* cnt = pinfo + 2 * (parts + 1);
+  const unsigned peers = __match_any_sync(0xffffffffu, p);  // contiguous lanes: p grows with k
+  // inclusive sum of c over this lane's part group, in lane order
+  int incl = c;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  // the group's sums are differences of the warp's inclusive sums
+  const int leader = __ffs(peers) - 1, last = 31 - __clz(peers);
+  const int before = __shfl_sync(0xffffffffu, incl - c, leader);  // exclusive sum at the group's first lane
+  const int total = __shfl_sync(0xffffffffu, incl, last) - before;
+  int base = 0;
+  if (lane == leader && total > 0) base = atomicAdd(cnt + p, total);
+  base = __shfl_sync(0xffffffffu, base, leader) + pb[p] + incl - c - before;
+  for (int j = 0; j < c; ++j) chunks[base + j] = make_int2((int)k, j * chunk);
+}
+
 // Field at the samples of one chunk per warp (persistent, grid-stride over
 // the chunks); a chunk holds up to 32 K samples and lane l holds samples
 // l, l + 32, ..., K per lane (K, W and CB are autotuned per context, see
@@ -322,6 +405,7 @@ __global__ void __launch_bounds__(32 * W, (K > 2 ? 24 : 32) / W) k_q_eval(QArgs 
                                                             const int* __restrict__ ucnt,
                                                             const int2* __restrict__ chunks,
                                                             const int* __restrict__ nchunks_ptr,
+                                                            const int* __restrict__ cbeg_ptr,
                                                             const float4* __restrict__ nd_c,
                                                             const float4* __restrict__ nd_v,
                                                             float* __restrict__ qval,
@@ -337,10 +421,12 @@ __global__ void __launch_bounds__(32 * W, (K > 2 ? 24 : 32) / W) k_q_eval(QArgs 
     if (lane == 0) mbar_init(bs.bar);
     __syncwarp();
   }
-  const int nchunks = *nchunks_ptr;
+  // chunks [c0, c0 + count): a part of the level, or all of it from 0
+  const int c0 = cbeg_ptr ? *cbeg_ptr : 0;
+  const int cend = c0 + *nchunks_ptr;
   const int nwarps = gridDim.x * W;
   long long pairs = 0, done = 0;
-  for (int ci = blockIdx.x * W + wib; ci < nchunks; ci += nwarps) {
+  for (int ci = c0 + blockIdx.x * W + wib; ci < cend; ci += nwarps) {
     const int2 ch = chunks[ci];
     const int len = min(32 * K, __ldg(ucnt + ch.x) - ch.y);
     done += len;
@@ -539,10 +625,11 @@ __global__ void __launch_bounds__(256) k_classify_thread(LevelArgs a, const floa
                                                          float4* __restrict__ nd_v, int8_t* __restrict__ nd_type,
                                                          int8_t* __restrict__ nd_sc, float* __restrict__ nd_curv,
                                                          float* __restrict__ nd_samp, int qef,
-                                                         unsigned long long* __restrict__ counters) {
+                                                         unsigned long long* __restrict__ counters,
+                                                         const int8_t* __restrict__ npart, int part) {
   const long long node = a.lb + (long long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long evals = 0;
-  if (node < a.le && nd_type[node] == T_UNCERTAIN) {
+  if (node < a.le && (!npart || npart[node - a.lb] == part) && nd_type[node] == T_UNCERTAIN) {
     const long long qb = (node - a.lb) * kQ;
     float val[kQ];
 #pragma unroll
@@ -946,19 +1033,26 @@ __global__ void k_root(float cx, float cy, float cz, float h, int size, float4* 
 
 template <int K, int W, int CB, bool BULK>
 static void launch_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, const int* order, const int* qoff,
-                        const int* ucnt, const int2* chunks, const int* nchunks, float* qval,
-                        unsigned long long* counters) {
+                        const int* ucnt, const int2* chunks, const int* nchunks, const int* cbeg, int reserve,
+                        float* qval, unsigned long long* counters) {
   pi_ctx* ctx = f->ctx;
   static thread_local int occ[64][kEvalConfigs] = {};
+  static thread_local int regs[64][kEvalConfigs] = {};
   const int dev = ctx->device & 63;
   if (occ[dev][cfg] == 0) {
     int nb = 0;
     PI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_q_eval<K, W, CB, BULK>, 32 * W, 0));
+    cudaFuncAttributes fa;
+    PI_CUDA(cudaFuncGetAttributes(&fa, k_q_eval<K, W, CB, BULK>));
     occ[dev][cfg] = nb > 0 ? nb : 1;
+    regs[dev][cfg] = ((fa.numRegs + 7) / 8) * 8 * 32 * W;  // allocated per block: 8-register steps per thread
   }
-  const int blocks = (int)std::min<long long>((long long)ctx->smCount * occ[dev][cfg], div_up(qn, 32 * W));
+  // reserve: registers per SM left to the QEF stream's kernel
+  int per_sm = occ[dev][cfg];
+  if (reserve > 0) per_sm = std::max(1, std::min(per_sm, (65536 - reserve) / regs[dev][cfg]));
+  const int blocks = (int)std::min<long long>((long long)ctx->smCount * per_sm, div_up(qn, 32 * W));
   PI_LAUNCH((k_q_eval<K, W, CB, BULK>), blocks, 32 * W, 0, ctx->stream, qa, order, qoff, ucnt, chunks, nchunks,
-            f->nd_c.p, f->nd_v.p, qval, counters);
+            cbeg, f->nd_c.p, f->nd_v.p, qval, counters);
 }
 
 // The chunked evaluator's configurations: samples per lane K, warps per
@@ -971,16 +1065,12 @@ const EvalConfig kEvalTable[kEvalConfigs] = {{1, 8, 96, 0}, {2, 8, 96, 0}, {4, 8
                                              {2, 4, 96, 1}, {4, 4, 96, 1}};
 
 // Chunk list for configuration cfg, then the chunked evaluation.
-static void dense_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, long long nbuckets, const int* order,
-                       const int* qoff, const int* ucnt, int2* chunks, int* nchunks, float* qval,
-                       unsigned long long* counters) {
-  cudaStream_t s = f->ctx->stream;
-  const int K = kEvalTable[cfg].K;
-  PI_CUDA(cudaMemsetAsync(nchunks, 0, sizeof(int), s));
-  PI_LAUNCH(k_q_chunks, div_up(nbuckets, 256), 256, 0, s, nbuckets, ucnt, 32 * K, chunks, nchunks);
+static void eval_chunks(pi_frame* f, int cfg, const QArgs& qa, long long qn, const int* order, const int* qoff,
+                        const int* ucnt, const int2* chunks, const int* nchunks, const int* cbeg, int reserve,
+                        float* qval, unsigned long long* counters) {
 #define PI_EVAL_CASE(i, k, w, cb, bulk) \
   case i:                               \
-    launch_eval<k, w, cb, bulk>(f, i, qa, qn, order, qoff, ucnt, chunks, nchunks, qval, counters); \
+    launch_eval<k, w, cb, bulk>(f, i, qa, qn, order, qoff, ucnt, chunks, nchunks, cbeg, reserve, qval, counters); \
     break;
   switch (cfg) {
     PI_EVAL_CASE(0, 1, 8, 96, false)
@@ -997,6 +1087,16 @@ static void dense_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, long
       throw std::logic_error("unknown evaluation configuration");
   }
 #undef PI_EVAL_CASE
+}
+
+static void dense_eval(pi_frame* f, int cfg, const QArgs& qa, long long qn, long long nbuckets, const int* order,
+                       const int* qoff, const int* ucnt, int2* chunks, int* nchunks, float* qval,
+                       unsigned long long* counters) {
+  cudaStream_t s = f->ctx->stream;
+  const int K = kEvalTable[cfg].K;
+  PI_CUDA(cudaMemsetAsync(nchunks, 0, sizeof(int), s));
+  PI_LAUNCH(k_q_chunks, div_up(nbuckets, 256), 256, 0, s, nbuckets, ucnt, 32 * K, chunks, nchunks);
+  eval_chunks(f, cfg, qa, qn, order, qoff, ucnt, chunks, nchunks, nullptr, 0, qval, counters);
 }
 
 // Configuration for a dense level of the given kind: the context's choice,
@@ -1399,6 +1499,30 @@ void stage_octree(pi_frame* f) {
       if (dense)
         cfg = eval_config_for(f, depth == f->dmax ? 0 : 1, qa, qn, nb, order.p, qcnt.p, ucnt.p, chunks.p,
                               qcnt.p + nb + 1, qval.p);
+      if (dense && f->P.qef && depth == f->dmax && ctx->qef_parts > 1) {
+        // the leaf level in parts: part p's QEF beside part p + 1's sampling
+        const int parts = ctx->qef_parts;
+        DBuf<int> pinfo;
+        pinfo.alloc(ctx, s, 3 * (parts + 1));
+        // the frame's array, so that it outlives the QEF stream's reads (the
+        // QEF of this frame's coarser levels never reads it)
+        DBuf<int8_t>& npart = f->npart;
+        if (npart.n < (size_t)nl) npart.alloc(ctx, s, nl);
+        PI_LAUNCH(k_part_bounds, 1, 128, 0, s, qcnt.p, (int)nb, parts, pinfo.p);
+        PI_LAUNCH(k_node_part, div_up(nl, 256), 256, 0, s, nl, qkey.p, pinfo.p, parts, npart.p);
+        PI_LAUNCH(k_q_chunks_parts, div_up(nb, 256), 256, 0, s, nb, ucnt.p, 32 * kEvalTable[cfg].K, parts, pinfo.p,
+                  chunks.p);
+        for (int p = 0; p < parts; ++p) {
+          prof_begin(ctx, s, PG_CHUNK);
+          eval_chunks(f, cfg, qa, qn / parts, order.p, qcnt.p, ucnt.p, chunks.p, pinfo.p + 2 * (parts + 1) + p,
+                      pinfo.p + parts + 1 + p, kQefReserveRegs, qval.p, f->dcount.p);
+          prof_end(ctx, s, PG_CHUNK);
+          PI_LAUNCH(k_classify_thread, div_up(nl, 256), 256, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p,
+                    f->nd_type.p, f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, f->dcount.p,
+                    (const int8_t*)npart.p, p);
+          qef_level(f, lb, le, depth, npart.p, p);
+        }
+      } else {
       const int pg = dense ? PG_CHUNK : PG_THREAD;
       prof_begin(ctx, s, pg);
       if (dense)
@@ -1409,12 +1533,14 @@ void stage_octree(pi_frame* f) {
       prof_end(ctx, s, pg);
       if (known || leaf_level)  // no node needs a particle scan
         PI_LAUNCH(k_classify_thread, div_up(nl, 256), 256, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p,
-                  f->nd_type.p, f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, f->dcount.p);
+                  f->nd_type.p, f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, f->dcount.p,
+                  (const int8_t*)nullptr, 0);
       else
         PI_LAUNCH(k_classify, div_up(nl, wpb), 32 * wpb, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p,
                   f->nd_type.p, f->nd_sc.p, f->nd_curv.p, f->nd_samp.p, f->P.qef, known ? 1 : 0, f->dcount.p,
                   (const float*)nullptr);
       if (f->P.qef) qef_level(f, lb, le, depth);
+      }
     }
     flag.alloc(ctx, s, nl + 1);
     if (f->tmp.n < scan_tmp_ints(nl + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(nl + 1));

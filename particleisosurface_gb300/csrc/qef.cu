@@ -139,10 +139,12 @@ __device__ int ldlt4(const double A[4][4], double floor, double d[4], double id[
 // idle (on a level with few leaves most of them).  One atomic per warp;
 // list[0] counts the leaves and they follow from list[1] (each warp's in
 // node order; each leaf's result does not depend on the order).
-__global__ void k_qef_pick(const int8_t* __restrict__ nd_type, long long lb, long long le, int* __restrict__ list) {
+// With npart, only the leaves of part `part` (the leaf level in parts).
+__global__ void k_qef_pick(const int8_t* __restrict__ nd_type, long long lb, long long le,
+                           const int8_t* __restrict__ npart, int part, int* __restrict__ list) {
   const long long node = lb + (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
-  const bool leaf = node < le && nd_type[node] == Q_LEAF;
+  const bool leaf = node < le && (!npart || npart[node - lb] == part) && nd_type[node] == Q_LEAF;
   const unsigned m = __ballot_sync(0xffffffffu, leaf);
   if (m == 0u) return;  // warp-uniform
   int base = 0;
@@ -403,7 +405,7 @@ __global__ void __launch_bounds__(kQefThreads) k_qef(QefArgs a, const int* __res
 // pipes run the next level's sampling (or the mesh topology after the last
 // level).  The leaf list is the QEF stream's own, allocated and freed in its
 // order.
-void qef_level(pi_frame* f, long long lb, long long le, int depth) {
+void qef_level(pi_frame* f, long long lb, long long le, int depth, const int8_t* npart, int part) {
   pi_ctx* c = f->ctx;
   cudaStream_t s = c->qef_stream;
   PI_CUDA(cudaEventRecord(c->ev_qef_in, c->stream));
@@ -425,7 +427,7 @@ void qef_level(pi_frame* f, long long lb, long long le, int depth) {
              (double)step,
              1.0 / (double)step};
   PI_CUDA(cudaMemsetAsync(scratch, 0, sizeof(int), s));
-  PI_LAUNCH(k_qef_pick, div_up(le - lb, 256), 256, 0, s, f->nd_type.p, lb, le, scratch);
+  PI_LAUNCH(k_qef_pick, div_up(le - lb, 256), 256, 0, s, f->nd_type.p, lb, le, npart, part, scratch);
   prof_begin(f->ctx, s, PG_QEF);
   PI_LAUNCH(k_qef, div_up(le - lb, kQefThreads), kQefThreads, 0, s, qa, scratch, f->nd_v.p, f->nd_c.p,
             f->nd_samp.p, nullptr, f->dcount.p);

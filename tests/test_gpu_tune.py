@@ -86,3 +86,37 @@ def test_tune_rejects_other_values(ctx):
         with pytest.raises(N.PiError):
             ctx.tune_config(i)
     ctx.tune(0)
+
+
+@pytest.mark.parametrize("case", ["slab20k", "blob2k"])
+def test_qef_parts_change_no_result(ctx, case):
+    """The leaf level with the QEF on in 1 to 64 parts (each part's QEF on the
+    QEF stream beside the next part's sampling, pi_ctx_tune_qef_parts): nodes,
+    QEF vertices, the QEF counts and the mesh are the same bit for bit; a
+    small frame leaves most of 64 parts empty."""
+    fr = synth.slab_and_sphere(n=20000, seed=1) if case == "slab20k" else synth.small_blob(n=2000, seed=3)
+    assert ctx.qef_parts() == 16
+
+    def run(parts):
+        ctx.tune_qef_parts(parts)
+        g = N.Frame(ctx, N.default_params(fr.radius, qef=True)).upload(fr.xyz).run()
+        out = (g.dump(N.DUMP_NODES).tobytes(), g.mesh(), g.info())
+        g.close()
+        return out
+
+    ref = run(1)
+    assert ref[2]["qef_accepted"] > 0
+    for parts in (2, 3, 16, 64):
+        nodes, (v, t), info = run(parts)
+        assert nodes == ref[0], parts
+        assert np.array_equal(v, ref[1][0]) and np.array_equal(t, ref[1][1]), parts
+        assert (info["qef_accepted"], info["qef_singular"]) == (ref[2]["qef_accepted"], ref[2]["qef_singular"])
+    ctx.tune_qef_parts(16)
+
+
+def test_qef_parts_rejects_other_values(ctx):
+    for parts in (0, -1, 65):
+        with pytest.raises(N.PiError) as e:
+            ctx.tune_qef_parts(parts)
+        assert e.value.code == N.PI_ERR_INVALID
+    assert ctx.qef_parts() == 16
