@@ -87,6 +87,8 @@ def parse():
     p.add_argument("--eval-config", type=int, default=-1,
                    help="fix the chunked evaluator's configuration (table index; -1 = the autotuner's choice); "
                         "with --single also time it")
+    p.add_argument("--qef-parts", type=int, default=0,
+                   help="parts of the leaf level pipelined against the QEF stream (0 = the library's default)")
     p.add_argument("--single", action="store_true",
                    help="reconstruct one frame once and print its counters (for profiler captures)")
     p.add_argument("--workload", choices=["dam_break_1m", "batch64", "serving", "stress", "grid"],
@@ -527,6 +529,8 @@ def ours(a):
     ctx = N.Context(local)
     if a.eval_config >= 0:
         ctx.tune_config(a.eval_config)
+    if a.qef_parts > 0:
+        ctx.tune_qef_parts(a.qef_parts)
     stream = torch.cuda.ExternalStream(N.lib().pi_ctx_stream(ctx.h), device=local)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
 
@@ -871,6 +875,8 @@ def single(a):
     ctx.tune(a.samples_per_lane)
     if a.eval_config >= 0:
         ctx.tune_config(a.eval_config)
+    if a.qef_parts > 0:
+        ctx.tune_qef_parts(a.qef_parts)
     p = N.default_params(fr.radius, qef=a.qef)
     f = N.Frame(ctx, p).upload(fr.xyz).run()
     info = f.info()
