@@ -11,7 +11,7 @@
 //                monotonic in the coordinate), and they lie inside the
 //                reference's block of box +- 1 cell, so the verdict is the
 //                reference's.
-//   k_q_count /  the 27 lattice samples and the centre of every non-empty
+//   k_q_count_node / the 27 lattice samples and the centre of every non-empty
 //   k_q_dedupe   node (TNode::GenerateSampling, src/iso_method_ours.cpp:52-75)
 //                are bucketed by hash cell and octant with an atomic counting
 //                sort, and points with bit-identical coordinates (shared by
@@ -183,35 +183,87 @@ __device__ __forceinline__ int ext_key(const QArgs& a, int cx, int cy, int cz) {
   return ((cz + 2) * a.eky + (cy + 2)) * a.ekx + (cx + 2);
 }
 
-// Bucket of a sample: its hash cell (extended key), times 8 plus the octant
-// of the cell it lies in when a.octants is set, so that a chunk's points are
-// close together.  Counts come from one warp-aggregated atomic per bucket and
-// warp.
-__global__ void k_q_count(QArgs a, const float4* __restrict__ nd_c, const float4* __restrict__ nd_v,
-                          const int8_t* __restrict__ nd_type, int* __restrict__ qcnt, int* __restrict__ qkey) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
-  const long long node = a.lb + i / kQ;
-  const bool in_level = node < a.le;
-  const bool valid = in_level && nd_type[node] == T_UNCERTAIN;
-  int k = -1;
-  if (valid) {
-    float qx, qy, qz;
-    sample_point(nd_c[node], nd_v[node], (int)(i % kQ), qx, qy, qz);
-    // the cell (CalcXYZIdx) and, from the same quotients, the octant
-    float fx, fy, fz;
-    const int cx = cell_coord_q(qx, a.g.b0, a.g.cell, a.g.nx, fx);
-    const int cy = cell_coord_q(qy, a.g.b2, a.g.cell, a.g.ny, fy);
-    const int cz = cell_coord_q(qz, a.g.b4, a.g.cell, a.g.nz, fz);
-    k = ext_key(a, cx, cy, cz);
-    if (a.octants)
-      k = k * 8 + ((fx - (float)cx >= 0.5f ? 1 : 0) | (fy - (float)cy >= 0.5f ? 2 : 0) |
-                   (fz - (float)cz >= 0.5f ? 4 : 0));
+// Bucket of a sample: its hash cell (extended key, the cell of
+// CalcXYZIdx), times 8 plus the octant of the cell it lies in when a.octants
+// is set (from the same quotients), so that a chunk's points are close
+// together.  One thread per node: a sample's coordinate on an axis is one of
+// three values per node (t = 0, 1/2, 1), so the node needs 9 cell
+// coordinates and octant bits (plus 3 for its position) rather than 84; the
+// key separates by axis, so the 27 samples fall into the products of the
+// per-axis runs of equal (cell, octant), counted with one atomic per
+// distinct bucket.  The keys go through shared memory so that the block
+// writes its nodes' keys as one contiguous run.
+constexpr int kCountThreads = 128;
+__global__ void __launch_bounds__(kCountThreads) k_q_count_node(QArgs a, const float4* __restrict__ nd_c,
+                                                                const float4* __restrict__ nd_v,
+                                                                const int8_t* __restrict__ nd_type,
+                                                                int* __restrict__ qcnt, int* __restrict__ qkey) {
+  __shared__ int s_key[kCountThreads * kQ];
+  const long long t0 = (long long)blockIdx.x * kCountThreads;
+  const long long node = a.lb + t0 + threadIdx.x;
+  const long long nl = a.le - a.lb;
+  int* const mine = s_key + threadIdx.x * kQ;
+  if (node < a.le && nd_type[node] == T_UNCERTAIN) {
+    const float4 c = nd_c[node], v = nd_v[node];
+    const float h = c.w;
+    const float cc[3] = {c.x, c.y, c.z}, vv[3] = {v.x, v.y, v.z};
+    const float lo[3] = {a.g.b0, a.g.b2, a.g.b4};
+    const int n[3] = {a.g.nx, a.g.ny, a.g.nz};
+    int ck[3][4], ob[3][4];  // per axis: cell and octant bit of t = 0, 1/2, 1 and of the node position
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+      const float mn = __fsub_rn(cc[ax], h), mx = __fadd_rn(cc[ax], h);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        // sample_point's expression for t = k / 2 (k < 3), the position for k = 3
+        const float tt = k * 0.5f;
+        const float q = k < 3 ? __fadd_rn(__fmul_rn(1.0f - tt, mn), __fmul_rn(tt, mx)) : vv[ax];
+        float f;
+        ck[ax][k] = cell_coord_q(q, lo[ax], a.g.cell, n[ax], f);
+        ob[ax][k] = f - (float)ck[ax][k] >= 0.5f ? 1 : 0;
+      }
+    }
+    auto key = [&](int kx, int ky, int kz) {
+      int k = ext_key(a, ck[0][kx], ck[1][ky], ck[2][kz]);
+      if (a.octants) k = k * 8 + (ob[0][kx] | (ob[1][ky] << 1) | (ob[2][kz] << 2));
+      return k;
+    };
+#pragma unroll
+    for (int s = 0; s < 27; ++s) mine[s] = key(s % 3, (s / 3) % 3, s / 9);
+    mine[27] = key(3, 3, 3);
+    // runs of equal (cell, octant) per axis over t = 0, 1/2, 1 (both grow
+    // with t, so equal values are adjacent): a run starts at k where the
+    // value changes, and the samples whose indices all start runs carry the
+    // count of their bucket (the product of the three run lengths)
+    bool same[3][2];  // same[ax][k]: t = k / 2 and t = (k + 1) / 2 share a bucket component
+    int len[3][3];    // run length from k (counted at run starts only)
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k)
+        same[ax][k] = ck[ax][k] == ck[ax][k + 1] && (!a.octants || ob[ax][k] == ob[ax][k + 1]);
+      len[ax][0] = 1 + (same[ax][0] ? 1 + (same[ax][1] ? 1 : 0) : 0);
+      len[ax][1] = 1 + (same[ax][1] ? 1 : 0);
+      len[ax][2] = 1;
+    }
+#pragma unroll
+    for (int s = 0; s < 27; ++s) {
+      const int kx = s % 3, ky = (s / 3) % 3, kz = s / 9;
+      const bool start = (kx == 0 || !same[0][kx > 0 ? kx - 1 : 0]) && (ky == 0 || !same[1][ky > 0 ? ky - 1 : 0]) &&
+                         (kz == 0 || !same[2][kz > 0 ? kz - 1 : 0]);
+      if (start) atomicAdd(qcnt + mine[s], len[0][kx] * len[1][ky] * len[2][kz]);
+    }
+    atomicAdd(qcnt + mine[27], 1);
+  } else {
+#pragma unroll
+    for (int s = 0; s < kQ; ++s) mine[s] = -1;
   }
-  const unsigned peers = __match_any_sync(0xffffffffu, k);
-  const int leader = __ffs(peers) - 1;
-  if (valid && lane == leader) atomicAdd(qcnt + k, __popc(peers));
-  if (in_level) qkey[i] = k;
+  __syncthreads();
+  // the block's keys: slots [t0 * kQ, (t0 + its nodes) * kQ) of the level
+  const long long nodes = nl - t0 < kCountThreads ? nl - t0 : kCountThreads;
+  const int total = (int)(nodes * kQ);
+  int* const out = qkey + t0 * kQ;
+  for (int i = threadIdx.x; i < total; i += kCountThreads) out[i] = s_key[i];
 }
 
 __device__ __forceinline__ uint32_t hash3(float x, float y, float z) {
@@ -1338,7 +1390,8 @@ static void stage_octree_vr(pi_frame* f) {
       PI_CUDA(cudaMemsetAsync(ucnt.p, 0, sizeof(int) * (nb + 1), s));
       PI_CUDA(cudaMemsetAsync(hslot.p, 0, sizeof(unsigned) * 2 * qn, s));
       QArgs qa{bg, P, f->iso, lb, le, ekx, eky, 0};
-      PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
+      PI_LAUNCH(k_q_count_node, div_up(nl, kCountThreads), kCountThreads, 0, s, qa, f->nd_c.p, f->nd_v.p,
+                f->nd_type.p, qcnt.p, qkey.p);
       exclusive_scan_i32(qcnt.p, qcnt.p, nb + 1, nullptr, f->tmp.p, s);
       PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
                 ucnt.p, rep.p, order.p);
@@ -1486,7 +1539,8 @@ void stage_octree(pi_frame* f) {
       // coarser levels hold a few per cell
       const int dense = depth >= f->dmax - 1 ? 1 : 0;
       QArgs qa{g, P, f->iso, lb, le, ekx, eky, octants};
-      PI_LAUNCH(k_q_count, div_up(qn, 256), 256, 0, s, qa, f->nd_c.p, f->nd_v.p, f->nd_type.p, qcnt.p, qkey.p);
+      PI_LAUNCH(k_q_count_node, div_up(nl, kCountThreads), kCountThreads, 0, s, qa, f->nd_c.p, f->nd_v.p,
+                f->nd_type.p, qcnt.p, qkey.p);
       exclusive_scan_i32(qcnt.p, qcnt.p, nb + 1, nullptr, f->tmp.p, s);
       PI_LAUNCH(k_q_dedupe, div_up(qn, 256), 256, 0, s, qa, qn, f->nd_c.p, f->nd_v.p, qkey.p, qcnt.p, hslot.p,
                 ucnt.p, rep.p, order.p);
