@@ -141,6 +141,7 @@ static void fold_counters(const unsigned long long* h, unsigned long long out[kC
 
 void resolve_pending(pi_frame* f) {
   qef_join(f);
+  topology_join(f);
   if (!f->ev_pending && !f->pin_pending) return;
   PI_CUDA(cudaStreamSynchronize(f->ctx->stream));
   for (int k = 0; k < 8; ++k)
@@ -338,6 +339,7 @@ void check_params(const pi_params* p) {
 // result and counter cleared; device buffers are kept for reuse.
 void frame_clear(pi_frame* f, int stage) {
   qef_join(f);
+  topology_join(f);
   f->stage = stage;
   f->f64_ready = false;
   f->nNodes = f->nV = f->nT = f->nDual = 0;
@@ -433,6 +435,10 @@ int pi_ctx_create(int device, size_t budget_bytes, pi_ctx** out) {
   PI_CUDA(cudaMallocHost(&c->hpin, sizeof(unsigned long long) * (size_t)kPinWords));
   PI_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
   PI_CUDA(cudaStreamCreateWithFlags(&c->qef_stream, cudaStreamNonBlocking));
+  PI_CUDA(cudaStreamCreateWithFlags(&c->topo_stream, cudaStreamNonBlocking));
+  PI_CUDA(cudaEventCreateWithFlags(&c->ev_topo_in, cudaEventDisableTiming));
+  PI_CUDA(cudaEventCreateWithFlags(&c->ev_topo_done, cudaEventDisableTiming));
+  PI_CUDA(cudaEventCreateWithFlags(&c->ev_topo_read, cudaEventDisableTiming));
   PI_CUDA(cudaEventCreateWithFlags(&c->ev_qef_in, cudaEventDisableTiming));
   PI_CUDA(cudaEventCreateWithFlags(&c->ev_qef_done, cudaEventDisableTiming));
   c->coop_blocks = top_levels_grid(device, c->smCount);
@@ -451,6 +457,12 @@ static void ctx_release(pi_ctx* c) {
   if (c->refs.fetch_sub(1) != 1) return;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  if (c->topo_stream) {
+    cudaStreamSynchronize(c->topo_stream);
+    cudaStreamDestroy(c->topo_stream);
+  }
+  for (cudaEvent_t e : {c->ev_topo_in, c->ev_topo_done, c->ev_topo_read})
+    if (e) cudaEventDestroy(e);
   for (auto& ev : c->prof_events)
     for (auto e : ev) cudaEventDestroy(e);
   if (c->hpin) cudaFreeHost(c->hpin);
@@ -623,6 +635,7 @@ int pi_frame_destroy(pi_frame* f) {
   pi_ctx* c = f->ctx;
   set_device(c);
   qef_join(f);  // the frees below follow any QEF work in flight
+  topology_fence(f);  // and the topology stream's frees follow the context stream's work
   for (auto& e : f->ev)
     if (e) cudaEventDestroy(e);
   delete f;  // device buffers are freed on the context stream
@@ -770,13 +783,15 @@ int pi_run(pi_frame* f) {
   const bool fresh = f->stage < 6;
   // the octree's last QEF level may overlap the extraction's topology
   f->defer_qef_join = true;
+  f->extract_follows = true;
   try {
     for (int t = 2; t <= 6; ++t) run_stage(f, t);
   } catch (...) {
-    f->defer_qef_join = false;
+    f->defer_qef_join = f->extract_follows = false;
+    topology_join(f);
     throw;
   }
-  f->defer_qef_join = false;
+  f->defer_qef_join = f->extract_follows = false;
   resolve_pending(f);
   if (fresh) metrics_record(f);
   PI_API_END

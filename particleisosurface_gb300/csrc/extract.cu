@@ -561,10 +561,33 @@ static int read_int_finish(pi_frame* f) {
   return *reinterpret_cast<const int*>(f->ctx->hpin + kPinReadOffset);
 }
 
-void stage_extract(pi_frame* f) {
+// A count read on stream st through a pinned word and an event.
+struct CountReader {
+  pi_frame* f;
+  cudaStream_t st;
+  int off;
+  cudaEvent_t ev;
+  int read(const int* d) const {
+    start(d);
+    return finish();
+  }
+  void start(const int* d) const {
+    int* const h = reinterpret_cast<int*>(f->ctx->hpin + off);
+    PI_CUDA(cudaMemcpyAsync(h, d, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PI_CUDA(cudaEventRecord(ev, st));
+  }
+  int finish() const {
+    PI_CUDA(cudaEventSynchronize(ev));
+    return *reinterpret_cast<const int*>(f->ctx->hpin + off);
+  }
+};
+
+// Steps 1-2 of the extraction, the mesh topology: it reads only the tree
+// (nd_child, nd_org of the f->nNodes nodes), not the leaves' values.  Sets
+// f->nLeaves, f->tp_uverts (the unique interior leaf corners as lattice
+// keys, in Z order) and f->tp_nu.
+static void extract_topology(pi_frame* f, cudaStream_t s, const CountReader& rd) {
   pi_ctx* c = f->ctx;
-  cudaStream_t s = c->stream;
-  upload_tables(c->device);
   const long long nn = f->nNodes;
   // 1. leaves
   DBuf<int> flag, leaves, tmp;
@@ -572,16 +595,16 @@ void stage_extract(pi_frame* f) {
   tmp.alloc(c, s, scan_tmp_ints(nn * 8 + 1));
   PI_LAUNCH(k_leaf_flag, div_up(nn + 1, 256), 256, 0, s, f->nd_child.p, nn, flag.p);
   exclusive_scan_i32(flag.p, flag.p, nn + 1, nullptr, tmp.p, s);
-  read_int_start(f, flag.p + nn);
+  rd.start(flag.p + nn);
   leaves.alloc(c, s, nn > 0 ? nn : 1);  // room for every node
   PI_LAUNCH(k_leaf_list, div_up(nn, 256), 256, 0, s, f->nd_child.p, flag.p, nn, leaves.p);
-  const long long nl = read_int_finish(f);
+  const long long nl = rd.finish();
   f->nLeaves = nl;
   // 2. dual vertices = unique interior leaf corners
   const int B = f->dmax + 1;
   const int full = 1 << f->dmax;
   const long long nk = nl * 8;
-  DBuf<uint64_t> uverts;
+  DBuf<uint64_t>& uverts = f->tp_uverts;
   long long nu = 0;
   // block size: 2^bb Morton codes, bb a multiple of 3 and at least 15 (32^3
   // points, 1024 words), so that at most 2^24 blocks cover the lattice; past
@@ -602,7 +625,7 @@ void stage_extract(pi_frame* f) {
       PI_LAUNCH(k_block_mark, div_up(nk, 256), 256, 0, s, leaves.p, nl, f->nd_org.p, full, bb, used.p);
       slot.alloc(c, s, nb + 1);
       exclusive_scan_i32(used.p, slot.p, nb + 1, nullptr, tmp.p, s);
-      nused = read_int(f, slot.p + nb);
+      nused = rd.read(slot.p + nb);
       blist.alloc(c, s, nused > 0 ? nused : 1);
       PI_LAUNCH(k_block_list, div_up(nb, 256), 256, 0, s, nb, used.p, slot.p, blist.p);
     }
@@ -617,8 +640,8 @@ void stage_extract(pi_frame* f) {
               dense ? nullptr : slot.p, bits.p);
     PI_LAUNCH(k_bitmap_count, div_up(nw + 1, 256), 256, 0, s, bits.p, nw, cnt.p);
     exclusive_scan_i32(cnt.p, cnt.p, nw + 1, nullptr, tmp.p, s);
-    nu = read_int(f, cnt.p + nw);
-    uverts.alloc(c, s, nu > 0 ? nu : 1);
+    nu = rd.read(cnt.p + nw);
+    if (uverts.n < (size_t)(nu > 0 ? nu : 1)) uverts.alloc(c, s, nu > 0 ? nu : 1);
     PI_LAUNCH(k_bitmap_keys, div_up(nw, 256), 256, 0, s, bits.p, nw, cnt.p, bb, dense ? nullptr : blist.p, B,
               uverts.p);
   } else {
@@ -639,10 +662,50 @@ void stage_extract(pi_frame* f) {
     uf.alloc(c, s, nk + 1);
     PI_LAUNCH(k_unique_flag, div_up(nk + 1, 256), 256, 0, s, kp, nk, invalid, uf.p);
     exclusive_scan_i32(uf.p, uf.p, nk + 1, nullptr, tmp.p, s);
-    nu = read_int(f, uf.p + nk);
-    uverts.alloc(c, s, nu > 0 ? nu : 1);
+    nu = rd.read(uf.p + nk);
+    if (uverts.n < (size_t)(nu > 0 ? nu : 1)) uverts.alloc(c, s, nu > 0 ? nu : 1);
     PI_LAUNCH(k_unique_write, div_up(nk, 256), 256, 0, s, kp, uf.p, nk, invalid, uverts.p);
   }
+  f->tp_nu = nu;
+}
+
+void topology_start(pi_frame* f) {
+  pi_ctx* c = f->ctx;
+  cudaStream_t ts = c->topo_stream;
+  PI_CUDA(cudaStreamWaitEvent(ts, c->ev_topo_in, 0));
+  extract_topology(f, ts, CountReader{f, ts, kPinTopoReadOffset, c->ev_topo_read});
+  PI_CUDA(cudaEventRecord(c->ev_topo_done, ts));
+  f->tp_inflight = true;
+}
+
+void topology_join(pi_frame* f) {
+  if (!f->tp_inflight) return;
+  PI_CUDA(cudaStreamWaitEvent(f->ctx->stream, f->ctx->ev_topo_done, 0));
+  f->tp_inflight = false;
+}
+
+void topology_fence(pi_frame* f) {
+  topology_join(f);
+  pi_ctx* c = f->ctx;
+  PI_CUDA(cudaEventRecord(c->ev_topo_in, c->stream));
+  PI_CUDA(cudaStreamWaitEvent(c->topo_stream, c->ev_topo_in, 0));
+}
+
+void stage_extract(pi_frame* f) {
+  pi_ctx* c = f->ctx;
+  cudaStream_t s = c->stream;
+  upload_tables(c->device);
+  // steps 1-2: the topology, started beside the octree's last level or run
+  // here
+  if (f->tp_inflight)
+    topology_join(f);
+  else
+    extract_topology(f, s, CountReader{f, s, kPinReadOffset, c->ev_read});
+  const int B = f->dmax + 1;
+  const long long nu = f->tp_nu;
+  const uint64_t* const uverts = f->tp_uverts.p;
+  DBuf<int> tmp;
+  tmp.alloc(c, s, scan_tmp_ints(nu + 1));
   // 3. dual cells
   DBuf<int> cells, procs, toff;
   cells.alloc(c, s, nu * 8 > 0 ? nu * 8 : 1);
@@ -656,7 +719,7 @@ void stage_extract(pi_frame* f) {
     counters_snapshot(f, kPinOctree);
   }
   counters_reset(f);
-  PI_LAUNCH(k_dual, div_up(nu + 1, 128), 128, 0, s, uverts.p, nu, B, f->nd_child.p, f->nd_org.p, f->nd_v.p,
+  PI_LAUNCH(k_dual, div_up(nu + 1, 128), 128, 0, s, uverts, nu, B, f->nd_child.p, f->nd_org.p, f->nd_v.p,
             cells.p, procs.p, toff.p, f->dcount.p);
   exclusive_scan_i32(toff.p, toff.p, nu + 1, nullptr, tmp.p, s);
   const long long nt0 = read_int(f, toff.p + nu);
@@ -677,7 +740,6 @@ void stage_extract(pi_frame* f) {
   cells.release();
   procs.release();
   toff.release();
-  uverts.release();
   // 5. unique mesh vertices: first slot of each key, numbered in slot order
   DBuf<unsigned> vtab;
   DBuf<uint32_t> vwhere;

@@ -115,6 +115,11 @@ struct pi_ctx {
   cudaEvent_t ev_qef_in = nullptr, ev_qef_done = nullptr;
   cudaEvent_t ev_tris_ready = nullptr, ev_tris_copied = nullptr;
   cudaEvent_t ev_read = nullptr;  // the extraction's split count reads
+  // the extraction's mesh topology, started beside the octree's last level
+  // (extract_topology): its stream, the event that hands it the final tree,
+  // the one that hands back its result, and its count reads
+  cudaStream_t topo_stream = nullptr;
+  cudaEvent_t ev_topo_in = nullptr, ev_topo_done = nullptr, ev_topo_read = nullptr;
 };
 
 struct pi_frame {
@@ -140,6 +145,7 @@ struct pi_frame {
   // the extraction to overlap (pi_run, pi_reconstruct)
   bool qef_inflight = false;
   bool defer_qef_join = false;
+  bool extract_follows = false;  // pi_run: the extraction follows the octree (its topology may start early)
   // splash particles (pi_params.splash): the flag per particle (sorted
   // order), the sorted positions of the splash particles listed in particle
   // order, and their count
@@ -194,6 +200,11 @@ struct pi_frame {
   pisurf::DBuf<int> mt;          // nT*3
   pisurf::DBuf<uint64_t> mk;     // nV*2
   pisurf::DBuf<int2> vedge;      // nV: the two leaf nodes whose edge each vertex bisects (-1 for splash)
+  // the extraction's topology: unique interior leaf corners (dual vertices)
+  // as lattice keys, their count, and whether it runs on the topology stream
+  pisurf::DBuf<uint64_t> tp_uverts;
+  long long tp_nu = 0;
+  bool tp_inflight = false;
 
   // counters
   long long fieldEvals = 0, pairs = 0, bisectEvals = 0, fp64Count = 0, nLeaves = 0, nEmpty = 0;
@@ -224,9 +235,10 @@ constexpr int kPinValid = kPinSlots;  // bit of pin_pending for the valid-key co
 // INTERNAL count; then the coarse-level kernel's level starts and depth
 constexpr int kPinTopOffset = kPinSlots * kCounterWords + 8;
 constexpr int kPinTopWords = 32;
-// one word for the extraction's split count reads
+// one word for the extraction's split count reads, one for the topology's
 constexpr int kPinReadOffset = kPinTopOffset + kPinTopWords;
-constexpr int kPinWords = kPinReadOffset + 8;
+constexpr int kPinTopoReadOffset = kPinReadOffset + 8;
+constexpr int kPinWords = kPinTopoReadOffset + 8;
 // event that marks the INTERNAL count's copy in the octree level loop
 constexpr int kLevelEvent = 16;
 // Copies the frame's device counters into pinned slot `slot` (stream-ordered,
@@ -274,6 +286,14 @@ int top_levels_grid(int device, int sm_count);
 void qef_level(pi_frame* f, long long lb, long long le, int depth, const int8_t* npart = nullptr, int part = 0);
 // The context stream waits for the QEF work in flight (no host wait).
 void qef_join(pi_frame* f);
+// The extraction's topology on the topology stream, after the context
+// stream's ev_topo_in (the caller records it where the tree is final);
+// topology_join makes the context stream wait for it; topology_fence also
+// orders the topology stream after the context stream's work so far (before
+// frees of buffers it allocated).
+void topology_start(pi_frame* f);
+void topology_join(pi_frame* f);
+void topology_fence(pi_frame* f);
 // UniformGrid: lattice of the loadRootBox box; sampling into d_out (device,
 // x fastest) when cap holds it; returns the number of lattice points.
 void uniform_grid_host(const pi_frame* f, float box[6], int steps[3], int dims[3]);

@@ -1511,6 +1511,15 @@ void stage_octree(pi_frame* f) {
     // every node of the level has half size rootH / 2^depth (children halve exactly)
     const float cell_d = 2.0f * std::ldexp(f->rootH, -depth);
     const bool leaf_level = (double)(cell_d - f->P.radius) < 1e-8;
+    // every non-empty node of a sampled leaf-by-size level becomes a leaf
+    // (afterSampleEval returns before any INTERNAL test), so the tree is
+    // final now: nothing spawns below this level.  Without the QEF the
+    // extraction's topology, which reads only the tree, starts beside the
+    // level's field values when the extraction follows; with the QEF it is
+    // better left to run beside the last part's QEF at the extraction's start
+    const bool last = depth >= f->dmin && leaf_level;
+    const bool topo_early = last && f->extract_follows && !f->P.qef;
+    if (topo_early) PI_CUDA(cudaEventRecord(ctx->ev_topo_in, s));
     const int wpb = 2;  // warps per block of the warp-per-node kernels (small blocks: uneven warps free their SM slots sooner)
     if (!known)
       PI_LAUNCH(k_empty, div_up(nl, wpb), 32 * wpb, 0, s, la, f->nd_c.p, f->nd_v.p, f->nd_type.p, f->nd_curv.p);
@@ -1595,6 +1604,11 @@ void stage_octree(pi_frame* f) {
                   (const float*)nullptr);
       if (f->P.qef) qef_level(f, lb, le, depth);
       }
+    }
+    if (last) {
+      f->nNodes = le;
+      if (topo_early) topology_start(f);
+      break;
     }
     flag.alloc(ctx, s, nl + 1);
     if (f->tmp.n < scan_tmp_ints(nl + 1)) f->tmp.alloc(ctx, s, scan_tmp_ints(nl + 1));
