@@ -199,3 +199,25 @@ def test_vertices_are_the_bisection_of_their_edges(ctx, case):
     bad = np.nonzero(np.any(got.view(np.uint32) != want.view(np.uint32), axis=1))[0]
     assert len(bad) == 0, (len(bad), len(e), got[bad[:3]], want[bad[:3]])
     g.close()
+
+
+@pytest.mark.parametrize("case", ["slab_sphere_20k", "dam_break_1m"])
+@pytest.mark.parametrize("qef", [False, True])
+def test_run_and_staged_calls_give_the_same_mesh(ctx, case, qef):
+    """pi_run starts the extraction's topology (leaf list, unique corners) on
+    its own stream beside the octree's last level when the QEF is off; the
+    staged calls (pi_octree_build, then pi_extract_mesh) run it inside the
+    extraction.  Nodes and mesh are the same bit for bit either way."""
+    fr = (synth.slab_and_sphere(n=20000, seed=1) if case == "slab_sphere_20k"
+          else synth.dam_break(n=1_000_000, seed=2))
+    p = N.default_params(fr.radius, qef=qef)
+    a = N.Frame(ctx, p).upload(fr.xyz).run()
+    b = N.Frame(ctx, p).upload(fr.xyz).hashgrid().aniso().normals()
+    b.octree()
+    b.extract()
+    assert a.dump(N.DUMP_NODES).tobytes() == b.dump(N.DUMP_NODES).tobytes()
+    for x, y in zip(a.mesh(keys=True), b.mesh(keys=True)):
+        assert np.array_equal(x, y)
+    assert a.info()["num_leaves"] == b.info()["num_leaves"] > 0
+    a.close()
+    b.close()
