@@ -1577,7 +1577,9 @@ void stage_octree(pi_frame* f) {
                   chunks.p);
         for (int p = 0; p < parts; ++p) {
           prof_begin(ctx, s, PG_CHUNK);
-          eval_chunks(f, cfg, qa, qn / parts, order.p, qcnt.p, ucnt.p, chunks.p, pinfo.p + 2 * (parts + 1) + p,
+          // the grid is sized by the level (a part may hold fewer slots than
+          // it has parts, and the blocks stride over the part's chunks)
+          eval_chunks(f, cfg, qa, qn, order.p, qcnt.p, ucnt.p, chunks.p, pinfo.p + 2 * (parts + 1) + p,
                       pinfo.p + parts + 1 + p, kQefReserveRegs, qval.p, f->dcount.p);
           prof_end(ctx, s, PG_CHUNK);
           PI_LAUNCH(k_classify_thread, div_up(nl, 256), 256, 0, s, la, qval.p, rep.p, f->nd_c.p, f->nd_v.p,

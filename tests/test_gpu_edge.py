@@ -175,3 +175,23 @@ def test_metrics_record_per_frame(tmp_path):
     assert len(lines) == 2
     assert lines[0]["triangles"] == int(r.stdout.strip().splitlines()[-1]) == lines[1]["triangles"]
     assert lines[0]["particles"] == 2000 and lines[0]["stage_ms"]["octree"] > 0
+
+
+@pytest.mark.parametrize("name", ["one", "coincident", "line", "sheet"])
+def test_degenerate_frame_qef_parts(ctx, name):
+    """With the QEF on, a leaf level of a few nodes split into 64 parts (most
+    of them empty) gives the nodes, QEF vertices and mesh of the level in one
+    piece."""
+    xyz = CASES[name]()
+    p = N.default_params(0.01, qef=True)
+    out = []
+    for parts in (1, 64):
+        ctx.tune_qef_parts(parts)
+        g = N.Frame(ctx, p).upload(xyz).run()
+        out.append((g.dump(N.DUMP_NODES).tobytes(), g.mesh(keys=True), g.info()["qef_accepted"]))
+        g.close()
+    ctx.tune_qef_parts(16)
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a, b)
+    assert out[0][2] == out[1][2]
