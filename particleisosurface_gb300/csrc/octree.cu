@@ -9,7 +9,7 @@
 //                r * smooth_factor touches.  Every particle strictly inside
 //                the grown box lies in those cells (the float cell index is
 //                monotonic in the coordinate), and they lie inside the
-//                reference's block of box +- 1 cell, so the verdict is the
+//                reference's block of box +- 1 cell, so the decision is the
 //                reference's.
 //   k_q_count_node / the 27 lattice samples and the centre of every non-empty
 //   k_q_dedupe   node (TNode::GenerateSampling, src/iso_method_ours.cpp:52-75)
